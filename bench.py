@@ -1,0 +1,321 @@
+#!/usr/bin/env python3
+"""Benchmark: MG-CFD multigrid V-cycles on the 8M-node synthetic mesh.
+
+Workload: 200^3 jittered lattice (8,000,000 nodes, 23,880,000 edges, 240,000
+boundary entries on level 0), 4 multigrid levels (200^3, 100^3, 50^3, 25^3),
+Mach 0.8, angle of attack 3 degrees, FP64.  One step = one V-cycle
+(euler3d.cpp:458-641: 6 smoothing steps, 18 edge-flux sweeps).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                  [--precision fp64|mixed] [--increment atomic|gather] [--n 200]
+
+Prints one JSON line.  `value` is V-cycles/s with the mesh resident in HBM,
+`e2e` is V-cycles/s through the host-buffer entry point mgcfd_solve (mesh
+upload, setup, 25 V-cycles, download of every level's state), and `roofline`
+describes the level-0 edge-flux kernel.  --impl reference times the CPU
+restatement of the reference path (OpenMP, all host threads) on the same
+mesh.  Under torchrun each rank runs an independent replica (the solve does
+not shard across GPUs); value is the sum over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "mg-cfd-app-op2_gb300"))
+
+MACH, AOA, NLEVELS, SEED = 0.8, 3.0, 4, 20240501
+E2E_CYCLES = 25
+
+
+def algorithmic_flux_bytes(nnodes: int, nedges: int) -> int:
+    """Per level-0 flux sweep: 24 B weights + 8 B map per edge; 80 B state
+    read, 40 B flux read and 40 B flux written per node."""
+    return 32 * nedges + 120 * nnodes
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def committed_profile(name):
+    p = ROOT / "profiles" / name
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except json.JSONDecodeError:
+            return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait(timeout=10)
+
+    def summary(self):
+        rows = []
+        if self.path and os.path.exists(self.path):
+            for line in open(self.path):
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+            os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_gb300(args):
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    import mgcfd
+    from mgcfd import _lib
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+
+    mesh = mgcfd.HostMesh.generate(args.n, NLEVELS, SEED)
+    L0 = mesh.level(0)
+    N, E = L0.nnodes, L0.nedges
+    solver = mgcfd.Solver(mesh, MACH, AOA, precision=args.precision, increment=args.increment,
+                          renumber=args.renumber, time_kernels=True)
+    solver.run(args.warmup)
+    if solver.synchronize() != 0:
+        raise RuntimeError(_lib.load().mgcfd_last_error().decode())
+    st0 = solver.stats()
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        t0 = time.perf_counter()
+        solver.run(args.steps)
+        status = solver.synchronize()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+    barrier()
+    if status != 0:
+        raise RuntimeError(_lib.load().mgcfd_last_error().decode())
+    st1 = solver.stats()
+    elapsed = t1 - t0
+    if dist:
+        t = torch.tensor([elapsed], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    flux_ms = (st1.flux_ms_l0 - st0.flux_ms_l0) / max(1, st1.flux_sweeps_l0 - st0.flux_sweeps_l0)
+    launches = int(st1.kernel_launches - st0.kernel_launches)
+    solver.close()
+
+    # End to end through the host-buffer entry point, pinned host memory.
+    levels = mesh.levels()
+    pinned = []
+
+    def pin(a):
+        t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+        pinned.append(t)
+        return t.numpy()
+
+    hl = [mgcfd.Level(coords=pin(L.coords), edge_to_nodes=pin(L.edge_to_nodes), bnd_to_node=pin(L.bnd_to_node),
+                      bnd_group=pin(L.bnd_group), edge_weights=pin(L.edge_weights), bnd_weights=pin(L.bnd_weights),
+                      node_to_mg=pin(L.node_to_mg) if L.node_to_mg is not None else None) for L in levels]
+    outs = [torch.empty((L.nnodes, 5), dtype=torch.float64).pin_memory() for L in levels]
+    views = mgcfd.level_views_from_arrays(hl)
+    out_ptrs = (_lib.c_double_p * len(outs))(*[C.cast(o.data_ptr(), _lib.c_double_p) for o in outs])
+    opts = mgcfd.options(precision=args.precision, increment=args.increment, renumber=args.renumber)
+    lib = _lib.load()
+    h2d = sum(a.nbytes for L in hl for a in (L.coords, L.edge_to_nodes, L.bnd_to_node, L.bnd_group, L.edge_weights,
+                                              L.bnd_weights) + ((L.node_to_mg,) if L.node_to_mg is not None else ()))
+    d2h = sum(o.numel() * 8 for o in outs)
+    _lib.check(lib.mgcfd_solve(len(hl), views, MACH, AOA, 1, C.byref(opts), out_ptrs))  # warm-up
+    e2e_steps = max(1, min(args.steps, args.e2e_steps))
+    barrier()
+    te0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        _lib.check(lib.mgcfd_solve(len(hl), views, MACH, AOA, E2E_CYCLES, C.byref(opts), out_ptrs))
+    te1 = time.perf_counter()
+    barrier()
+    e2e_elapsed = te1 - te0
+    if dist:
+        t = torch.tensor([e2e_elapsed], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_elapsed = float(t.item())
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(levels, args.cpu_cycles)
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    peak, peak_kind = measured_peaks()
+    bytes_per_sweep = algorithmic_flux_bytes(N, E)
+    achieved = bytes_per_sweep / (flux_ms * 1e-3) / 1e9
+    prof = committed_profile(f"flux_edge_{args.precision}_{args.increment}.json") or {}
+    traffic = prof.get("dram_bytes_per_launch_scaled_to_bench")
+    value = world * args.steps / elapsed
+    line = {
+        "metric": "MG V-cycles/s at 8M nodes (200^3, 4 levels)",
+        "value": round(value, 3),
+        "unit": "cycles/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(1e3 * elapsed / args.steps, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f32-flux/f64-accumulate",
+        "data": "synthetic: seeded jittered 200^3 lattice, permuted ids (SURVEY 8d generator)",
+        "config": {"workload": f"{args.n}^3 jittered lattice, {NLEVELS} levels, Mach {MACH}, AoA {AOA} deg, "
+                               f"{N} nodes / {E} edges on level 0",
+                   "precision": args.precision, "increment": args.increment, "renumber": args.renumber,
+                   "l2": "inputs larger than L2 (level-0 state and edges ~2.4 GB), no flush",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "kernel": "k_flux (level-0 edge flux sweep)", "flux_ms_per_launch": round(flux_ms, 4),
+                     "algorithmic_bytes_per_launch": bytes_per_sweep, "peak_source": peak_kind,
+                     "fp64": prof.get("fp64")},
+        "e2e": {"value": round(world * e2e_steps * E2E_CYCLES / e2e_elapsed, 3), "unit": "cycles/s",
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "step": f"mgcfd_solve: upload mesh, setup, {E2E_CYCLES} V-cycles, download all levels",
+                "steps": e2e_steps},
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def cpu_baseline(levels, cycles):
+    """The oracle restatement with OpenMP on every host core, timed on a
+    bounded sample (a few V-cycles of the same mesh)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+    threads = os.cpu_count() or 1
+    run = O.OracleRun(levels)
+    run.run(MACH, AOA, 1, nthreads=threads)  # warm-up: colouring, page faults
+    st, secs = run.run(MACH, AOA, cycles, nthreads=threads)
+    run.close()
+    return {"value": round(cycles / secs, 4), "unit": "cycles/s", "cores": threads, "kind": "port",
+            "sample": f"{cycles} V-cycles of the same 8M-node 4-level mesh, OpenMP over coloured edges"}
+
+
+def run_reference(args):
+    world, rank, local = dist_setup()
+    if rank != 0:
+        return
+    import mgcfd
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+    mesh = mgcfd.HostMesh.generate(args.n, NLEVELS, SEED)
+    levels = mesh.levels()
+    threads = os.cpu_count() or 1
+    run = O.OracleRun(levels)
+    run.run(MACH, AOA, args.warmup, nthreads=threads)
+    st, secs = run.run(MACH, AOA, args.steps, nthreads=threads)
+    value = args.steps / secs
+    L0 = levels[0]
+    line = {
+        "impl": "reference",
+        "metric": "MG V-cycles/s at 8M nodes (200^3, 4 levels)",
+        "value": round(value, 4), "unit": "cycles/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(1e3 * secs / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded jittered 200^3 lattice, permuted ids",
+        "config": {"workload": f"{args.n}^3 jittered lattice, {NLEVELS} levels, Mach {MACH}, AoA {AOA} deg, "
+                               f"{L0.nnodes} nodes / {L0.nedges} edges on level 0",
+                   "implementation": "CPU restatement of the reference path (oracle/mgcfd_oracle.c), OpenMP"},
+        "cpu_baseline": {"value": round(value, 4), "unit": "cycles/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} V-cycles after {args.warmup} warm-up cycles"},
+        "e2e": {"value": round(value, 4), "unit": "cycles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "status": st,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--increment", default="atomic", choices=["atomic", "gather"])
+    ap.add_argument("--renumber", default="spatial", choices=["none", "spatial", "rcm"])
+    ap.add_argument("--n", type=int, default=200)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-cycles", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 0 or args.steps < 1:
+        ap.error("need --steps >= 1 and --warmup >= 0")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,261 @@
+/*
+ * mgcfd_gb300 -- C ABI of the GB300-native MG-CFD multigrid Euler hot path.
+ *
+ * Reference: warwick-hpsc/MG-CFD-app-OP2.  In the reference every step of the
+ * V-cycle is an OP2 parallel loop,
+ *     op_par_loop(kernel, "name", set, op_arg_dat(...), ...)
+ * over an elemental kernel with plain pointer arguments (for example
+ * compute_flux_edge_kernel, flux.h:41-46).  OP2's code generator turns each
+ * such call into a backend-specific host stub.  This library is what such a
+ * stub binds to on GB300:
+ *
+ *   1. Per-loop entry points (mgcfd_op_*), one per op_par_loop of the hot
+ *      path.  Arguments are device pointers to arrays in exactly the layout
+ *      of the OP2 dats and maps they replace (row-major [set size][dim],
+ *      0-based int32 maps), the set size, and the CUDA stream (cudaStream_t
+ *      passed as void*, NULL = default stream).  The call enqueues work and
+ *      returns; increments land in unspecified order (FP64 atomics), so
+ *      sums differ from OP2's sequential order only by rounding.  Mapped
+ *      loops also take the size of the set the map points into; an element
+ *      whose map entry is out of range is skipped and counted (see
+ *      mgcfd_op_map_errors) instead of being dereferenced.
+ *   2. A device-resident solver (mgcfd_solver_*) that owns a whole multigrid
+ *      mesh in HBM and runs complete V-cycles (euler3d.cpp:452-641) with
+ *      renumbered, fused kernels and no host synchronisation inside a cycle.
+ *   3. Host helpers: synthetic meshes, the input.dat + HDF5 mesh layout
+ *      (euler3d.cpp:243-336, io.h:28-205) and the far-field state
+ *      (euler3d.cpp:157-189).
+ *
+ * Conventions: every function returns an int status (MGCFD_OK = 0); no C++
+ * exception crosses the ABI; mgcfd_last_error() gives a message for the last
+ * failure on the calling thread.  The reference prints and exits where this
+ * library returns MGCFD_ERR_NEGATIVE_DT (euler3d.cpp:480-484) or
+ * MGCFD_ERR_BAD_VALUES (euler3d.cpp:539-548).
+ */
+#ifndef MGCFD_GB300_H
+#define MGCFD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MGCFD_ABI_VERSION 1
+
+enum {
+  MGCFD_OK = 0,
+  MGCFD_ERR_INVALID = 1,      /* bad argument, size or call order */
+  MGCFD_ERR_CUDA = 2,         /* CUDA runtime error (message in mgcfd_last_error) */
+  MGCFD_ERR_NOMEM = 3,        /* host or device allocation failed */
+  MGCFD_ERR_IO = 4,           /* file missing, unreadable or malformed */
+  MGCFD_ERR_NEGATIVE_DT = 5,  /* min_dt < 0 (euler3d.cpp:480-484) */
+  MGCFD_ERR_BAD_VALUES = 6,   /* NaN/Inf in level-0 variables (euler3d.cpp:539-548) */
+  MGCFD_ERR_TIMEOUT = 7,      /* a bounded device-side wait gave up */
+  MGCFD_ERR_BUDGET = 8        /* request exceeds the configured HBM budget */
+};
+
+int mgcfd_abi_version(void);
+const char* mgcfd_status_string(int status);
+const char* mgcfd_last_error(void);
+
+/* ------------------------------------------------------------------------ */
+/* Far-field state: global.h:4-14 values computed as euler3d.cpp:157-189,   */
+/* with Mach and angle of attack (degrees) as run-time inputs (the          */
+/* reference fixes them in const.h:32-33 at 1.2 and 0.0).                   */
+typedef struct mgcfd_freestream {
+  double smoothing_coefficient;                 /* euler3d.cpp:47: double(0.2f) */
+  double ff_variable[5];
+  double ff_flux_contribution_momentum_x[3];
+  double ff_flux_contribution_momentum_y[3];
+  double ff_flux_contribution_momentum_z[3];
+  double ff_flux_contribution_density_energy[3];
+} mgcfd_freestream;
+
+int mgcfd_freestream_init(double mach, double aoa_deg, mgcfd_freestream* out);
+
+/* ------------------------------------------------------------------------ */
+/* Host meshes.                                                             */
+typedef struct mgcfd_level_view {
+  int32_t nnodes, nedges, nbnd, n_axis;  /* n_axis: lattice size for synthetic meshes, else 0 */
+  const double* coords;         /* [nnodes][3]  "node_coordinates"   */
+  const int32_t* edge_to_nodes; /* [nedges][2]  "edge-->node", 0-based */
+  const int32_t* bnd_to_node;   /* [nbnd]       "bnd_node-->node"    */
+  const int32_t* bnd_group;     /* [nbnd]       "bnd_node-->group"   */
+  const double* edge_weights;   /* [nedges][3]  "edge_weights"       */
+  const double* bnd_weights;    /* [nbnd][3]    "bnd_node_weights"   */
+  const int32_t* node_to_mg;    /* [nnodes]     "node-->mg_node" (NULL on the coarsest level) */
+  const double* volumes;        /* [nnodes] legacy-mode dual volumes ("areas", euler3d.cpp:292-299);
+                                   NULL = compute them from the edges (euler3d.cpp:416-431) */
+} mgcfd_level_view;
+
+typedef struct mgcfd_host_mesh mgcfd_host_mesh;
+
+/* Seeded jittered-lattice mesh (n^3 nodes on level 0, `nlevels` levels). */
+int mgcfd_host_mesh_generate(int n, int nlevels, uint64_t seed, mgcfd_host_mesh** out);
+/* Read an input.dat deck (io.h:28-205 semantics, base_array_index default 1)
+ * and its per-level HDF5 files; input_dir may be NULL or "" (euler3d.cpp:84-100).
+ * legacy_mode selects the ".renumbered"/"edge_weights.recalculated"/"areas"
+ * datasets of euler3d.cpp:247-309; legacy volumes are used as read and the
+ * edge weights are not re-oriented (euler3d.cpp:416-431 is skipped). */
+int mgcfd_host_mesh_load(const char* input_file, const char* input_dir, int legacy_mode,
+                         mgcfd_host_mesh** out);
+/* Write "<dir>/<prefix>L<l>.h5" per level and "<dir>/input.dat". */
+int mgcfd_host_mesh_write(const mgcfd_host_mesh* mesh, const char* dir, const char* prefix);
+int mgcfd_host_mesh_num_levels(const mgcfd_host_mesh* mesh);
+/* Views stay valid until the mesh is destroyed. */
+int mgcfd_host_mesh_level(const mgcfd_host_mesh* mesh, int level, mgcfd_level_view* out);
+void mgcfd_host_mesh_destroy(mgcfd_host_mesh* mesh);
+
+/* HDF5 subset used by the reference's files (op_decl_*_hdf5 and
+ * op_fetch_data_hdf5_file in euler3d.cpp).  dims receives up to 2 extents. */
+int mgcfd_h5_dataset_shape(const char* path, const char* name, int64_t dims[2], int* rank);
+int mgcfd_h5_read_f64(const char* path, const char* name, double* out, int64_t nelems);
+int mgcfd_h5_read_i32(const char* path, const char* name, int32_t* out, int64_t nelems);
+/* Writes a new file holding one [rows][cols] float64 dataset with OP2's
+ * "size"/"dim"/"type" attributes (the op_fetch_data_hdf5_file layout). */
+int mgcfd_h5_write_f64(const char* path, const char* name, const double* data, int64_t rows, int64_t cols);
+
+/* ------------------------------------------------------------------------ */
+/* Per-loop drop-in entry points (device pointers, OP2 dat layout).         */
+/* Each replaces one op_par_loop of euler3d.cpp; the elemental kernel it    */
+/* implements is cited.                                                     */
+
+/* initialize_variables_kernel, misc.h:10-16; loop euler3d.cpp:414-415. */
+int mgcfd_op_initialize_variables(int32_t nnodes, const mgcfd_freestream* ff, double* variables, void* stream);
+/* zero_5d/3d/1d_array_kernel, misc.h:18-38; euler3d.cpp:416-424. */
+int mgcfd_op_zero(int32_t n, int32_t dim, double* array, void* stream);
+/* calculate_cell_volumes, misc.h:40-76; euler3d.cpp:425-431 (edge weights OP_RW,
+ * volumes OP_INC). */
+int mgcfd_op_calculate_cell_volumes(int32_t nedges, int32_t nnodes, const int32_t* edge_to_nodes,
+                                    const double* coords, double* edge_weights, double* volumes, void* stream);
+/* dampen_ewt, misc.h:78-84; euler3d.cpp:436-441 (n elements of dim 3). */
+int mgcfd_op_dampen_ewt(int32_t n, double* weights, void* stream);
+/* copy_double_kernel, copy_double_kernel.h:6-13; euler3d.cpp:467-469. */
+int mgcfd_op_copy_double(int32_t nnodes, const double* variables, double* old_variables, void* stream);
+/* calculate_dt_kernel, time_stepping_kernels.h:13-32; euler3d.cpp:472-475. */
+int mgcfd_op_calculate_dt(int32_t nnodes, const double* variables, const double* volumes, double* dt,
+                          void* stream);
+/* get_min_dt_kernel with OP_MIN, time_stepping_kernels.h:34-41; euler3d.cpp:476-479.
+ * Writes min(DBL_MAX, dt[0..n)) to the device scalar *min_dt (NaNs ignored,
+ * as `dt < min` is false for them). */
+int mgcfd_op_get_min_dt(int32_t nnodes, const double* dt, double* min_dt, void* stream);
+/* compute_step_factor_kernel, time_stepping_kernels.h:43-64; euler3d.cpp:485-489.
+ * min_dt is a device scalar. */
+int mgcfd_op_compute_step_factor(int32_t nnodes, const double* variables, const double* volumes,
+                                 const double* min_dt, double* step_factors, void* stream);
+/* compute_flux_edge_kernel, flux.h:41-208; euler3d.cpp:498-503 (both ends OP_INC). */
+int mgcfd_op_compute_flux_edge(int32_t nedges, int32_t nnodes, const int32_t* edge_to_nodes,
+                               const double* variables, const double* edge_weights,
+                               double smoothing_coefficient, double* fluxes, void* stream);
+/* compute_bnd_node_flux_kernel, flux.h:14-39; euler3d.cpp:505-509. */
+int mgcfd_op_compute_bnd_node_flux(int32_t nbnd, int32_t nnodes, const int32_t* bnd_to_node,
+                                   const int32_t* bnd_group,
+                                   const double* bnd_weights, const double* variables,
+                                   const mgcfd_freestream* ff, double* fluxes, void* stream);
+/* time_step_kernel, time_stepping_kernels.h:66-86; euler3d.cpp:511-516. */
+int mgcfd_op_time_step(int32_t nnodes, int32_t rk_cycle, const double* step_factors, double* fluxes,
+                       const double* old_variables, double* variables, void* stream);
+/* unstructured_stream_kernel, unstructured_stream.h:7-57; euler3d.cpp:518-525. */
+int mgcfd_op_unstructured_stream(int32_t nedges, int32_t nnodes, const int32_t* edge_to_nodes,
+                                 const double* variables, const double* edge_weights, double* fluxes,
+                                 void* stream);
+/* residual_kernel, validation.h:27-35; euler3d.cpp:528-531. */
+int mgcfd_op_residual(int32_t nnodes, const double* old_variables, const double* variables,
+                      double* residuals, void* stream);
+/* calc_rms_kernel with OP_INC, validation.h:37-44; euler3d.cpp:533-537.
+ * Adds sum(residual^2) to the device scalar *rms. */
+int mgcfd_op_calc_rms(int32_t nnodes, const double* residuals, double* rms, void* stream);
+/* count_bad_vals with OP_INC, validation.h:102-115; euler3d.cpp:539-544.
+ * Adds the NaN/Inf count to the device scalar *count. */
+int mgcfd_op_count_bad_vals(int32_t nnodes, const double* variables, int32_t* count, void* stream);
+/* up_pre_kernel, mg.h:29-39; euler3d.cpp:581-583 (over fine nodes). */
+int mgcfd_op_up_pre(int32_t nfine, int32_t ncoarse, const int32_t* node_to_mg, double* coarse_variables,
+                    int32_t* up_scratch, void* stream);
+/* up_kernel, mg.h:41-52; euler3d.cpp:585-588. */
+int mgcfd_op_up(int32_t nfine, int32_t ncoarse, const int32_t* node_to_mg, const double* fine_variables,
+                double* coarse_variables, int32_t* up_scratch, void* stream);
+/* up_post_kernel, mg.h:54-64; euler3d.cpp:590-592 (over coarse nodes). */
+int mgcfd_op_up_post(int32_t ncoarse, double* coarse_variables, const int32_t* up_scratch, void* stream);
+/* down_kernel, mg.h:66-88; euler3d.cpp:626-631. */
+int mgcfd_op_down(int32_t nfine, int32_t ncoarse, const int32_t* node_to_mg, double* fine_variables,
+                  const double* fine_residuals, const double* fine_coords, const double* coarse_residuals,
+                  const double* coarse_coords, void* stream);
+/* Number of elements the mapped entry points above skipped because a map
+ * entry was outside [0, set size) since the last reset; reset != 0 zeroes the
+ * counter.  Reads a device counter: call after the streams used are idle. */
+int mgcfd_op_map_errors(int64_t* count, int32_t reset);
+/* identify_differences + count_non_zeros, validation.h:46-100; euler3d.cpp:689-699.
+ * Adds the number of values of `test` that differ from `master` by more than
+ * the reference's tolerance to the device scalar *count. */
+int mgcfd_op_count_differences(int32_t nnodes, const double* test, const double* master, int32_t* count,
+                               void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Device-resident multigrid solver.                                        */
+enum { MGCFD_PRECISION_FP64 = 0, MGCFD_PRECISION_MIXED = 1 };
+enum { MGCFD_INCREMENT_AUTO = 0, MGCFD_INCREMENT_ATOMIC = 1, MGCFD_INCREMENT_GATHER = 2 };
+enum { MGCFD_RENUMBER_NONE = 0, MGCFD_RENUMBER_SPATIAL = 1, MGCFD_RENUMBER_RCM = 2 };
+enum {
+  MGCFD_Q_VARIABLES = 0,    /* [N][5] */
+  MGCFD_Q_FLUXES = 1,       /* [N][5] */
+  MGCFD_Q_STEP_FACTORS = 2, /* [N]    */
+  MGCFD_Q_VOLUMES = 3,      /* [N]    */
+  MGCFD_Q_RESIDUALS = 4,    /* [N][5] */
+  MGCFD_Q_OLD_VARIABLES = 5 /* [N][5] */
+};
+
+typedef struct mgcfd_solver_options {
+  int32_t precision;         /* MGCFD_PRECISION_*                                   */
+  int32_t increment;         /* MGCFD_INCREMENT_*                                   */
+  int32_t renumber;          /* MGCFD_RENUMBER_*                                    */
+  int32_t use_graph;         /* capture one V-cycle as a CUDA graph and replay it  */
+  int32_t measure_mem_bound; /* also run unstructured_stream each RK stage (-b)   */
+  int32_t block_size;        /* threads per block of the edge kernels; 0 = default */
+  int32_t time_kernels;      /* record CUDA events around level-0 flux sweeps      */
+  int32_t reserved[9];
+} mgcfd_solver_options;
+
+typedef struct mgcfd_solver_stats {
+  int64_t cycles;            /* V-cycles completed since create/reset             */
+  int64_t smoothing_steps;   /* smoothing steps (euler3d.cpp:467-550)             */
+  int64_t flux_sweeps_l0;    /* level-0 edge-flux launches timed                  */
+  double flux_ms_l0;         /* summed CUDA-event time of those launches          */
+  int64_t kernel_launches;   /* kernels this solver enqueued since create/reset   */
+  int64_t device_bytes;      /* HBM held by the solver                             */
+  double rms_l0;             /* last level-0 sqrt(sum res^2 / N) (euler3d.cpp:537) */
+  int32_t status;            /* sticky device status (MGCFD_OK or an error)       */
+  int32_t ncolors_reserved;
+} mgcfd_solver_stats;
+
+typedef struct mgcfd_solver mgcfd_solver;
+
+void mgcfd_solver_default_options(mgcfd_solver_options* opt);
+/* Copies the mesh to the device (renumbered per opt->renumber), computes
+ * volumes and re-oriented, damped weights (euler3d.cpp:413-441) and sets the
+ * flow to freestream.  `stream` is used for every later launch. */
+int mgcfd_solver_create(int32_t nlevels, const mgcfd_level_view* levels, double mach, double aoa_deg,
+                        const mgcfd_solver_options* opt, void* stream, mgcfd_solver** out);
+/* Back to the state right after create (freestream, counters zeroed). */
+int mgcfd_solver_reset(mgcfd_solver* s);
+/* Enqueue `ncycles` V-cycles (euler3d.cpp:458-641).  Asynchronous. */
+int mgcfd_solver_run(mgcfd_solver* s, int32_t ncycles);
+/* Wait for enqueued work; returns the sticky status. */
+int mgcfd_solver_synchronize(mgcfd_solver* s);
+/* Copy a per-node quantity of one level to host memory in the caller's
+ * (input) node order.  Synchronises. */
+int mgcfd_solver_fetch(mgcfd_solver* s, int32_t level, int32_t quantity, double* host_out);
+int mgcfd_solver_get_stats(mgcfd_solver* s, mgcfd_solver_stats* out);
+void mgcfd_solver_destroy(mgcfd_solver* s);
+
+/* One full solve through host buffers: upload the mesh, initialise, run
+ * ncycles V-cycles, download every level's variables (file order) into
+ * out_variables[l] (host, [N_l][5]).  The reference-facing end-to-end call. */
+int mgcfd_solve(int32_t nlevels, const mgcfd_level_view* levels, double mach, double aoa_deg, int32_t ncycles,
+                const mgcfd_solver_options* opt, double* const* out_variables);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,44 @@
+// Host-side preparation of a multigrid mesh for the device solver:
+// geometry initialisation (euler3d.cpp:413-441), node renumbering for
+// locality, edge orientation and ordering, boundary entries folded per node,
+// and the multigrid transfer tables.  Everything here is integer work except
+// the geometry initialisation, which follows the reference's sequential
+// order exactly (so volumes and weights are bit-identical to the reference).
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "mgcfd_gb300.h"
+
+namespace mgcfd {
+
+struct PreparedLevel {
+  int32_t n = 0, ne = 0;
+  std::vector<int32_t> perm;       // new id -> input id
+  std::vector<int32_t> inv;        // input id -> new id
+  std::vector<double> vol;         // [n] dual volumes (new order)
+  std::vector<int32_t> e2n;        // [ne][2] new ids, a < b, sorted by (a, b)
+  std::vector<double> w4;          // [ne][4] (wx, wy, wz, -|w| * smoothing * 0.5), damped
+  std::vector<int32_t> a_off;      // [n+1] edges with first node a occupy [a_off[a], a_off[a+1])
+  std::vector<int32_t> b_off;      // [n+1] CSR of edges by second node
+  std::vector<int32_t> b_list;     // [ne]
+  std::vector<int32_t> bidx;       // [n] row in bdata or -1
+  std::vector<double> bdata;       // [nb][12] far-field sum w (3), wall sum w (3), w.F_ff (5), pad
+  std::vector<int32_t> n2mg;       // [n] new coarse id (empty on coarsest level)
+  std::vector<double> dvec;        // [n][4] |dx|, |dy|, |dz|, dist to the coarse parent
+  std::vector<int32_t> ch_off;     // [n+1] fine children of each node of this level (as coarse)
+  std::vector<int32_t> ch_list;    // [n_fine]
+  int32_t nb = 0;
+};
+
+// Returns MGCFD_OK or an error status (message via set_error).
+int prepare_mesh(int32_t nlevels, const mgcfd_level_view* levels, const mgcfd_freestream& ff, int renumber,
+                 std::vector<PreparedLevel>* out);
+
+// Node orderings (new id -> input id).
+void spatial_order(const double* xyz, int32_t n, std::vector<int32_t>* perm);
+void rcm_order(int32_t n, int32_t ne, const int32_t* e2n, std::vector<int32_t>* perm);
+
+}  // namespace mgcfd

@@ -1,0 +1,905 @@
+// Device-resident multigrid solver: the whole V-cycle of euler3d.cpp:452-641
+// on one GPU with no host synchronisation inside a cycle.
+//
+// Layout in HBM (per level, nodes in renumbered order, see setup.h):
+//   rec    [N][8]  f64  rho, rho*u, rho*v, rho*w, rho*E, p, |u|+c, 1/rho
+//                       (the conserved state plus the primitives the edge
+//                       kernel needs; 64 B rows read with two 256-bit loads)
+//   rec32  [N][8]  f32  the same in FP32 (mixed precision only)
+//   old, res, flux [N][5] f64; inv_vol, cbrt_vol, vol [N] f64
+//   e2n    [E]     int2 (a < b, sorted by a then b); w4 [E] double4
+//                       (wx, wy, wz, -|w|*smoothing*0.5) or float4 (mixed)
+//   fe     [E][5]  f64  per-edge fluxes (gather increment strategy only)
+//   bidx [N] int32 and bdata [NB][12] f64: boundary entries folded per node
+//   n2mg [N], dvec [N] double4: prolongation parent and |dx|,|dy|,|dz|,dist
+//   ch_off/ch_list: restriction children of each coarse node
+//
+// Kernels per smoothing step (euler3d.cpp:467-550):
+//   memset(min_dt key)                      get_min_dt's DBL_MAX start
+//   k_step_begin   nodes  old = var, primitives, dt, block min -> atomicMin
+//   3 x { k_flux   edges  edge flux, +f to a and -f to b (FP64 atomics) or
+//                         f stored per edge (gather strategy)
+//         k_update nodes  gathered flux + boundary flux, time step, flux = 0,
+//                         primitives for the next stage; in the last stage
+//                         residual, and at level 0 the rms and NaN/Inf count }
+// then k_restrict (coarse nodes, children mean, mg.h:29-64) or k_prolong
+// (fine nodes, mg.h:66-88).
+//
+// Failure handling: min_dt < 0 and NaN/Inf at level 0 set a sticky device
+// status word; every later kernel sees it and returns, so the run stops at the
+// same point the reference aborts.  The host reads the status on synchronize.
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "common.h"
+#include "device_math.cuh"
+#include "setup.h"
+
+using namespace mgcfd;
+
+namespace {
+
+constexpr int kMaxLevels = 16;
+constexpr int kNodeThreads = 256;
+
+struct DevStatus {
+  unsigned long long dt_key[kMaxLevels];  // order-preserving key of each level's last min_dt
+  int halt;                                // non-zero: stop all further work
+  int neg_dt;                              // min_dt < 0 seen
+  int bad_count;                           // NaN/Inf count at level 0
+  int pad;
+  double rms_acc;                          // sum of residual^2, last level-0 step
+};
+
+#define CK(call)                                                                                         \
+  do {                                                                                                   \
+    cudaError_t e_ = (call);                                                                             \
+    if (e_ != cudaSuccess) return set_error(MGCFD_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// Kernels.
+
+__device__ __forceinline__ void store_rec(double* rec, int64_t i, const NodePrim& p) {
+  double4_32a* r = reinterpret_cast<double4_32a*>(rec + 8 * i);
+  r[0] = make_double4_32a(p.rho, p.mx, p.my, p.mz);
+  r[1] = make_double4_32a(p.rhoE, p.p, p.s, p.rinv);
+}
+
+__device__ __forceinline__ NodePrim load_rec(const double* rec, int64_t i) {
+  const double4_32a* r = reinterpret_cast<const double4_32a*>(rec + 8 * i);
+  const double4_32a x = r[0], y = r[1];
+  NodePrim p;
+  p.rho = x.x; p.mx = x.y; p.my = x.z; p.mz = x.w;
+  p.rhoE = y.x; p.p = y.y; p.s = y.z; p.rinv = y.w;
+  return p;
+}
+
+struct NodePrimF {
+  float rho, mx, my, mz, rhoE, p, s, rinv;
+};
+
+__device__ __forceinline__ void store_rec32(float* rec32, int64_t i, const NodePrim& p) {
+  float4* r = reinterpret_cast<float4*>(rec32 + 8 * i);
+  r[0] = make_float4((float)p.rho, (float)p.mx, (float)p.my, (float)p.mz);
+  r[1] = make_float4((float)p.rhoE, (float)p.p, (float)p.s, (float)p.rinv);
+}
+
+// Mixed precision: FP32 primitives straight from the FP64 state.
+__device__ __forceinline__ void store_rec32_from_var(float* rec32, int64_t i, double rho, double mx, double my,
+                                                     double mz, double rhoE) {
+  const float r = (float)rho, x = (float)mx, y = (float)my, z = (float)mz, e = (float)rhoE;
+  const float rinv = 1.0f / r;
+  const float ux = x * rinv, uy = y * rinv, uz = z * rinv;
+  const float q2 = ux * ux + uy * uy + uz * uz;
+  const float p = 0.4f * (e - 0.5f * r * q2);
+  const float s = sqrtf(q2) + sqrtf(1.4f * p * rinv);
+  float4* o = reinterpret_cast<float4*>(rec32 + 8 * i);
+  o[0] = make_float4(r, x, y, z);
+  o[1] = make_float4(e, p, s, rinv);
+}
+
+__device__ __forceinline__ NodePrimF load_rec32(const float* rec32, int64_t i) {
+  const float4* r = reinterpret_cast<const float4*>(rec32 + 8 * i);
+  const float4 x = r[0], y = r[1];
+  return NodePrimF{x.x, x.y, x.z, x.w, y.x, y.y, y.z, y.w};
+}
+
+__device__ __forceinline__ void edge_flux_f32(const NodePrimF& a, const NodePrimF& b, float4 w, float f[5]) {
+  const float mwa = a.mx * w.x + a.my * w.y + a.mz * w.z;
+  const float mwb = b.mx * w.x + b.my * w.y + b.mz * w.z;
+  const float uwa = mwa * a.rinv, uwb = mwb * b.rinv;
+  const float fac = w.w * (a.s + b.s);
+  const float pp = a.p + b.p;
+  f[0] = fac * (a.rho - b.rho) - 0.5f * (mwa + mwb);
+  f[1] = fac * (a.mx - b.mx) - 0.5f * (a.mx * uwa + b.mx * uwb + pp * w.x);
+  f[2] = fac * (a.my - b.my) - 0.5f * (a.my * uwa + b.my * uwb + pp * w.y);
+  f[3] = fac * (a.mz - b.mz) - 0.5f * (a.mz * uwa + b.mz * uwb + pp * w.z);
+  f[4] = fac * (a.rhoE - b.rhoE) - 0.5f * ((a.rhoE + a.p) * uwa + (b.rhoE + b.p) * uwb);
+}
+
+// Freestream state into rec (initialize_variables_kernel, misc.h:10-16).
+__global__ void k_init_state(int32_t n, double* __restrict__ rec, double v0, double v1, double v2, double v3,
+                             double v4) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  store_rec(rec, i, node_prim(v0, v1, v2, v3, v4));
+}
+
+// copy_double_kernel + calculate_dt_kernel + get_min_dt_kernel (block part).
+template <bool MIXED>
+__global__ void __launch_bounds__(kNodeThreads) k_step_begin(int32_t n, double* __restrict__ rec,
+                                                             float* __restrict__ rec32, double* __restrict__ old,
+                                                             const double* __restrict__ cbrt_vol,
+                                                             unsigned long long* __restrict__ dt_key,
+                                                             const DevStatus* __restrict__ st) {
+  __shared__ double smin[kNodeThreads / 32];
+  __shared__ int s_halt;
+  if (threadIdx.x == 0) s_halt = st->halt;
+  __syncthreads();
+  if (s_halt) return;  // block-uniform: the reduction below synchronises
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double m = DBL_MAX;
+  if (i < n) {
+    const double4_32a* r = reinterpret_cast<const double4_32a*>(rec + 8 * i);
+    const double4_32a x = r[0];
+    const double e = r[1].x;
+    const NodePrim p = node_prim(x.x, x.y, x.z, x.w, e);
+    store_rec(rec, i, p);
+    if (MIXED) store_rec32_from_var(rec32, i, x.x, x.y, x.z, x.w, e);
+    double* o = old + 5 * i;
+    o[0] = x.x; o[1] = x.y; o[2] = x.z; o[3] = x.w; o[4] = e;
+    const double dt = 0.5 * (cbrt_vol[i] / p.s);  // time_stepping_kernels.h:31
+    if (dt < m) m = dt;                            // NaN never wins, as in get_min_dt_kernel
+  }
+  m = warp_min(m);
+  if ((threadIdx.x & 31) == 0) smin[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    m = threadIdx.x < kNodeThreads / 32 ? smin[threadIdx.x] : DBL_MAX;
+    m = warp_min(m);
+    if (threadIdx.x == 0 && m < DBL_MAX) atomicMin(dt_key, dkey(m));
+  }
+}
+
+// compute_flux_edge_kernel (flux.h:41-208), FP64, both ends by FP64 atomics
+// (GATHER=false) or stored per edge for the node-side gather (GATHER=true).
+template <bool GATHER>
+__global__ void k_flux_f64(int32_t ne, const int2* __restrict__ e2n, const double4_32a* __restrict__ w4,
+                           const double* __restrict__ rec, double* __restrict__ flux, double* __restrict__ fe,
+                           const DevStatus* __restrict__ st) {
+  if (st->halt) return;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  const int2 ab = e2n[e];
+  const double4_32a w = w4[e];
+  const NodePrim a = load_rec(rec, ab.x);
+  const NodePrim b = load_rec(rec, ab.y);
+  double f[5];
+  edge_flux(a, b, w.x, w.y, w.z, w.w, f);
+  if (GATHER) {
+    double* o = fe + 5 * e;
+#pragma unroll
+    for (int k = 0; k < 5; k++) o[k] = f[k];
+  } else {
+    double* fa = flux + 5 * (int64_t)ab.x;
+    double* fb = flux + 5 * (int64_t)ab.y;
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+      atomicAdd(fa + k, f[k]);
+      atomicAdd(fb + k, -f[k]);
+    }
+  }
+}
+
+// Mixed precision edge flux: FP32 arithmetic, FP64 accumulation.
+template <bool GATHER>
+__global__ void k_flux_mixed(int32_t ne, const int2* __restrict__ e2n, const float4* __restrict__ w4f,
+                             const float* __restrict__ rec32, double* __restrict__ flux, double* __restrict__ fe,
+                             const DevStatus* __restrict__ st) {
+  if (st->halt) return;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  const int2 ab = e2n[e];
+  const float4 w = w4f[e];
+  const NodePrimF a = load_rec32(rec32, ab.x);
+  const NodePrimF b = load_rec32(rec32, ab.y);
+  float f[5];
+  edge_flux_f32(a, b, w, f);
+  if (GATHER) {
+    double* o = fe + 5 * e;
+#pragma unroll
+    for (int k = 0; k < 5; k++) o[k] = (double)f[k];
+  } else {
+    double* fa = flux + 5 * (int64_t)ab.x;
+    double* fb = flux + 5 * (int64_t)ab.y;
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+      atomicAdd(fa + k, (double)f[k]);
+      atomicAdd(fb + k, -(double)f[k]);
+    }
+  }
+}
+
+// unstructured_stream_kernel (unstructured_stream.h:7-57): the flux kernel's
+// data movement with trivial arithmetic (the reference's -b probe).
+__global__ void k_stream(int32_t ne, const int2* __restrict__ e2n, const double4_32a* __restrict__ w4,
+                         const double* __restrict__ rec, double* __restrict__ dummy,
+                         const DevStatus* __restrict__ st) {
+  if (st->halt) return;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  const int2 ab = e2n[e];
+  const double4_32a w = w4[e];
+  const NodePrim a = load_rec(rec, ab.x);
+  const NodePrim b = load_rec(rec, ab.y);
+  double* fa = dummy + 5 * (int64_t)ab.x;
+  double* fb = dummy + 5 * (int64_t)ab.y;
+  atomicAdd(fa + 0, b.rho + w.x);
+  atomicAdd(fa + 1, b.mx + w.z);
+  atomicAdd(fa + 2, b.my);
+  atomicAdd(fa + 3, b.mz);
+  atomicAdd(fa + 4, b.rhoE + w.y);
+  atomicAdd(fb + 0, a.rho);
+  atomicAdd(fb + 1, a.mx);
+  atomicAdd(fb + 2, a.my);
+  atomicAdd(fb + 3, a.mz);
+  atomicAdd(fb + 4, a.rhoE);
+}
+
+struct UpdateArgs {
+  int32_t n;
+  int32_t level0;
+  double inv_div;  // 1 / (RK + 1 - rk)
+  double* rec;
+  float* rec32;
+  const double* old;
+  double* flux;
+  const double* fe;
+  const int32_t* a_off;
+  const int32_t* b_off;
+  const int32_t* b_list;
+  const double* inv_vol;
+  const int32_t* bidx;
+  const double* bdata;
+  double* res;
+  const unsigned long long* dt_key;
+  DevStatus* st;
+};
+
+// Boundary flux of one node (flux.h:14-39 summed over the node's entries).
+__device__ __forceinline__ void add_boundary(const NodePrim& p, const double* __restrict__ b, double F[5]) {
+  double ffw[5] = {b[6], b[7], b[8], b[9], b[10]};
+  double f[5];
+  farfield_flux(p, b[0], b[1], b[2], ffw, f);
+#pragma unroll
+  for (int k = 0; k < 5; k++) F[k] += f[k];
+  F[1] += b[3] * p.p;
+  F[2] += b[4] * p.p;
+  F[3] += b[5] * p.p;
+}
+
+// compute_bnd_node_flux_kernel + time_step_kernel (+ residual_kernel,
+// calc_rms_kernel and count_bad_vals in the last stage).
+template <bool GATHER, bool LAST, bool MIXED>
+__global__ void __launch_bounds__(kNodeThreads) k_update(UpdateArgs A) {
+  __shared__ double srms[kNodeThreads / 32];
+  __shared__ int sbad[kNodeThreads / 32];
+  __shared__ int s_halt;
+  if (threadIdx.x == 0) s_halt = A.st->halt;
+  __syncthreads();
+  if (s_halt) return;  // block-uniform: the reduction below synchronises
+  const double min_dt = dkey_inv(*A.dt_key);
+  if (min_dt < 0.0) {  // euler3d.cpp:480: abort before the step factor is used
+    if (threadIdx.x == 0) { A.st->neg_dt = 1; atomicOr(&A.st->halt, 1); }
+    return;
+  }
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double r2 = 0.0;
+  int bad = 0;
+  if (i < A.n) {
+    double F[5];
+    if (GATHER) {
+#pragma unroll
+      for (int k = 0; k < 5; k++) F[k] = 0.0;
+      for (int32_t e = A.a_off[i]; e < A.a_off[i + 1]; e++)
+#pragma unroll
+        for (int k = 0; k < 5; k++) F[k] += A.fe[5 * (int64_t)e + k];
+      for (int32_t j = A.b_off[i]; j < A.b_off[i + 1]; j++) {
+        const int64_t e = A.b_list[j];
+#pragma unroll
+        for (int k = 0; k < 5; k++) F[k] -= A.fe[5 * e + k];
+      }
+    } else {
+      double* fl = A.flux + 5 * i;
+#pragma unroll
+      for (int k = 0; k < 5; k++) { F[k] = fl[k]; fl[k] = 0.0; }
+    }
+    const int32_t bi = A.bidx[i];
+    if (bi >= 0) {
+      NodePrim p;
+      if (MIXED) {
+        const double4_32a* r = reinterpret_cast<const double4_32a*>(A.rec + 8 * i);
+        const double4_32a x = r[0];
+        p = node_prim(x.x, x.y, x.z, x.w, r[1].x);
+      } else {
+        p = load_rec(A.rec, i);
+      }
+      add_boundary(p, A.bdata + 12 * (int64_t)bi, F);
+    }
+    const double factor = (min_dt * A.inv_vol[i]) * A.inv_div;  // step_factor / (RK+1-rk)
+    const double* o = A.old + 5 * i;
+    double v[5];
+#pragma unroll
+    for (int k = 0; k < 5; k++) v[k] = o[k] + factor * F[k];
+    if (LAST) {
+      double4_32a* r = reinterpret_cast<double4_32a*>(A.rec + 8 * i);
+      r[0] = make_double4_32a(v[0], v[1], v[2], v[3]);
+      A.rec[8 * i + 4] = v[4];
+      double* rs = A.res + 5 * i;
+#pragma unroll
+      for (int k = 0; k < 5; k++) {
+        const double d = v[k] - o[k];
+        rs[k] = d;
+        r2 += d * d;
+        if (isnan(v[k]) || isinf(v[k])) bad++;
+      }
+    } else if (MIXED) {
+      double4_32a* r = reinterpret_cast<double4_32a*>(A.rec + 8 * i);
+      r[0] = make_double4_32a(v[0], v[1], v[2], v[3]);
+      A.rec[8 * i + 4] = v[4];
+      store_rec32_from_var(A.rec32, i, v[0], v[1], v[2], v[3], v[4]);
+    } else {
+      store_rec(A.rec, i, node_prim(v[0], v[1], v[2], v[3], v[4]));
+    }
+  }
+  if (LAST) {
+    if (!A.level0) return;
+    r2 = warp_sum(r2);
+    bad = warp_sum_int(bad);
+    if ((threadIdx.x & 31) == 0) { srms[threadIdx.x >> 5] = r2; sbad[threadIdx.x >> 5] = bad; }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      r2 = threadIdx.x < kNodeThreads / 32 ? srms[threadIdx.x] : 0.0;
+      bad = threadIdx.x < kNodeThreads / 32 ? sbad[threadIdx.x] : 0;
+      r2 = warp_sum(r2);
+      bad = warp_sum_int(bad);
+      if (threadIdx.x == 0) {
+        atomicAdd(&A.st->rms_acc, r2);
+        if (bad) { atomicAdd(&A.st->bad_count, bad); atomicOr(&A.st->halt, 1); }
+      }
+    }
+  }
+}
+
+// up_pre/up/up_post (mg.h:29-64) as a gather over each coarse node's children.
+__global__ void k_restrict(int32_t nc, const int32_t* __restrict__ ch_off, const int32_t* __restrict__ ch_list,
+                           const double* __restrict__ frec, double* __restrict__ crec,
+                           const DevStatus* __restrict__ st) {
+  if (st->halt) return;
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  const int32_t lo = ch_off[c], hi = ch_off[c + 1];
+  if (hi == lo) return;  // no children: state unchanged (avg = 1 on untouched values)
+  double s[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int32_t j = lo; j < hi; j++) {
+    const double* r = frec + 8 * (int64_t)ch_list[j];
+#pragma unroll
+    for (int k = 0; k < 5; k++) s[k] += r[k];
+  }
+  const double avg = 1.0 / (double)(hi - lo);
+  double* r = crec + 8 * c;
+#pragma unroll
+  for (int k = 0; k < 5; k++) r[k] = s[k] * avg;
+}
+
+// down_kernel (mg.h:66-88) with the parent offsets precomputed.
+__global__ void k_prolong(int32_t nf, const int32_t* __restrict__ n2mg, const double4_32a* __restrict__ dvec,
+                          double* __restrict__ frec, const double* __restrict__ fres,
+                          const double* __restrict__ cres, const DevStatus* __restrict__ st) {
+  if (st->halt) return;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nf) return;
+  const int64_t c = n2mg[i];
+  const double4_32a d = dvec[i];
+  const double dd[5] = {d.w, d.x, d.y, d.z, d.w};
+  double* r = frec + 8 * i;
+#pragma unroll
+  for (int k = 0; k < 5; k++) r[k] -= dd[k] * (cres[5 * c + k] - fres[5 * i + k]);
+}
+
+// Fetch helpers: scatter renumbered rows back to input order.
+__global__ void k_unpermute(int32_t n, int32_t width, int32_t stride, const double* __restrict__ src,
+                            const int32_t* __restrict__ perm, double* __restrict__ dst) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)n * width) return;
+  const int64_t i = t / width, k = t % width;
+  dst[(int64_t)perm[i] * width + k] = src[i * stride + k];
+}
+
+__global__ void k_step_factors(int32_t n, const double* __restrict__ vol, const unsigned long long* dt_key,
+                               const int32_t* __restrict__ perm, double* __restrict__ dst) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  dst[perm[i]] = dkey_inv(*dt_key) / vol[i];  // time_stepping_kernels.h:63
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Host side.
+
+struct DevLevel {
+  int32_t n = 0, ne = 0, nb = 0;
+  double* rec = nullptr;
+  float* rec32 = nullptr;
+  double* old = nullptr;
+  double* flux = nullptr;
+  double* res = nullptr;
+  double* dummy = nullptr;
+  double* inv_vol = nullptr;
+  double* cbrt_vol = nullptr;
+  double* vol = nullptr;
+  int2* e2n = nullptr;
+  double4_32a* w4 = nullptr;
+  float4* w4f = nullptr;
+  double* fe = nullptr;
+  int32_t* a_off = nullptr;
+  int32_t* b_off = nullptr;
+  int32_t* b_list = nullptr;
+  int32_t* bidx = nullptr;
+  double* bdata = nullptr;
+  int32_t* n2mg = nullptr;
+  double4_32a* dvec = nullptr;
+  int32_t* ch_off = nullptr;
+  int32_t* ch_list = nullptr;
+  int32_t* perm = nullptr;
+};
+
+struct mgcfd_solver {
+  mgcfd_solver_options opt{};
+  mgcfd_freestream ff{};
+  cudaStream_t stream = nullptr;
+  bool owns_stream = false;  // graph capture needs a non-legacy stream
+  int device = 0;
+  std::vector<DevLevel> L;
+  std::vector<void*> allocs;
+  DevStatus* st = nullptr;
+  double* fetch_buf = nullptr;
+  int64_t device_bytes = 0;
+  // V-cycle state (euler3d.cpp:452-457).
+  int64_t cycle = 0;
+  int level = 0;
+  bool up = true;
+  int64_t steps = 0;
+  int64_t launches = 0;
+  int64_t launches_per_cycle = 0;
+  bool gather = false;
+  cudaGraphExec_t graph = nullptr;
+  // Kernel timing.
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending, spare;
+  double flux_ms = 0.0;
+  int64_t flux_sweeps = 0;
+  int status = MGCFD_OK;
+
+  template <class T>
+  int alloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) return MGCFD_OK;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return set_error(MGCFD_ERR_NOMEM, "cudaMalloc of " + std::to_string(count * sizeof(T)) + " bytes failed: " +
+                                            cudaGetErrorString(e));
+    }
+    allocs.push_back(*p);
+    device_bytes += (int64_t)(count * sizeof(T));
+    return MGCFD_OK;
+  }
+  template <class T>
+  int upload(T** p, const void* src, size_t count) {
+    int r = alloc(p, count);
+    if (r) return r;
+    if (count) CK(cudaMemcpyAsync(*p, src, count * sizeof(T), cudaMemcpyHostToDevice, stream));
+    return MGCFD_OK;
+  }
+};
+
+namespace {
+
+int grid(int64_t n, int threads) { return (int)((n + threads - 1) / threads); }
+
+int edge_threads(const mgcfd_solver* s) { return s->opt.block_size > 0 ? s->opt.block_size : 128; }
+
+// One smoothing step at `level` (euler3d.cpp:467-550).
+int enqueue_smooth(mgcfd_solver* s, int level) {
+  DevLevel& D = s->L[(size_t)level];
+  const bool mixed = s->opt.precision == MGCFD_PRECISION_MIXED;
+  const bool timing = s->opt.time_kernels && level == 0;
+  CK(cudaMemsetAsync(&s->st->dt_key[level], 0xff, sizeof(unsigned long long), s->stream));
+  if (level == 0) CK(cudaMemsetAsync(&s->st->rms_acc, 0, sizeof(double), s->stream));
+  if (mixed)
+    k_step_begin<true><<<grid(D.n, kNodeThreads), kNodeThreads, 0, s->stream>>>(D.n, D.rec, D.rec32, D.old, D.cbrt_vol,
+                                                                                 &s->st->dt_key[level], s->st);
+  else
+    k_step_begin<false><<<grid(D.n, kNodeThreads), kNodeThreads, 0, s->stream>>>(D.n, D.rec, D.rec32, D.old, D.cbrt_vol,
+                                                                                  &s->st->dt_key[level], s->st);
+  s->launches++;
+  const int et = edge_threads(s);
+  for (int rk = 0; rk < kRK; rk++) {
+    if (D.ne > 0) {
+      std::pair<cudaEvent_t, cudaEvent_t> ev{nullptr, nullptr};
+      if (timing) {
+        if (!s->spare.empty()) { ev = s->spare.back(); s->spare.pop_back(); }
+        else {
+          CK(cudaEventCreate(&ev.first));
+          CK(cudaEventCreate(&ev.second));
+        }
+        CK(cudaEventRecord(ev.first, s->stream));
+      }
+      const int g = grid(D.ne, et);
+      if (mixed) {
+        if (s->gather) k_flux_mixed<true><<<g, et, 0, s->stream>>>(D.ne, D.e2n, D.w4f, D.rec32, D.flux, D.fe, s->st);
+        else k_flux_mixed<false><<<g, et, 0, s->stream>>>(D.ne, D.e2n, D.w4f, D.rec32, D.flux, D.fe, s->st);
+      } else {
+        if (s->gather) k_flux_f64<true><<<g, et, 0, s->stream>>>(D.ne, D.e2n, D.w4, D.rec, D.flux, D.fe, s->st);
+        else k_flux_f64<false><<<g, et, 0, s->stream>>>(D.ne, D.e2n, D.w4, D.rec, D.flux, D.fe, s->st);
+      }
+      s->launches++;
+      if (timing) {
+        CK(cudaEventRecord(ev.second, s->stream));
+        s->pending.push_back(ev);
+      }
+    }
+    UpdateArgs A;
+    A.n = D.n; A.level0 = level == 0; A.inv_div = 1.0 / (double)(kRK + 1 - rk);
+    A.rec = D.rec; A.rec32 = D.rec32; A.old = D.old; A.flux = D.flux; A.fe = D.fe;
+    A.a_off = D.a_off; A.b_off = D.b_off; A.b_list = D.b_list; A.inv_vol = D.inv_vol; A.bidx = D.bidx;
+    A.bdata = D.bdata; A.res = D.res; A.dt_key = &s->st->dt_key[level]; A.st = s->st;
+    const int gn = grid(D.n, kNodeThreads);
+    const bool last = rk == kRK - 1;
+    if (s->gather) {
+      if (last && mixed) k_update<true, true, true><<<gn, kNodeThreads, 0, s->stream>>>(A);
+      else if (last) k_update<true, true, false><<<gn, kNodeThreads, 0, s->stream>>>(A);
+      else if (mixed) k_update<true, false, true><<<gn, kNodeThreads, 0, s->stream>>>(A);
+      else k_update<true, false, false><<<gn, kNodeThreads, 0, s->stream>>>(A);
+    } else {
+      if (last && mixed) k_update<false, true, true><<<gn, kNodeThreads, 0, s->stream>>>(A);
+      else if (last) k_update<false, true, false><<<gn, kNodeThreads, 0, s->stream>>>(A);
+      else if (mixed) k_update<false, false, true><<<gn, kNodeThreads, 0, s->stream>>>(A);
+      else k_update<false, false, false><<<gn, kNodeThreads, 0, s->stream>>>(A);
+    }
+    s->launches++;
+    if (s->opt.measure_mem_bound && D.ne > 0) {
+      k_stream<<<grid(D.ne, et), et, 0, s->stream>>>(D.ne, D.e2n, D.w4, D.rec, D.dummy, s->st);
+      s->launches++;
+    }
+  }
+  CK(cudaGetLastError());
+  s->steps++;
+  return MGCFD_OK;
+}
+
+// One iteration of the reference's while loop (euler3d.cpp:458-640).
+int enqueue_iteration(mgcfd_solver* s) {
+  const int levels = (int)s->L.size();
+  int r = enqueue_smooth(s, s->level);
+  if (r) return r;
+  if (levels <= 1) {
+    s->cycle++;
+    return MGCFD_OK;
+  }
+  if (s->up) {
+    s->level++;
+    DevLevel& F = s->L[(size_t)s->level - 1];
+    DevLevel& Cl = s->L[(size_t)s->level];
+    k_restrict<<<grid(Cl.n, kNodeThreads), kNodeThreads, 0, s->stream>>>(Cl.n, Cl.ch_off, Cl.ch_list, F.rec, Cl.rec, s->st);
+    s->launches++;
+    if (s->level == levels - 1) s->up = false;
+  } else {
+    s->level--;
+    DevLevel& F = s->L[(size_t)s->level];
+    DevLevel& Cl = s->L[(size_t)s->level + 1];
+    k_prolong<<<grid(F.n, kNodeThreads), kNodeThreads, 0, s->stream>>>(F.n, F.n2mg, F.dvec, F.rec, F.res, Cl.res, s->st);
+    s->launches++;
+    if (s->level == 0) {
+      s->up = true;
+      s->cycle++;
+    }
+  }
+  CK(cudaGetLastError());
+  return MGCFD_OK;
+}
+
+int enqueue_cycle(mgcfd_solver* s) {
+  const int64_t target = s->cycle + 1;
+  while (s->cycle < target) {
+    int r = enqueue_iteration(s);
+    if (r) return r;
+  }
+  return MGCFD_OK;
+}
+
+int collect_timings(mgcfd_solver* s) {
+  for (auto& ev : s->pending) {
+    float ms = 0.0f;
+    CK(cudaEventElapsedTime(&ms, ev.first, ev.second));
+    s->flux_ms += ms;
+    s->flux_sweeps++;
+    s->spare.push_back(ev);
+  }
+  s->pending.clear();
+  return MGCFD_OK;
+}
+
+int read_status(mgcfd_solver* s) {
+  DevStatus h;
+  CK(cudaMemcpy(&h, s->st, sizeof(h), cudaMemcpyDeviceToHost));
+  if (h.neg_dt) {
+    double m = 0.0;
+    for (int l = 0; l < (int)s->L.size(); l++) {
+      unsigned long long k = h.dt_key[l];
+      if (k != ~0ull) {
+        unsigned long long u = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+        double v;
+        std::memcpy(&v, &u, 8);
+        if (v < m) m = v;
+      }
+    }
+    char buf[128];
+    std::snprintf(buf, sizeof buf, "Fatal error during 'step factor' calculation, min_dt = %.5e", m);
+    s->status = set_error(MGCFD_ERR_NEGATIVE_DT, buf);
+  } else if (h.bad_count > 0) {
+    s->status = set_error(MGCFD_ERR_BAD_VALUES, "Bad variable values detected, aborting");
+  }
+  return s->status;
+}
+
+int init_state(mgcfd_solver* s) {
+  const double* v = s->ff.ff_variable;
+  for (auto& D : s->L) {
+    k_init_state<<<grid(D.n, kNodeThreads), kNodeThreads, 0, s->stream>>>(D.n, D.rec, v[0], v[1], v[2], v[3], v[4]);
+    CK(cudaMemsetAsync(D.old, 0, sizeof(double) * 5 * (size_t)D.n, s->stream));
+    CK(cudaMemsetAsync(D.res, 0, sizeof(double) * 5 * (size_t)D.n, s->stream));
+    if (D.flux) CK(cudaMemsetAsync(D.flux, 0, sizeof(double) * 5 * (size_t)D.n, s->stream));
+    if (D.dummy) CK(cudaMemsetAsync(D.dummy, 0, sizeof(double) * 5 * (size_t)D.n, s->stream));
+  }
+  CK(cudaMemsetAsync(s->st, 0, sizeof(DevStatus), s->stream));
+  CK(cudaMemsetAsync(s->st->dt_key, 0xff, sizeof(s->st->dt_key), s->stream));
+  CK(cudaGetLastError());
+  s->cycle = 0; s->level = 0; s->up = true; s->steps = 0; s->launches = 0;
+  s->flux_ms = 0.0; s->flux_sweeps = 0; s->status = MGCFD_OK;
+  for (auto& ev : s->pending) s->spare.push_back(ev);
+  s->pending.clear();
+  return MGCFD_OK;
+}
+
+void free_solver(mgcfd_solver* s) {
+  if (!s) return;
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  if (s->graph) cudaGraphExecDestroy(s->graph);
+  for (auto& ev : s->pending) { cudaEventDestroy(ev.first); cudaEventDestroy(ev.second); }
+  for (auto& ev : s->spare) { cudaEventDestroy(ev.first); cudaEventDestroy(ev.second); }
+  for (void* p : s->allocs) cudaFree(p);
+  if (s->owns_stream) cudaStreamDestroy(s->stream);
+  delete s;
+}
+
+}  // namespace
+
+extern "C" void mgcfd_solver_default_options(mgcfd_solver_options* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->precision = MGCFD_PRECISION_FP64;
+  o->increment = MGCFD_INCREMENT_AUTO;
+  o->renumber = MGCFD_RENUMBER_SPATIAL;
+  o->use_graph = 1;
+}
+
+extern "C" int mgcfd_solver_create(int32_t nlevels, const mgcfd_level_view* levels, double mach, double aoa_deg,
+                                   const mgcfd_solver_options* opt, void* stream, mgcfd_solver** out) {
+  if (!out) return set_error(MGCFD_ERR_INVALID, "mgcfd_solver_create: null output");
+  *out = nullptr;
+  if (nlevels < 1 || nlevels > kMaxLevels) return set_error(MGCFD_ERR_INVALID, "mgcfd_solver_create: 1..16 levels supported");
+  std::unique_ptr<mgcfd_solver, void (*)(mgcfd_solver*)> s(new (std::nothrow) mgcfd_solver(), free_solver);
+  if (!s) return set_error(MGCFD_ERR_NOMEM, "host allocation failed");
+  if (opt) s->opt = *opt; else mgcfd_solver_default_options(&s->opt);
+  if (s->opt.precision != MGCFD_PRECISION_FP64 && s->opt.precision != MGCFD_PRECISION_MIXED)
+    return set_error(MGCFD_ERR_INVALID, "unknown precision");
+  if (s->opt.block_size < 0 || s->opt.block_size > 1024 || (s->opt.block_size % 32) != 0)
+    return set_error(MGCFD_ERR_INVALID, "block_size must be 0 or a multiple of 32 up to 1024");
+  s->gather = s->opt.increment == MGCFD_INCREMENT_GATHER;
+  s->stream = static_cast<cudaStream_t>(stream);
+  CK(cudaGetDevice(&s->device));
+  if (!s->stream) {
+    CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+    s->owns_stream = true;
+  }
+  mgcfd_freestream_init(mach, aoa_deg, &s->ff);
+
+  std::vector<PreparedLevel> P;
+  int r;
+  try {
+    r = prepare_mesh(nlevels, levels, s->ff, s->opt.renumber, &P);
+  } catch (const std::bad_alloc&) {
+    return set_error(MGCFD_ERR_NOMEM, "host allocation failed while preparing the mesh");
+  }
+  if (r) return r;
+  const bool mixed = s->opt.precision == MGCFD_PRECISION_MIXED;
+  s->L.resize((size_t)nlevels);
+  size_t max_n = 0;
+  for (int l = 0; l < nlevels; l++) {
+    PreparedLevel& p = P[(size_t)l];
+    DevLevel& D = s->L[(size_t)l];
+    D.n = p.n; D.ne = p.ne; D.nb = p.nb;
+    max_n = std::max(max_n, (size_t)p.n);
+    std::vector<double> inv_vol((size_t)p.n), cbrt_vol((size_t)p.n);
+    for (int32_t i = 0; i < p.n; i++) { inv_vol[(size_t)i] = 1.0 / p.vol[(size_t)i]; cbrt_vol[(size_t)i] = std::cbrt(p.vol[(size_t)i]); }
+    if ((r = s->alloc(&D.rec, 8 * (size_t)p.n)) || (r = s->alloc(&D.old, 5 * (size_t)p.n)) ||
+        (r = s->alloc(&D.res, 5 * (size_t)p.n)) ||
+        (r = s->upload(&D.inv_vol, inv_vol.data(), (size_t)p.n)) ||
+        (r = s->upload(&D.cbrt_vol, cbrt_vol.data(), (size_t)p.n)) ||
+        (r = s->upload(&D.vol, p.vol.data(), (size_t)p.n)) ||
+        (r = s->upload(&D.e2n, p.e2n.data(), (size_t)p.ne)) ||
+        (r = s->upload(&D.bidx, p.bidx.data(), (size_t)p.n)) ||
+        (r = s->upload(&D.bdata, p.bdata.data(), p.bdata.size())) ||
+        (r = s->upload(&D.perm, p.perm.data(), (size_t)p.n)))
+      return r;
+    if (mixed) {
+      std::vector<float> w4f((size_t)p.ne * 4);
+      for (size_t k = 0; k < w4f.size(); k++) w4f[k] = (float)p.w4[k];
+      if ((r = s->alloc(&D.rec32, 8 * (size_t)p.n)) || (r = s->upload(&D.w4f, w4f.data(), (size_t)p.ne))) return r;
+      // Compute-bound only on the FP64 path; mixed still needs FP64 weights for the -b probe.
+      if (s->opt.measure_mem_bound && (r = s->upload(&D.w4, p.w4.data(), (size_t)p.ne))) return r;
+      CK(cudaStreamSynchronize(s->stream));  // w4f host buffer goes out of scope
+    } else {
+      if ((r = s->upload(&D.w4, p.w4.data(), (size_t)p.ne))) return r;
+    }
+    if (s->gather) {
+      if ((r = s->alloc(&D.fe, 5 * (size_t)p.ne)) || (r = s->upload(&D.a_off, p.a_off.data(), (size_t)p.n + 1)) ||
+          (r = s->upload(&D.b_off, p.b_off.data(), (size_t)p.n + 1)) ||
+          (r = s->upload(&D.b_list, p.b_list.data(), (size_t)p.ne)))
+        return r;
+    } else {
+      if ((r = s->alloc(&D.flux, 5 * (size_t)p.n))) return r;
+    }
+    if (s->opt.measure_mem_bound && (r = s->alloc(&D.dummy, 5 * (size_t)p.n))) return r;
+    if (!p.n2mg.empty() && ((r = s->upload(&D.n2mg, p.n2mg.data(), (size_t)p.n)) ||
+                            (r = s->upload(&D.dvec, p.dvec.data(), (size_t)p.n))))
+      return r;
+    if (!p.ch_off.empty() && ((r = s->upload(&D.ch_off, p.ch_off.data(), p.ch_off.size())) ||
+                              (r = s->upload(&D.ch_list, p.ch_list.data(), p.ch_list.size()))))
+      return r;
+    // The host vectors of this level die at the end of create: finish the copies first.
+    CK(cudaStreamSynchronize(s->stream));
+  }
+  if ((r = s->alloc(&s->st, 1)) || (r = s->alloc(&s->fetch_buf, 5 * max_n))) return r;
+  if ((r = init_state(s.get()))) return r;
+  CK(cudaStreamSynchronize(s->stream));
+  *out = s.release();
+  return MGCFD_OK;
+}
+
+extern "C" int mgcfd_solver_reset(mgcfd_solver* s) {
+  if (!s) return set_error(MGCFD_ERR_INVALID, "null solver");
+  CK(cudaStreamSynchronize(s->stream));
+  return init_state(s);
+}
+
+extern "C" int mgcfd_solver_run(mgcfd_solver* s, int32_t ncycles) {
+  if (!s) return set_error(MGCFD_ERR_INVALID, "null solver");
+  if (ncycles < 0) return set_error(MGCFD_ERR_INVALID, "negative cycle count");
+  if (s->status) return s->status;
+  if (s->level != 0 || !s->up) return set_error(MGCFD_ERR_INVALID, "solver is not at a V-cycle boundary");
+  const bool use_graph = s->opt.use_graph && !s->opt.time_kernels;
+  for (int32_t c = 0; c < ncycles; c++) {
+    if (use_graph) {
+      if (!s->graph) {
+        // Capture one V-cycle; its launch sequence is the same every cycle.
+        cudaGraph_t g;
+        const int64_t l0 = s->launches, st0 = s->steps, c0 = s->cycle;
+        CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+        int r = enqueue_cycle(s);
+        cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
+        if (r) return r;
+        if (ce != cudaSuccess) return set_error(MGCFD_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+        cudaError_t ie = cudaGraphInstantiate(&s->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess) return set_error(MGCFD_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+        s->launches_per_cycle = s->launches - l0;
+        s->launches = l0; s->steps = st0; s->cycle = c0;
+      }
+      CK(cudaGraphLaunch(s->graph, s->stream));
+      s->launches += s->launches_per_cycle;
+      s->steps += (int64_t)(s->L.size() <= 1 ? 1 : 2 * s->L.size() - 2);
+      s->cycle++;
+    } else {
+      int r = enqueue_cycle(s);
+      if (r) return r;
+    }
+  }
+  return MGCFD_OK;
+}
+
+extern "C" int mgcfd_solver_synchronize(mgcfd_solver* s) {
+  if (!s) return set_error(MGCFD_ERR_INVALID, "null solver");
+  CK(cudaStreamSynchronize(s->stream));
+  int r = collect_timings(s);
+  if (r) return r;
+  return read_status(s);
+}
+
+extern "C" int mgcfd_solver_fetch(mgcfd_solver* s, int32_t level, int32_t q, double* host_out) {
+  if (!s || !host_out) return set_error(MGCFD_ERR_INVALID, "mgcfd_solver_fetch: null argument");
+  if (level < 0 || level >= (int)s->L.size()) return set_error(MGCFD_ERR_INVALID, "mgcfd_solver_fetch: bad level");
+  DevLevel& D = s->L[(size_t)level];
+  const int T = 256;
+  int width = 5;
+  switch (q) {
+    case MGCFD_Q_VARIABLES:
+      k_unpermute<<<grid((int64_t)D.n * 5, T), T, 0, s->stream>>>(D.n, 5, 8, D.rec, D.perm, s->fetch_buf);
+      break;
+    case MGCFD_Q_FLUXES:
+      if (D.flux) k_unpermute<<<grid((int64_t)D.n * 5, T), T, 0, s->stream>>>(D.n, 5, 5, D.flux, D.perm, s->fetch_buf);
+      else CK(cudaMemsetAsync(s->fetch_buf, 0, sizeof(double) * 5 * (size_t)D.n, s->stream));
+      break;
+    case MGCFD_Q_RESIDUALS:
+      k_unpermute<<<grid((int64_t)D.n * 5, T), T, 0, s->stream>>>(D.n, 5, 5, D.res, D.perm, s->fetch_buf);
+      break;
+    case MGCFD_Q_OLD_VARIABLES:
+      k_unpermute<<<grid((int64_t)D.n * 5, T), T, 0, s->stream>>>(D.n, 5, 5, D.old, D.perm, s->fetch_buf);
+      break;
+    case MGCFD_Q_VOLUMES:
+      width = 1;
+      k_unpermute<<<grid(D.n, T), T, 0, s->stream>>>(D.n, 1, 1, D.vol, D.perm, s->fetch_buf);
+      break;
+    case MGCFD_Q_STEP_FACTORS:
+      width = 1;
+      k_step_factors<<<grid(D.n, T), T, 0, s->stream>>>(D.n, D.vol, &s->st->dt_key[level], D.perm, s->fetch_buf);
+      break;
+    default:
+      return set_error(MGCFD_ERR_INVALID, "mgcfd_solver_fetch: unknown quantity");
+  }
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(host_out, s->fetch_buf, sizeof(double) * (size_t)width * (size_t)D.n, cudaMemcpyDeviceToHost,
+                     s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return MGCFD_OK;
+}
+
+extern "C" int mgcfd_solver_get_stats(mgcfd_solver* s, mgcfd_solver_stats* o) {
+  if (!s || !o) return set_error(MGCFD_ERR_INVALID, "mgcfd_solver_get_stats: null argument");
+  int r = mgcfd_solver_synchronize(s);
+  std::memset(o, 0, sizeof(*o));
+  o->cycles = s->cycle;
+  o->smoothing_steps = s->steps;
+  o->flux_sweeps_l0 = s->flux_sweeps;
+  o->flux_ms_l0 = s->flux_ms;
+  o->kernel_launches = s->launches;
+  o->device_bytes = s->device_bytes;
+  DevStatus h;
+  CK(cudaMemcpy(&h, s->st, sizeof(h), cudaMemcpyDeviceToHost));
+  o->rms_l0 = std::sqrt(h.rms_acc / (double)s->L[0].n);  // euler3d.cpp:537
+  o->status = r;
+  return MGCFD_OK;
+}
+
+extern "C" void mgcfd_solver_destroy(mgcfd_solver* s) { free_solver(s); }
+
+extern "C" int mgcfd_solve(int32_t nlevels, const mgcfd_level_view* levels, double mach, double aoa_deg,
+                           int32_t ncycles, const mgcfd_solver_options* opt, double* const* out_variables) {
+  if (!out_variables) return set_error(MGCFD_ERR_INVALID, "mgcfd_solve: null output");
+  mgcfd_solver* s = nullptr;
+  int r = mgcfd_solver_create(nlevels, levels, mach, aoa_deg, opt, nullptr, &s);
+  if (r) return r;
+  r = mgcfd_solver_run(s, ncycles);
+  if (!r) r = mgcfd_solver_synchronize(s);
+  for (int l = 0; !r && l < nlevels; l++)
+    if (out_variables[l]) r = mgcfd_solver_fetch(s, l, MGCFD_Q_VARIABLES, out_variables[l]);
+  mgcfd_solver_destroy(s);
+  return r;
+}

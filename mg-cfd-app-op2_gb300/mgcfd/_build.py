@@ -1,0 +1,164 @@
+"""Build recipes for the mgcfd_gb300 native code.
+
+Outputs (all git-ignored, rebuilt when a source is newer than the output):
+  mg-cfd-app-op2_gb300/lib/libmgcfd_gb300.so   the product: CUDA kernels + C ABI
+  mg-cfd-app-op2_gb300/bin/euler3d_gb300        euler3d-compatible command line driver
+  oracle/_build/liboracle.so                    the oracle (C restatement), test-only
+  oracle/_build/mgcfd_oracle_run                the oracle as a timed CPU baseline, test-only
+  oracle/_ref/euler3d_ref                       reference euler3d.cpp against the OP2
+                                                stand-in (only where the reference
+                                                sources are present)
+
+CUDA code is compiled for sm_103a only.  Host C/C++ is compiled with
+-ffp-contract=off so results are identical on x86_64 and aarch64 hosts.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import platform
+import shutil
+import subprocess
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent.parent          # mg-cfd-app-op2_gb300/
+ROOT = PKG.parent                                      # repository root
+CSRC = PKG / "csrc"
+INCLUDE = ROOT / "include"
+LIB = PKG / "lib" / "libmgcfd_gb300.so"
+CLI = PKG / "bin" / "euler3d_gb300"
+OBJ = PKG / "_build"
+ORACLE = ROOT / "oracle"
+ORACLE_LIB = ORACLE / "_build" / "liboracle.so"
+ORACLE_RUN = ORACLE / "_build" / "mgcfd_oracle_run"
+REF_BIN = ORACLE / "_ref" / "euler3d_ref"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
+                     "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
+                     f"-I{INCLUDE}", f"-I{CSRC}"]
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", f"-I{INCLUDE}", f"-I{CSRC}"]
+
+
+def _nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and Path(cand).exists():
+            return cand
+    raise RuntimeError("nvcc not found: the CUDA toolkit is required to build mgcfd_gb300")
+
+
+def _stamp_ok(directory: Path) -> bool:
+    """True when `directory` holds outputs built on this host architecture."""
+    stamp = directory / ".host"
+    return stamp.exists() and stamp.read_text().strip() == platform.machine()
+
+
+def _write_stamp(directory: Path) -> None:
+    directory.mkdir(parents=True, exist_ok=True)
+    (directory / ".host").write_text(platform.machine() + "\n")
+
+
+def _stale(out: Path, deps) -> bool:
+    if not out.exists():
+        return True
+    t = out.stat().st_mtime
+    return any(Path(d).stat().st_mtime > t for d in deps)
+
+
+def _run(cmd, cwd=None):
+    r = subprocess.run(cmd, cwd=cwd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build step failed:\n" + " ".join(map(str, cmd)) + "\n" + r.stdout + r.stderr)
+    return r
+
+
+def _headers():
+    return sorted(list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list(INCLUDE.glob("*.h")))
+
+
+def library_sources():
+    return sorted(CSRC.glob("*.cu")), sorted(p for p in CSRC.glob("*.cpp") if p.name != "euler3d_gb300.cpp")
+
+
+def build_library(force: bool = False, jobs: int | None = None) -> Path:
+    """Compile every .cu/.cpp under csrc/ and link libmgcfd_gb300.so."""
+    cu, cpp = library_sources()
+    OBJ.mkdir(parents=True, exist_ok=True)
+    force = force or not _stamp_ok(OBJ)
+    LIB.parent.mkdir(parents=True, exist_ok=True)
+    hdrs = _headers()
+    nvcc = _nvcc()
+    jobs_list = []
+    objs = []
+    for src in cu:
+        obj = OBJ / (src.name + ".o")
+        objs.append(obj)
+        if force or _stale(obj, [src] + hdrs):
+            jobs_list.append([nvcc, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)])
+    for src in cpp:
+        obj = OBJ / (src.name + ".o")
+        objs.append(obj)
+        if force or _stale(obj, [src] + hdrs):
+            jobs_list.append(["g++", *CXX_FLAGS, "-c", str(src), "-o", str(obj)])
+    if jobs_list:
+        with cf.ThreadPoolExecutor(max_workers=jobs or min(8, os.cpu_count() or 4)) as ex:
+            for f in [ex.submit(_run, c) for c in jobs_list]:
+                f.result()
+    if force or jobs_list or _stale(LIB, objs):
+        _run([nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lpthread"])
+    cli_src = CSRC / "euler3d_gb300.cpp"
+    if cli_src.exists() and (force or _stale(CLI, [cli_src, LIB] + hdrs)):
+        CLI.parent.mkdir(parents=True, exist_ok=True)
+        _run(["g++", *CXX_FLAGS, str(cli_src), "-o", str(CLI), f"-L{LIB.parent}", "-lmgcfd_gb300",
+              f"-Wl,-rpath,{LIB.parent}", "-Wl,-rpath,$ORIGIN/../lib"])
+    _write_stamp(OBJ)
+    return LIB
+
+
+def build_oracle(force: bool = False) -> Path:
+    """Compile the oracle restatement (test infrastructure only)."""
+    src = ORACLE / "mgcfd_oracle.c"
+    hdr = ORACLE / "mgcfd_oracle.h"
+    run_src = ORACLE / "oracle_run.c"
+    ORACLE_LIB.parent.mkdir(parents=True, exist_ok=True)
+    force = force or not _stamp_ok(ORACLE_LIB.parent)
+    cflags = ["-O2", "-std=c11", "-ffp-contract=off", "-fopenmp", "-fPIC"]
+    if force or _stale(ORACLE_LIB, [src, hdr]):
+        _run(["gcc", *cflags, "-shared", "-o", str(ORACLE_LIB), str(src), "-lm"])
+    if run_src.exists() and (force or _stale(ORACLE_RUN, [src, hdr, run_src])):
+        _run(["gcc", *cflags, "-o", str(ORACLE_RUN), str(run_src), str(src), "-lm"])
+    _write_stamp(ORACLE_LIB.parent)
+    return ORACLE_LIB
+
+
+def reference_dir() -> Path | None:
+    p = Path(os.environ.get("MGCFD_REFERENCE_DIR", "/root/reference"))
+    return p if (p / "euler3d.cpp").exists() else None
+
+
+def build_reference(force: bool = False) -> Path | None:
+    """Compile the unmodified reference driver against the OP2 stand-in.
+
+    Only possible where the reference sources exist; returns None elsewhere.
+    """
+    ref = reference_dir()
+    if ref is None:
+        return None
+    deps = [ORACLE / "ref_main.cpp", ORACLE / "op2shim" / "op2shim.cpp", ORACLE / "op2shim" / "op_seq.h",
+            ORACLE / "op2shim" / "op_hdf5.h", CSRC / "h5lite.cpp", CSRC / "h5lite.h"]
+    deps += sorted(ref.glob("*.h")) + [ref / "euler3d.cpp"]
+    if force or not _stamp_ok(REF_BIN.parent) or _stale(REF_BIN, deps):
+        REF_BIN.parent.mkdir(parents=True, exist_ok=True)
+        _run(["g++", "-O2", "-std=c++14", "-ffp-contract=off", "-w",
+              f"-I{ORACLE / 'op2shim'}", f"-I{CSRC}", f"-I{ref}",
+              "-o", str(REF_BIN), str(ORACLE / "ref_main.cpp"), str(ORACLE / "op2shim" / "op2shim.cpp"),
+              str(CSRC / "h5lite.cpp")])
+        _write_stamp(REF_BIN.parent)
+    return REF_BIN
+
+
+def build_all(force: bool = False) -> None:
+    with cf.ThreadPoolExecutor(max_workers=3) as ex:
+        futs = [ex.submit(build_library, force), ex.submit(build_oracle, force), ex.submit(build_reference, force)]
+        for f in futs:
+            f.result()

@@ -1,0 +1,31 @@
+import os
+import sys
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+sys.path.insert(0, str(ROOT / "mg-cfd-app-op2_gb300"))
+sys.path.insert(0, str(ROOT / "oracle"))
+sys.path.insert(0, str(Path(__file__).resolve().parent))
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+    config.addinivalue_line("markers", "reference: needs the reference sources (builds oracle/_ref)")
+
+
+@pytest.fixture(scope="session", autouse=True)
+def built():
+    """Builds the library, the oracle and (where possible) the reference binary once."""
+    from mgcfd import _build
+    _build.build_library()
+    _build.build_oracle()
+    _build.build_reference()
+    yield
+
+
+@pytest.fixture(scope="session")
+def reference_available():
+    from mgcfd import _build
+    return _build.reference_dir() is not None

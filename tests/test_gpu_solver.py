@@ -1,0 +1,163 @@
+"""Full V-cycle parity of the device solver against the oracle (GPU)."""
+import numpy as np
+import pytest
+
+import mgcfd
+import oracle as O
+from parity import DELTA_TOL, MIXED_TOL, STATE_TOL, delta_error, per_variable_errors, state_error
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle(levels, mach, aoa, cycles):
+    run = O.OracleRun(levels)
+    st, _ = run.run(mach, aoa, cycles)
+    assert st == 0
+    return run
+
+
+def _ff(mach, aoa):
+    return np.array(O.freestream(mach, aoa).ff_variable[:])
+
+
+@pytest.mark.parametrize("n,nl,cycles", [(6, 1, 3), (8, 2, 3), (9, 3, 2), (16, 3, 4), (20, 4, 2)])
+@pytest.mark.parametrize("increment", ["atomic", "gather"])
+def test_small_meshes_fp64(n, nl, cycles, increment):
+    mesh = mgcfd.HostMesh.generate(n, nl, 1000 + n)
+    levels = mesh.levels()
+    mach, aoa = 0.5, 3.0
+    ref = _oracle(levels, mach, aoa, cycles)
+    s = mgcfd.Solver(mesh, mach, aoa, increment=increment)
+    s.run(cycles)
+    assert s.synchronize() == 0
+    x0 = _ff(mach, aoa)
+    for l in range(nl):
+        r = ref.get(l, O.Q_VARIABLES)
+        x = s.fetch(l)
+        assert state_error(x, r) <= STATE_TOL, (l, state_error(x, r))
+        assert delta_error(x, r, x0) <= DELTA_TOL, (l, delta_error(x, r, x0))
+        np.testing.assert_allclose(s.fetch(l, mgcfd.Q_VOLUMES), ref.get(l, O.Q_VOLUMES), rtol=1e-14)
+        np.testing.assert_allclose(s.fetch(l, mgcfd.Q_STEP_FACTORS), ref.get(l, O.Q_STEP_FACTORS), rtol=1e-12)
+        np.testing.assert_allclose(s.fetch(l, mgcfd.Q_RESIDUALS), ref.get(l, O.Q_RESIDUALS),
+                                   rtol=0, atol=1e-9 * np.abs(ref.get(l, O.Q_RESIDUALS)).max() + 1e-300)
+
+
+@pytest.mark.parametrize("renumber", ["none", "spatial", "rcm"])
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_config0_mesh_fp64(renumber, use_graph):
+    """48^3, 3 levels, 10 V-cycles, Mach 0.5, 3 degrees: the reference's CPU case."""
+    mesh = mgcfd.HostMesh.generate(48, 3, 1234)
+    levels = mesh.levels()
+    mach, aoa, cycles = 0.5, 3.0, 10
+    ref = _oracle(levels, mach, aoa, cycles)
+    s = mgcfd.Solver(mesh, mach, aoa, renumber=renumber, use_graph=use_graph)
+    s.run(cycles)
+    assert s.synchronize() == 0
+    st = s.stats()
+    assert st.cycles == cycles and st.smoothing_steps == ref.smoothing_steps
+    x0 = _ff(mach, aoa)
+    for l in range(3):
+        r = ref.get(l, O.Q_VARIABLES)
+        x = s.fetch(l)
+        assert state_error(x, r) <= STATE_TOL
+        assert delta_error(x, r, x0) <= DELTA_TOL
+
+
+def test_mixed_precision_error_bound():
+    mesh = mgcfd.HostMesh.generate(32, 3, 77)
+    levels = mesh.levels()
+    mach, aoa, cycles = 0.8, 3.0, 5
+    ref = _oracle(levels, mach, aoa, cycles)
+    s = mgcfd.Solver(mesh, mach, aoa, precision="mixed")
+    s.run(cycles)
+    assert s.synchronize() == 0
+    x0 = _ff(mach, aoa)
+    for l in range(3):
+        r = ref.get(l, O.Q_VARIABLES)
+        x = s.fetch(l)
+        mx, l2 = per_variable_errors(x, r)  # relative to each variable's magnitude
+        assert mx.max() <= MIXED_TOL and l2.max() <= MIXED_TOL, (mx, l2)
+        assert delta_error(x, r, x0) <= 1e-4   # FP32 flux: the change itself is right to ~1e-6
+
+
+def test_run_in_pieces_equals_one_run():
+    mesh = mgcfd.HostMesh.generate(12, 3, 5)
+    a = mgcfd.Solver(mesh, 0.5, 3.0, increment="gather")
+    a.run(4)
+    assert a.synchronize() == 0
+    b = mgcfd.Solver(mesh, 0.5, 3.0, increment="gather")
+    b.run(1)
+    b.run(3)
+    assert b.synchronize() == 0
+    for l in range(3):
+        np.testing.assert_array_equal(a.fetch(l), b.fetch(l))  # gather strategy is deterministic
+    b.reset()
+    b.run(4)
+    assert b.synchronize() == 0
+    np.testing.assert_array_equal(a.fetch(0), b.fetch(0))
+
+
+def test_negative_volume_reports_negative_dt():
+    """Legacy-mode volumes (the "areas" dataset) with a negative entry give
+    min_dt < 0; the device detects it (euler3d.cpp:480-484) and the host gets a
+    status, the same outcome as the oracle's abort."""
+    mesh = mgcfd.HostMesh.generate(8, 2, 3)
+    levels = mesh.levels()
+    ref = O.OracleRun(levels)
+    assert ref.run(0.5, 3.0, 1)[0] == 0
+    legacy = []
+    for l, L in enumerate(levels):
+        vols = ref.get(l, O.Q_VOLUMES).copy()
+        if l == 1:
+            vols[3] = -vols[3]
+        legacy.append(mgcfd.Level(coords=L.coords, edge_to_nodes=L.edge_to_nodes, bnd_to_node=L.bnd_to_node,
+                                  bnd_group=L.bnd_group, edge_weights=ref.get(l, O.Q_EWT) / 1e-7,
+                                  bnd_weights=L.bnd_weights, node_to_mg=L.node_to_mg, volumes=vols))
+    assert O.OracleRun(legacy).run(0.5, 3.0, 2)[0] == 1
+    s = mgcfd.Solver(legacy, 0.5, 3.0)
+    s.run(2)
+    assert s.synchronize() == mgcfd._lib.ERR_NEGATIVE_DT
+    assert "min_dt" in mgcfd._lib.load().mgcfd_last_error().decode()
+
+
+def test_legacy_volumes_match_oracle():
+    mesh = mgcfd.HostMesh.generate(10, 2, 11)
+    levels = mesh.levels()
+    ref = O.OracleRun(levels)
+    assert ref.run(0.5, 3.0, 0)[0] == 0
+    legacy = [mgcfd.Level(coords=L.coords, edge_to_nodes=L.edge_to_nodes, bnd_to_node=L.bnd_to_node,
+                          bnd_group=L.bnd_group, edge_weights=ref.get(l, O.Q_EWT) / 1e-7 * 1.0,
+                          bnd_weights=L.bnd_weights, node_to_mg=L.node_to_mg,
+                          volumes=ref.get(l, O.Q_VOLUMES) * 1.5)
+              for l, L in enumerate(levels)]
+    ref2 = _oracle(legacy, 0.5, 3.0, 3)
+    s = mgcfd.Solver(legacy, 0.5, 3.0)
+    s.run(3)
+    assert s.synchronize() == 0
+    for l in range(2):
+        assert state_error(s.fetch(l), ref2.get(l, O.Q_VARIABLES)) <= STATE_TOL
+
+
+def test_nan_state_reports_bad_values():
+    mesh = mgcfd.HostMesh.generate(8, 2, 3)
+    levels = mesh.levels()
+    bad = [mgcfd.Level(**{k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in L.__dict__.items()})
+           for L in levels]
+    bad[0].edge_weights[0, :] = np.nan  # poisons the flux of two nodes at level 0
+    s = mgcfd.Solver(bad, 0.5, 3.0)
+    s.run(2)
+    assert s.synchronize() == mgcfd._lib.ERR_BAD_VALUES
+    assert "Bad variable values" in mgcfd._lib.load().mgcfd_last_error().decode()
+    with pytest.raises(mgcfd._lib.MgcfdError):
+        s.run(1)
+
+
+def test_solve_entry_point_matches_solver():
+    mesh = mgcfd.HostMesh.generate(10, 2, 9)
+    levels = mesh.levels()
+    outs = mgcfd.solve(levels, 0.6, 2.0, 3, increment="gather")
+    s = mgcfd.Solver(levels, 0.6, 2.0, increment="gather")
+    s.run(3)
+    assert s.synchronize() == 0
+    for l in range(2):
+        np.testing.assert_array_equal(outs[l], s.fetch(l))
