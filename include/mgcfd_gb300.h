@@ -182,6 +182,21 @@ int mgcfd_op_up_post(int32_t ncoarse, double* coarse_variables, const int32_t* u
 int mgcfd_op_down(int32_t nfine, int32_t ncoarse, const int32_t* node_to_mg, double* fine_variables,
                   const double* fine_residuals, const double* fine_coords, const double* coarse_residuals,
                   const double* coarse_coords, void* stream);
+/* Restriction (up_pre + up + up_post) that allocates nothing.  It has no
+ * counterpart in the reference: the reference, like mgcfd_op_up*, needs a
+ * caller-provided per-coarse-node count buffer (p_up_scratch).  This variant
+ * is for callers that cannot call cudaMalloc -- a host framework that owns
+ * all device memory through its own allocator, or code that must not
+ * allocate between time steps -- and keeps the counts in a fixed device
+ * array inside the library instead.  Limit: ncoarse <= 1,048,576 (larger
+ * levels are rejected with MGCFD_ERR_INVALID); the 4 MiB array stays
+ * resident on every GPU that loads the library until the process exits.
+ * Every call shares the array and clears the part it uses; calls that
+ * overlap on the GPU race and give wrong results.  The first call on each
+ * device looks up the array's address (cudaGetSymbolAddress); make it
+ * before any stream capture.  Out-of-range map entries are skipped. */
+int mgcfd_op_restrict_noalloc(int32_t nfine, int32_t ncoarse, const int32_t* node_to_mg,
+                              const double* fine_variables, double* coarse_variables, void* stream);
 /* Number of elements the mapped entry points above skipped because a map
  * entry was outside [0, set size) since the last reset; reset != 0 zeroes the
  * counter.  Reads a device counter: call after the streams used are idle. */

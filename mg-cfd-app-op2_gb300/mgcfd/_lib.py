@@ -85,6 +85,7 @@ SIGNATURES = {
     "mgcfd_op_up_post": (C.c_int, [_i32, _vp, _vp, _vp]),
     "mgcfd_op_down": (C.c_int, [_i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "mgcfd_op_map_errors": (C.c_int, [_pp(C.c_int64), _i32]),
+    "mgcfd_op_restrict_noalloc": (C.c_int, [_i32, _i32, _vp, _vp, _vp, _vp]),
     "mgcfd_op_count_differences": (C.c_int, [_i32, _vp, _vp, _vp, _vp]),
     "mgcfd_solver_default_options": (None, [_pp(SolverOptions)]),
     "mgcfd_solver_create": (C.c_int, [_i32, _pp(LevelView), C.c_double, C.c_double, _pp(SolverOptions), _vp,
