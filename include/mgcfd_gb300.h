@@ -101,8 +101,11 @@ int mgcfd_host_mesh_generate(int n, int nlevels, uint64_t seed, mgcfd_host_mesh*
  * edge weights are not re-oriented (euler3d.cpp:416-431 is skipped). */
 int mgcfd_host_mesh_load(const char* input_file, const char* input_dir, int legacy_mode,
                          mgcfd_host_mesh** out);
-/* Write "<dir>/<prefix>L<l>.h5" per level and "<dir>/input.dat". */
-int mgcfd_host_mesh_write(const mgcfd_host_mesh* mesh, const char* dir, const char* prefix);
+/* Write "<dir>/<prefix>L<l>.h5" per level and "<dir>/input.dat".  With
+ * legacy_datasets != 0 the files also hold the legacy-mode datasets
+ * ("*.renumbered", "areas", "edge_weights.recalculated"; euler3d.cpp:247-309). */
+int mgcfd_host_mesh_write(const mgcfd_host_mesh* mesh, const char* dir, const char* prefix,
+                          int32_t legacy_datasets);
 int mgcfd_host_mesh_num_levels(const mgcfd_host_mesh* mesh);
 /* Views stay valid until the mesh is destroyed. */
 int mgcfd_host_mesh_level(const mgcfd_host_mesh* mesh, int level, mgcfd_level_view* out);
@@ -229,7 +232,9 @@ typedef struct mgcfd_solver_options {
   int32_t measure_mem_bound; /* also run unstructured_stream each RK stage (-b)   */
   int32_t block_size;        /* threads per block of the edge kernels; 0 = default */
   int32_t time_kernels;      /* record CUDA events around level-0 flux sweeps      */
-  int32_t reserved[9];
+  int32_t host_setup;        /* build the mesh tables on the host instead of the GPU
+                                (always on for MGCFD_RENUMBER_RCM); same results      */
+  int32_t reserved[8];
 } mgcfd_solver_options;
 
 typedef struct mgcfd_solver_stats {
@@ -256,12 +261,42 @@ int mgcfd_solver_create(int32_t nlevels, const mgcfd_level_view* levels, double 
 int mgcfd_solver_reset(mgcfd_solver* s);
 /* Enqueue `ncycles` V-cycles (euler3d.cpp:458-641).  Asynchronous. */
 int mgcfd_solver_run(mgcfd_solver* s, int32_t ncycles);
+/* Enqueue one iteration of the reference's V-cycle loop (euler3d.cpp:458-640):
+ * one smoothing step at the current level followed by its restriction or
+ * prolongation.  *smoothed_level (may be NULL) receives the level smoothed and
+ * *cycles_done the number of completed V-cycles afterwards.  The level-0
+ * state after a step that smoothed level 0 is the state euler3d.cpp:552-571
+ * writes with -I. */
+int mgcfd_solver_step(mgcfd_solver* s, int32_t* smoothed_level, int64_t* cycles_done);
 /* Wait for enqueued work; returns the sticky status. */
 int mgcfd_solver_synchronize(mgcfd_solver* s);
 /* Copy a per-node quantity of one level to host memory in the caller's
  * (input) node order.  Synchronises. */
 int mgcfd_solver_fetch(mgcfd_solver* s, int32_t level, int32_t quantity, double* host_out);
 int mgcfd_solver_get_stats(mgcfd_solver* s, mgcfd_solver_stats* out);
+/* Internal per-level tables, for inspection and tests (renumbered order). */
+enum {
+  MGCFD_T_PERM = 0,      /* int32 [N]      new id -> input id                           */
+  MGCFD_T_EDGES = 1,     /* int32 [E][2]   (a, b), a < b, sorted                         */
+  MGCFD_T_WEIGHTS = 2,   /* f64   [E][4]   (-wx/2, -wy/2, -wz/2, -|w|*smoothing/2)       */
+  MGCFD_T_VOLUMES = 3,   /* f64   [N]                                                    */
+  MGCFD_T_INV_VOL = 4,   /* f64   [N]                                                    */
+  MGCFD_T_CBRT_VOL = 5,  /* f64   [N]                                                    */
+  MGCFD_T_BIDX = 6,      /* int32 [N]      boundary row or -1                            */
+  MGCFD_T_BDATA = 7,     /* f64   [rows][12]                                             */
+  MGCFD_T_N2MG = 8,      /* int32 [N]      coarse parent (not on the coarsest level)      */
+  MGCFD_T_DVEC = 9,      /* f64   [N][4]                                                 */
+  MGCFD_T_CH_OFF = 10,   /* int32 [N+1]    children offsets (not on the finest level)     */
+  MGCFD_T_CH_LIST = 11,  /* int32 [N_fine]                                                */
+  MGCFD_T_A_OFF = 12,    /* int32 [N+1]    gather strategy only                          */
+  MGCFD_T_B_OFF = 13,    /* int32 [N+1]    gather strategy only                          */
+  MGCFD_T_B_LIST = 14    /* int32 [E]      gather strategy only                          */
+};
+/* Copies table `table` of `level` into host_out if capacity_bytes suffices;
+ * *bytes receives the table's size (0 if the table does not exist).  With
+ * host_out == NULL only the size is returned. */
+int mgcfd_solver_table(mgcfd_solver* s, int32_t level, int32_t table, void* host_out, int64_t capacity_bytes,
+                       int64_t* bytes);
 void mgcfd_solver_destroy(mgcfd_solver* s);
 
 /* One full solve through host buffers: upload the mesh, initialise, run

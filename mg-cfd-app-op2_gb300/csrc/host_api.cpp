@@ -268,10 +268,12 @@ extern "C" int mgcfd_host_mesh_load(const char* input_file, const char* input_di
   return MGCFD_OK;
 }
 
-extern "C" int mgcfd_host_mesh_write(const mgcfd_host_mesh* mesh, const char* dir, const char* prefix) {
+extern "C" int mgcfd_host_mesh_write(const mgcfd_host_mesh* mesh, const char* dir, const char* prefix,
+                                     int32_t legacy_datasets) {
   if (!mesh || !dir) return set_error(MGCFD_ERR_INVALID, "mgcfd_host_mesh_write: null argument");
   std::string err;
-  if (!mgcfd::write_mesh_files(mesh->mesh, dir, prefix ? prefix : "", &err)) return set_error(MGCFD_ERR_IO, err);
+  if (!mgcfd::write_mesh_files(mesh->mesh, dir, prefix ? prefix : "", legacy_datasets != 0, &err))
+    return set_error(MGCFD_ERR_IO, err);
   return MGCFD_OK;
 }
 

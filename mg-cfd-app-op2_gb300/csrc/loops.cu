@@ -141,13 +141,13 @@ __global__ void k_flux_edge(int32_t ne, int32_t nn, const int32_t* __restrict__ 
     const double wx = ewt[3 * e], wy = ewt[3 * e + 1], wz = ewt[3 * e + 2];
     const double wfac = -sqrt(wx * wx + wy * wy + wz * wz) * sc * 0.5;
     double f[5];
-    edge_flux(a, b, wx, wy, wz, wfac, f);
+    edge_flux(a, b, -0.5 * wx, -0.5 * wy, -0.5 * wz, wfac, f);
     double* fa = flux + 5 * (int64_t)ia;
     double* fb = flux + 5 * (int64_t)ib;
 #pragma unroll
     for (int k = 0; k < 5; k++) {
       atomicAdd(fa + k, f[k]);
-      atomicAdd(fb + k, -f[k]);
+      atomicAdd(fb + k, negate(f[k]));
     }
   }
 }

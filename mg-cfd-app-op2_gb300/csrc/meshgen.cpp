@@ -186,10 +186,32 @@ bool generate_lattice_mesh(int n, int nlevels, uint64_t seed, HostMesh* out, std
 }
 
 bool write_mesh_files(const HostMesh& mesh, const std::string& dir, const std::string& prefix,
-                      std::string* err) {
+                      bool legacy_datasets, std::string* err) {
   const int nl = (int)mesh.levels.size();
   for (int l = 0; l < nl; l++) {
     const HostLevel& L = mesh.levels[l];
+    std::vector<double> areas, recalculated;
+    if (legacy_datasets) {  // misc.h:40-76 in edge order
+      areas.assign((size_t)L.nnodes, 0.0);
+      recalculated = L.edge_weights;
+      for (int32_t e = 0; e < L.nedges; e++) {
+        const int32_t a = L.edge_to_nodes[2 * (size_t)e], b = L.edge_to_nodes[2 * (size_t)e + 1];
+        double d[3], dist = 0.0, area = 0.0;
+        for (int i = 0; i < 3; i++) {
+          d[i] = L.coords[3 * (size_t)b + i] - L.coords[3 * (size_t)a + i];
+          dist += d[i] * d[i];
+        }
+        dist = std::sqrt(dist);
+        double* w = &recalculated[3 * (size_t)e];
+        for (int i = 0; i < 3; i++) area += w[i] * w[i];
+        area = std::sqrt(area);
+        const double tv = (1.0 / 3.0) * 0.5 * dist * area;
+        areas[(size_t)a] += tv;
+        areas[(size_t)b] += tv;
+        for (int i = 0; i < 3; i++) w[i] = (d[i] / dist) * area;
+        for (int i = 0; i < 3; i++) w[i] /= dist;
+      }
+    }
     std::vector<h5lite::DatasetOut> sets = {
         {"node_coordinates", h5lite::F64, (uint64_t)L.nnodes, 3, L.coords.data(), false},
         {"edge-->node", h5lite::I32, (uint64_t)L.nedges, 2, L.edge_to_nodes.data(), false},
@@ -200,6 +222,15 @@ bool write_mesh_files(const HostMesh& mesh, const std::string& dir, const std::s
     };
     if (!L.node_to_mg.empty())
       sets.push_back({"node-->mg_node", h5lite::I32, (uint64_t)L.nnodes, 1, L.node_to_mg.data(), false});
+    if (legacy_datasets) {
+      sets.push_back({"node_coordinates.renumbered", h5lite::F64, (uint64_t)L.nnodes, 3, L.coords.data(), false});
+      sets.push_back({"edge-->node.renumbered", h5lite::I32, (uint64_t)L.nedges, 2, L.edge_to_nodes.data(), false});
+      sets.push_back({"bnd_node-->node.renumbered", h5lite::I32, (uint64_t)L.nbnd, 1, L.bnd_to_node.data(), false});
+      sets.push_back({"areas", h5lite::F64, (uint64_t)L.nnodes, 1, areas.data(), false});
+      sets.push_back({"edge_weights.recalculated", h5lite::F64, (uint64_t)L.nedges, 3, recalculated.data(), false});
+      if (!L.node_to_mg.empty())
+        sets.push_back({"node-->mg_node.renumbered", h5lite::I32, (uint64_t)L.nnodes, 1, L.node_to_mg.data(), false});
+    }
     std::string path = dir + "/" + prefix + "L" + std::to_string(l) + ".h5";
     if (!h5lite::write_file(path, sets, err)) return false;
   }

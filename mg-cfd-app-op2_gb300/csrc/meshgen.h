@@ -52,8 +52,12 @@ struct HostMesh {
 bool generate_lattice_mesh(int n, int nlevels, uint64_t seed, HostMesh* out, std::string* err);
 
 // Write level files "<prefix>L<l>.h5" and "<dir>/input.dat" (base_array_index=0,
-// mesh_name=fvcorr) in the layout euler3d.cpp reads.
+// mesh_name=fvcorr) in the layout euler3d.cpp reads.  With legacy_datasets the
+// files also carry the legacy-mode datasets of euler3d.cpp:247-309
+// ("*.renumbered" copies, "areas" = dual volumes and
+// "edge_weights.recalculated" = re-oriented weights, both computed as
+// misc.h:40-76 does in edge order).
 bool write_mesh_files(const HostMesh& mesh, const std::string& dir, const std::string& prefix,
-                      std::string* err);
+                      bool legacy_datasets, std::string* err);
 
 }  // namespace mgcfd

@@ -131,8 +131,7 @@ void rcm_order(int32_t n, int32_t ne, const int32_t* e2n, std::vector<int32_t>* 
   perm->swap(order);
 }
 
-int prepare_mesh(int32_t nlevels, const mgcfd_level_view* lv, const mgcfd_freestream& ff, int renumber,
-                 std::vector<PreparedLevel>* out) {
+int validate_views(int32_t nlevels, const mgcfd_level_view* lv, bool check_maps) {
   if (nlevels < 1 || !lv) return set_error(MGCFD_ERR_INVALID, "need at least one level");
   for (int l = 0; l < nlevels; l++) {
     const mgcfd_level_view& v = lv[l];
@@ -143,6 +142,7 @@ int prepare_mesh(int32_t nlevels, const mgcfd_level_view* lv, const mgcfd_freest
       return set_error(MGCFD_ERR_INVALID, "level " + std::to_string(l) + ": null array");
     if (l + 1 < nlevels && !v.node_to_mg)
       return set_error(MGCFD_ERR_INVALID, "level " + std::to_string(l) + ": node_to_mg required above the coarsest level");
+    if (!check_maps) continue;
     for (int64_t i = 0; i < 2 * (int64_t)v.nedges; i++)
       if (v.edge_to_nodes[i] < 0 || v.edge_to_nodes[i] >= v.nnodes)
         return set_error(MGCFD_ERR_INVALID, "level " + std::to_string(l) + ": edge-->node entry out of range");
@@ -154,6 +154,13 @@ int prepare_mesh(int32_t nlevels, const mgcfd_level_view* lv, const mgcfd_freest
         if (v.node_to_mg[i] < 0 || v.node_to_mg[i] >= lv[l + 1].nnodes)
           return set_error(MGCFD_ERR_INVALID, "level " + std::to_string(l) + ": node-->mg_node entry out of range");
   }
+  return MGCFD_OK;
+}
+
+int prepare_mesh(int32_t nlevels, const mgcfd_level_view* lv, const mgcfd_freestream& ff, int renumber,
+                 std::vector<PreparedLevel>* out) {
+  int vr = validate_views(nlevels, lv, true);
+  if (vr) return vr;
   out->assign((size_t)nlevels, PreparedLevel());
   const double sc = ff.smoothing_coefficient;
   for (int l = 0; l < nlevels; l++) {
@@ -230,9 +237,9 @@ int prepare_mesh(int32_t nlevels, const mgcfd_level_view* lv, const mgcfd_freest
       P.e2n[2 * (size_t)k + 1] = nb_[(size_t)e];
       const double* w = &ewt[3 * (size_t)e];
       const double mag = std::sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
-      P.w4[4 * (size_t)k + 0] = w[0];
-      P.w4[4 * (size_t)k + 1] = w[1];
-      P.w4[4 * (size_t)k + 2] = w[2];
+      P.w4[4 * (size_t)k + 0] = -0.5 * w[0];  // flux.h:147 factor_x etc.
+      P.w4[4 * (size_t)k + 1] = -0.5 * w[1];
+      P.w4[4 * (size_t)k + 2] = -0.5 * w[2];
       P.w4[4 * (size_t)k + 3] = -mag * sc * 0.5;  // flux.h:139 factor without the speed sum
     }
     P.b_off.assign((size_t)n + 1, 0);

@@ -20,7 +20,7 @@ struct PreparedLevel {
   std::vector<int32_t> inv;        // input id -> new id
   std::vector<double> vol;         // [n] dual volumes (new order)
   std::vector<int32_t> e2n;        // [ne][2] new ids, a < b, sorted by (a, b)
-  std::vector<double> w4;          // [ne][4] (wx, wy, wz, -|w| * smoothing * 0.5), damped
+  std::vector<double> w4;          // [ne][4] (-wx/2, -wy/2, -wz/2, -|w| * smoothing * 0.5), damped
   std::vector<int32_t> a_off;      // [n+1] edges with first node a occupy [a_off[a], a_off[a+1])
   std::vector<int32_t> b_off;      // [n+1] CSR of edges by second node
   std::vector<int32_t> b_list;     // [ne]
@@ -32,6 +32,9 @@ struct PreparedLevel {
   std::vector<int32_t> ch_list;    // [n_fine]
   int32_t nb = 0;
 };
+
+// Sizes, null pointers and (when check_maps) every map entry of the views.
+int validate_views(int32_t nlevels, const mgcfd_level_view* levels, bool check_maps);
 
 // Returns MGCFD_OK or an error status (message via set_error).
 int prepare_mesh(int32_t nlevels, const mgcfd_level_view* levels, const mgcfd_freestream& ff, int renumber,

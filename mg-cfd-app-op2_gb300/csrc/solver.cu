@@ -8,7 +8,7 @@
 //   rec32  [N][8]  f32  the same in FP32 (mixed precision only)
 //   old, res, flux [N][5] f64; inv_vol, cbrt_vol, vol [N] f64
 //   e2n    [E]     int2 (a < b, sorted by a then b); w4 [E] double4
-//                       (wx, wy, wz, -|w|*smoothing*0.5) or float4 (mixed)
+//                       (-wx/2, -wy/2, -wz/2, -|w|*smoothing*0.5) or float4 (mixed)
 //   fe     [E][5]  f64  per-edge fluxes (gather increment strategy only)
 //   bidx [N] int32 and bdata [NB][12] f64: boundary entries folded per node
 //   n2mg [N], dvec [N] double4: prolongation parent and |dx|,|dy|,|dz|,dist
@@ -33,33 +33,23 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <vector>
 
 #include "common.h"
 #include "device_math.cuh"
 #include "setup.h"
+#include "solver_internal.h"
 
 using namespace mgcfd;
 
 namespace {
 
-constexpr int kMaxLevels = 16;
 constexpr int kNodeThreads = 256;
 
-struct DevStatus {
-  unsigned long long dt_key[kMaxLevels];  // order-preserving key of each level's last min_dt
-  int halt;                                // non-zero: stop all further work
-  int neg_dt;                              // min_dt < 0 seen
-  int bad_count;                           // NaN/Inf count at level 0
-  int pad;
-  double rms_acc;                          // sum of residual^2, last level-0 step
-};
 
-#define CK(call)                                                                                         \
-  do {                                                                                                   \
-    cudaError_t e_ = (call);                                                                             \
-    if (e_ != cudaSuccess) return set_error(MGCFD_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
-  } while (0)
+
+
 
 // ---------------------------------------------------------------------------
 // Kernels.
@@ -110,16 +100,27 @@ __device__ __forceinline__ NodePrimF load_rec32(const float* rec32, int64_t i) {
 }
 
 __device__ __forceinline__ void edge_flux_f32(const NodePrimF& a, const NodePrimF& b, float4 w, float f[5]) {
-  const float mwa = a.mx * w.x + a.my * w.y + a.mz * w.z;
-  const float mwb = b.mx * w.x + b.my * w.y + b.mz * w.z;
-  const float uwa = mwa * a.rinv, uwb = mwb * b.rinv;
+  // w = (-wx/2, -wy/2, -wz/2, wfac), as edge_flux in device_math.cuh.
+  const float mha = a.mx * w.x + a.my * w.y + a.mz * w.z;
+  const float mhb = b.mx * w.x + b.my * w.y + b.mz * w.z;
+  const float uha = mha * a.rinv, uhb = mhb * b.rinv;
   const float fac = w.w * (a.s + b.s);
   const float pp = a.p + b.p;
-  f[0] = fac * (a.rho - b.rho) - 0.5f * (mwa + mwb);
-  f[1] = fac * (a.mx - b.mx) - 0.5f * (a.mx * uwa + b.mx * uwb + pp * w.x);
-  f[2] = fac * (a.my - b.my) - 0.5f * (a.my * uwa + b.my * uwb + pp * w.y);
-  f[3] = fac * (a.mz - b.mz) - 0.5f * (a.mz * uwa + b.mz * uwb + pp * w.z);
-  f[4] = fac * (a.rhoE - b.rhoE) - 0.5f * ((a.rhoE + a.p) * uwa + (b.rhoE + b.p) * uwb);
+  f[0] = fac * (a.rho - b.rho) + (mha + mhb);
+  f[1] = fac * (a.mx - b.mx) + (a.mx * uha + b.mx * uhb + pp * w.x);
+  f[2] = fac * (a.my - b.my) + (a.my * uha + b.my * uhb + pp * w.y);
+  f[3] = fac * (a.mz - b.mz) + (a.mz * uha + b.mz * uhb + pp * w.z);
+  f[4] = fac * (a.rhoE - b.rhoE) + ((a.rhoE + a.p) * uha + (b.rhoE + b.p) * uhb);
+}
+
+// 1/vol and cbrt(vol) on the device for both setup paths, so the solver's
+// constants do not depend on the host's libm.
+__global__ void k_vol_constants(int32_t n, const double* __restrict__ vol, double* __restrict__ inv_vol,
+                                double* __restrict__ cbrt_vol) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  inv_vol[i] = __ddiv_rn(1.0, vol[i]);
+  cbrt_vol[i] = cbrt(vol[i]);
 }
 
 // Freestream state into rec (initialize_variables_kernel, misc.h:10-16).
@@ -191,7 +192,7 @@ __global__ void k_flux_f64(int32_t ne, const int2* __restrict__ e2n, const doubl
 #pragma unroll
     for (int k = 0; k < 5; k++) {
       atomicAdd(fa + k, f[k]);
-      atomicAdd(fb + k, -f[k]);
+      atomicAdd(fb + k, negate(f[k]));
     }
   }
 }
@@ -220,7 +221,7 @@ __global__ void k_flux_mixed(int32_t ne, const int2* __restrict__ e2n, const flo
 #pragma unroll
     for (int k = 0; k < 5; k++) {
       atomicAdd(fa + k, (double)f[k]);
-      atomicAdd(fb + k, -(double)f[k]);
+      atomicAdd(fb + k, (double)-f[k]);
     }
   }
 }
@@ -239,11 +240,12 @@ __global__ void k_stream(int32_t ne, const int2* __restrict__ e2n, const double4
   const NodePrim b = load_rec(rec, ab.y);
   double* fa = dummy + 5 * (int64_t)ab.x;
   double* fb = dummy + 5 * (int64_t)ab.y;
-  atomicAdd(fa + 0, b.rho + w.x);
-  atomicAdd(fa + 1, b.mx + w.z);
+  // w4 holds -w/2; -2*(-w/2) recovers the weight exactly.
+  atomicAdd(fa + 0, b.rho + -2.0 * w.x);
+  atomicAdd(fa + 1, b.mx + -2.0 * w.z);
   atomicAdd(fa + 2, b.my);
   atomicAdd(fa + 3, b.mz);
-  atomicAdd(fa + 4, b.rhoE + w.y);
+  atomicAdd(fa + 4, b.rhoE + -2.0 * w.y);
   atomicAdd(fb + 0, a.rho);
   atomicAdd(fb + 1, a.mx);
   atomicAdd(fb + 2, a.my);
@@ -433,81 +435,6 @@ __global__ void k_step_factors(int32_t n, const double* __restrict__ vol, const 
 // ---------------------------------------------------------------------------
 // Host side.
 
-struct DevLevel {
-  int32_t n = 0, ne = 0, nb = 0;
-  double* rec = nullptr;
-  float* rec32 = nullptr;
-  double* old = nullptr;
-  double* flux = nullptr;
-  double* res = nullptr;
-  double* dummy = nullptr;
-  double* inv_vol = nullptr;
-  double* cbrt_vol = nullptr;
-  double* vol = nullptr;
-  int2* e2n = nullptr;
-  double4_32a* w4 = nullptr;
-  float4* w4f = nullptr;
-  double* fe = nullptr;
-  int32_t* a_off = nullptr;
-  int32_t* b_off = nullptr;
-  int32_t* b_list = nullptr;
-  int32_t* bidx = nullptr;
-  double* bdata = nullptr;
-  int32_t* n2mg = nullptr;
-  double4_32a* dvec = nullptr;
-  int32_t* ch_off = nullptr;
-  int32_t* ch_list = nullptr;
-  int32_t* perm = nullptr;
-};
-
-struct mgcfd_solver {
-  mgcfd_solver_options opt{};
-  mgcfd_freestream ff{};
-  cudaStream_t stream = nullptr;
-  bool owns_stream = false;  // graph capture needs a non-legacy stream
-  int device = 0;
-  std::vector<DevLevel> L;
-  std::vector<void*> allocs;
-  DevStatus* st = nullptr;
-  double* fetch_buf = nullptr;
-  int64_t device_bytes = 0;
-  // V-cycle state (euler3d.cpp:452-457).
-  int64_t cycle = 0;
-  int level = 0;
-  bool up = true;
-  int64_t steps = 0;
-  int64_t launches = 0;
-  int64_t launches_per_cycle = 0;
-  bool gather = false;
-  cudaGraphExec_t graph = nullptr;
-  // Kernel timing.
-  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending, spare;
-  double flux_ms = 0.0;
-  int64_t flux_sweeps = 0;
-  int status = MGCFD_OK;
-
-  template <class T>
-  int alloc(T** p, size_t count) {
-    *p = nullptr;
-    if (count == 0) return MGCFD_OK;
-    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
-    if (e != cudaSuccess) {
-      cudaGetLastError();
-      return set_error(MGCFD_ERR_NOMEM, "cudaMalloc of " + std::to_string(count * sizeof(T)) + " bytes failed: " +
-                                            cudaGetErrorString(e));
-    }
-    allocs.push_back(*p);
-    device_bytes += (int64_t)(count * sizeof(T));
-    return MGCFD_OK;
-  }
-  template <class T>
-  int upload(T** p, const void* src, size_t count) {
-    int r = alloc(p, count);
-    if (r) return r;
-    if (count) CK(cudaMemcpyAsync(*p, src, count * sizeof(T), cudaMemcpyHostToDevice, stream));
-    return MGCFD_OK;
-  }
-};
 
 namespace {
 
@@ -684,7 +611,8 @@ void free_solver(mgcfd_solver* s) {
   if (s->graph) cudaGraphExecDestroy(s->graph);
   for (auto& ev : s->pending) { cudaEventDestroy(ev.first); cudaEventDestroy(ev.second); }
   for (auto& ev : s->spare) { cudaEventDestroy(ev.first); cudaEventDestroy(ev.second); }
-  for (void* p : s->allocs) cudaFree(p);
+  for (void* p : s->allocs) cudaFreeAsync(p, s->stream);
+  if (s->stream) cudaStreamSynchronize(s->stream);
   if (s->owns_stream) cudaStreamDestroy(s->stream);
   delete s;
 }
@@ -721,34 +649,51 @@ extern "C" int mgcfd_solver_create(int32_t nlevels, const mgcfd_level_view* leve
   }
   mgcfd_freestream_init(mach, aoa_deg, &s->ff);
 
-  std::vector<PreparedLevel> P;
-  int r;
-  try {
-    r = prepare_mesh(nlevels, levels, s->ff, s->opt.renumber, &P);
-  } catch (const std::bad_alloc&) {
-    return set_error(MGCFD_ERR_NOMEM, "host allocation failed while preparing the mesh");
-  }
-  if (r) return r;
-  const bool mixed = s->opt.precision == MGCFD_PRECISION_MIXED;
+  static std::once_flag pool_once[kMaxDevices];
+  if (s->device >= 0 && s->device < kMaxDevices)
+    std::call_once(pool_once[s->device], [dev = s->device] {
+      // Keep freed solver memory in this process's pool so repeated solves
+      // (bench, serving) do not go back to the driver for every allocation.
+      cudaMemPool_t pool;
+      if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        uint64_t keep = ~0ull;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+      }
+    });
   s->L.resize((size_t)nlevels);
   size_t max_n = 0;
-  for (int l = 0; l < nlevels; l++) {
+  for (int l = 0; l < nlevels; l++) max_n = std::max(max_n, (size_t)levels[l].nnodes);
+  int r;
+  const bool host_setup = s->opt.host_setup || s->opt.renumber == MGCFD_RENUMBER_RCM;
+  if (!host_setup) {
+    if ((r = validate_views(nlevels, levels, false))) return r;
+    if ((r = device_prepare(s.get(), nlevels, levels))) return r;
+  }
+  std::vector<PreparedLevel> P;
+  if (host_setup) {
+    try {
+      r = prepare_mesh(nlevels, levels, s->ff, s->opt.renumber, &P);
+    } catch (const std::bad_alloc&) {
+      return set_error(MGCFD_ERR_NOMEM, "host allocation failed while preparing the mesh");
+    }
+    if (r) return r;
+  }
+  const bool mixed = s->opt.precision == MGCFD_PRECISION_MIXED;
+  for (int l = 0; host_setup && l < nlevels; l++) {
     PreparedLevel& p = P[(size_t)l];
     DevLevel& D = s->L[(size_t)l];
-    D.n = p.n; D.ne = p.ne; D.nb = p.nb;
-    max_n = std::max(max_n, (size_t)p.n);
-    std::vector<double> inv_vol((size_t)p.n), cbrt_vol((size_t)p.n);
-    for (int32_t i = 0; i < p.n; i++) { inv_vol[(size_t)i] = 1.0 / p.vol[(size_t)i]; cbrt_vol[(size_t)i] = std::cbrt(p.vol[(size_t)i]); }
+    D.n = p.n; D.ne = p.ne; D.nb = p.nb; D.nbrows = p.nb;
+    if (l > 0) D.nfine = P[(size_t)l - 1].n;
     if ((r = s->alloc(&D.rec, 8 * (size_t)p.n)) || (r = s->alloc(&D.old, 5 * (size_t)p.n)) ||
-        (r = s->alloc(&D.res, 5 * (size_t)p.n)) ||
-        (r = s->upload(&D.inv_vol, inv_vol.data(), (size_t)p.n)) ||
-        (r = s->upload(&D.cbrt_vol, cbrt_vol.data(), (size_t)p.n)) ||
+        (r = s->alloc(&D.res, 5 * (size_t)p.n)) || (r = s->alloc(&D.inv_vol, (size_t)p.n)) ||
+        (r = s->alloc(&D.cbrt_vol, (size_t)p.n)) ||
         (r = s->upload(&D.vol, p.vol.data(), (size_t)p.n)) ||
         (r = s->upload(&D.e2n, p.e2n.data(), (size_t)p.ne)) ||
         (r = s->upload(&D.bidx, p.bidx.data(), (size_t)p.n)) ||
         (r = s->upload(&D.bdata, p.bdata.data(), p.bdata.size())) ||
         (r = s->upload(&D.perm, p.perm.data(), (size_t)p.n)))
       return r;
+    k_vol_constants<<<grid(p.n, kNodeThreads), kNodeThreads, 0, s->stream>>>(p.n, D.vol, D.inv_vol, D.cbrt_vol);
     if (mixed) {
       std::vector<float> w4f((size_t)p.ne * 4);
       for (size_t k = 0; k < w4f.size(); k++) w4f[k] = (float)p.w4[k];
@@ -825,6 +770,17 @@ extern "C" int mgcfd_solver_run(mgcfd_solver* s, int32_t ncycles) {
   return MGCFD_OK;
 }
 
+extern "C" int mgcfd_solver_step(mgcfd_solver* s, int32_t* smoothed_level, int64_t* cycles_done) {
+  if (!s) return set_error(MGCFD_ERR_INVALID, "null solver");
+  if (s->status) return s->status;
+  const int level = s->level;
+  int r = enqueue_iteration(s);
+  if (r) return r;
+  if (smoothed_level) *smoothed_level = level;
+  if (cycles_done) *cycles_done = s->cycle;
+  return MGCFD_OK;
+}
+
 extern "C" int mgcfd_solver_synchronize(mgcfd_solver* s) {
   if (!s) return set_error(MGCFD_ERR_INVALID, "null solver");
   CK(cudaStreamSynchronize(s->stream));
@@ -885,6 +841,39 @@ extern "C" int mgcfd_solver_get_stats(mgcfd_solver* s, mgcfd_solver_stats* o) {
   CK(cudaMemcpy(&h, s->st, sizeof(h), cudaMemcpyDeviceToHost));
   o->rms_l0 = std::sqrt(h.rms_acc / (double)s->L[0].n);  // euler3d.cpp:537
   o->status = r;
+  return MGCFD_OK;
+}
+
+extern "C" int mgcfd_solver_table(mgcfd_solver* s, int32_t level, int32_t table, void* out, int64_t cap,
+                                  int64_t* bytes) {
+  if (!s || !bytes) return set_error(MGCFD_ERR_INVALID, "mgcfd_solver_table: null argument");
+  if (level < 0 || level >= (int)s->L.size()) return set_error(MGCFD_ERR_INVALID, "mgcfd_solver_table: bad level");
+  const DevLevel& D = s->L[(size_t)level];
+  const void* src = nullptr;
+  int64_t n = 0;
+  switch (table) {
+    case MGCFD_T_PERM: src = D.perm; n = 4ll * D.n; break;
+    case MGCFD_T_EDGES: src = D.e2n; n = 8ll * D.ne; break;
+    case MGCFD_T_WEIGHTS: src = D.w4; n = D.w4 ? 32ll * D.ne : 0; break;
+    case MGCFD_T_VOLUMES: src = D.vol; n = 8ll * D.n; break;
+    case MGCFD_T_INV_VOL: src = D.inv_vol; n = 8ll * D.n; break;
+    case MGCFD_T_CBRT_VOL: src = D.cbrt_vol; n = 8ll * D.n; break;
+    case MGCFD_T_BIDX: src = D.bidx; n = 4ll * D.n; break;
+    case MGCFD_T_BDATA: src = D.bdata; n = 96ll * D.nbrows; break;
+    case MGCFD_T_N2MG: src = D.n2mg; n = D.n2mg ? 4ll * D.n : 0; break;
+    case MGCFD_T_DVEC: src = D.dvec; n = D.dvec ? 32ll * D.n : 0; break;
+    case MGCFD_T_CH_OFF: src = D.ch_off; n = D.ch_off ? 4ll * (D.n + 1) : 0; break;
+    case MGCFD_T_CH_LIST: src = D.ch_list; n = D.ch_list ? 4ll * D.nfine : 0; break;
+    case MGCFD_T_A_OFF: src = D.a_off; n = D.a_off ? 4ll * (D.n + 1) : 0; break;
+    case MGCFD_T_B_OFF: src = D.b_off; n = D.b_off ? 4ll * (D.n + 1) : 0; break;
+    case MGCFD_T_B_LIST: src = D.b_list; n = D.b_list ? 4ll * D.ne : 0; break;
+    default: return set_error(MGCFD_ERR_INVALID, "mgcfd_solver_table: unknown table");
+  }
+  *bytes = src ? n : 0;
+  if (!src || n == 0 || !out) return MGCFD_OK;  // out == NULL: size query
+  if (cap < n) return set_error(MGCFD_ERR_INVALID, "mgcfd_solver_table: output too small");
+  CK(cudaStreamSynchronize(s->stream));
+  CK(cudaMemcpy(out, src, (size_t)n, cudaMemcpyDeviceToHost));
   return MGCFD_OK;
 }
 

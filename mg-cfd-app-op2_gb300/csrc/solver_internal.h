@@ -1,0 +1,116 @@
+// Internal state of the device solver, shared by solver.cu (kernels and the
+// V-cycle driver) and device_setup.cu (building the per-level tables on the
+// GPU).  Device memory comes from the stream-ordered allocator
+// (cudaMallocAsync on the solver's stream) so that repeated solves reuse
+// pooled memory instead of paying for cudaMalloc each time.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "common.h"
+
+constexpr int kMaxLevels = 16;
+constexpr int kMaxDevices = 64;
+
+#define CK(call)                                                                                         \
+  do {                                                                                                   \
+    cudaError_t e_ = (call);                                                                             \
+    if (e_ != cudaSuccess) return mgcfd::set_error(MGCFD_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+struct DevStatus {
+  unsigned long long dt_key[kMaxLevels];  // order-preserving key of each level's last min_dt
+  int halt;                                // non-zero: stop all further work
+  int neg_dt;                              // min_dt < 0 seen
+  int bad_count;                           // NaN/Inf count at level 0
+  int pad;
+  double rms_acc;                          // sum of residual^2, last level-0 step
+};
+
+struct DevLevel {
+  int32_t n = 0, ne = 0, nb = 0;
+  int32_t nbrows = 0;  // folded boundary rows in bdata
+  int32_t nfine = 0;   // fine nodes (length of ch_list) when this level has a finer one
+  double* rec = nullptr;
+  float* rec32 = nullptr;
+  double* old = nullptr;
+  double* flux = nullptr;
+  double* res = nullptr;
+  double* dummy = nullptr;
+  double* inv_vol = nullptr;
+  double* cbrt_vol = nullptr;
+  double* vol = nullptr;
+  int2* e2n = nullptr;
+  double4_32a* w4 = nullptr;
+  float4* w4f = nullptr;
+  double* fe = nullptr;
+  int32_t* a_off = nullptr;
+  int32_t* b_off = nullptr;
+  int32_t* b_list = nullptr;
+  int32_t* bidx = nullptr;
+  double* bdata = nullptr;
+  int32_t* n2mg = nullptr;
+  double4_32a* dvec = nullptr;
+  int32_t* ch_off = nullptr;
+  int32_t* ch_list = nullptr;
+  int32_t* perm = nullptr;
+};
+
+struct mgcfd_solver {
+  mgcfd_solver_options opt{};
+  mgcfd_freestream ff{};
+  cudaStream_t stream = nullptr;
+  bool owns_stream = false;  // graph capture needs a non-legacy stream
+  int device = 0;
+  std::vector<DevLevel> L;
+  std::vector<void*> allocs;
+  DevStatus* st = nullptr;
+  double* fetch_buf = nullptr;
+  int64_t device_bytes = 0;
+  // V-cycle state (euler3d.cpp:452-457).
+  int64_t cycle = 0;
+  int level = 0;
+  bool up = true;
+  int64_t steps = 0;
+  int64_t launches = 0;
+  int64_t launches_per_cycle = 0;
+  bool gather = false;
+  cudaGraphExec_t graph = nullptr;
+  // Kernel timing.
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending, spare;
+  double flux_ms = 0.0;
+  int64_t flux_sweeps = 0;
+  int status = MGCFD_OK;
+
+  template <class T>
+  int alloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) return MGCFD_OK;
+    cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(p), count * sizeof(T), stream);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return mgcfd::set_error(MGCFD_ERR_NOMEM, "device allocation of " + std::to_string(count * sizeof(T)) +
+                                            " bytes failed: " + cudaGetErrorString(e));
+    }
+    allocs.push_back(*p);
+    device_bytes += (int64_t)(count * sizeof(T));
+    return MGCFD_OK;
+  }
+  template <class T>
+  int upload(T** p, const void* src, size_t count) {
+    int r = alloc(p, count);
+    if (r) return r;
+    if (count) CK(cudaMemcpyAsync(*p, src, count * sizeof(T), cudaMemcpyHostToDevice, stream));
+    return MGCFD_OK;
+  }
+};
+
+namespace mgcfd {
+// Builds every per-level device table of `s` from the host level views on the
+// GPU (device_setup.cu).  Same results as prepare_mesh() in setup.cpp.
+int device_prepare(mgcfd_solver* s, int32_t nlevels, const mgcfd_level_view* levels);
+}  // namespace mgcfd

@@ -33,7 +33,7 @@ class LevelView(C.Structure):
 class SolverOptions(C.Structure):
     _fields_ = [("precision", C.c_int32), ("increment", C.c_int32), ("renumber", C.c_int32),
                 ("use_graph", C.c_int32), ("measure_mem_bound", C.c_int32), ("block_size", C.c_int32),
-                ("time_kernels", C.c_int32), ("reserved", C.c_int32 * 9)]
+                ("time_kernels", C.c_int32), ("host_setup", C.c_int32), ("reserved", C.c_int32 * 8)]
 
 
 class SolverStats(C.Structure):
@@ -57,7 +57,7 @@ SIGNATURES = {
     "mgcfd_freestream_init": (C.c_int, [C.c_double, C.c_double, _pp(Freestream)]),
     "mgcfd_host_mesh_generate": (C.c_int, [C.c_int, C.c_int, C.c_uint64, _pp(_vp)]),
     "mgcfd_host_mesh_load": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int, _pp(_vp)]),
-    "mgcfd_host_mesh_write": (C.c_int, [_vp, C.c_char_p, C.c_char_p]),
+    "mgcfd_host_mesh_write": (C.c_int, [_vp, C.c_char_p, C.c_char_p, _i32]),
     "mgcfd_host_mesh_num_levels": (C.c_int, [_vp]),
     "mgcfd_host_mesh_level": (C.c_int, [_vp, C.c_int, _pp(LevelView)]),
     "mgcfd_host_mesh_destroy": (None, [_vp]),
@@ -93,9 +93,11 @@ SIGNATURES = {
     "mgcfd_solver_reset": (C.c_int, [_vp]),
     "mgcfd_solver_run": (C.c_int, [_vp, _i32]),
     "mgcfd_solver_synchronize": (C.c_int, [_vp]),
+    "mgcfd_solver_step": (C.c_int, [_vp, _pp(_i32), _pp(C.c_int64)]),
     "mgcfd_solver_fetch": (C.c_int, [_vp, _i32, _i32, c_double_p]),
     "mgcfd_solver_get_stats": (C.c_int, [_vp, _pp(SolverStats)]),
     "mgcfd_solver_destroy": (None, [_vp]),
+    "mgcfd_solver_table": (C.c_int, [_vp, _i32, _i32, _vp, C.c_int64, _pp(C.c_int64)]),
     "mgcfd_solve": (C.c_int, [_i32, _pp(LevelView), C.c_double, C.c_double, _i32, _pp(SolverOptions),
                               _pp(c_double_p)]),
 }

@@ -2,7 +2,7 @@
 from __future__ import annotations
 
 import ctypes as C
-from dataclasses import dataclass
+from dataclasses import dataclass, field
 
 import numpy as np
 
@@ -21,6 +21,7 @@ class Level:
     node_to_mg: np.ndarray | None  # [N] i32 into the next level
     n_axis: int = 0
     volumes: np.ndarray | None = None  # [N] legacy-mode volumes ("areas"), else computed
+    owner: object = field(default=None, repr=False, compare=False)  # keeps zero-copy views' memory alive
 
     @property
     def nnodes(self) -> int:
@@ -66,8 +67,9 @@ class HostMesh:
                                             C.byref(h)))
         return cls(h)
 
-    def write(self, directory: str, prefix: str = "mesh_") -> None:
-        _lib.check(self._lib.mgcfd_host_mesh_write(self._h, str(directory).encode(), prefix.encode()))
+    def write(self, directory: str, prefix: str = "mesh_", legacy_datasets: bool = False) -> None:
+        _lib.check(self._lib.mgcfd_host_mesh_write(self._h, str(directory).encode(), prefix.encode(),
+                                                   int(legacy_datasets)))
 
     @property
     def num_levels(self) -> int:
@@ -94,7 +96,7 @@ class HostMesh:
                      bnd_group=_view(v.bnd_group, (v.nbnd,), np.int32),
                      edge_weights=_view(v.edge_weights, (v.nedges, 3), np.float64),
                      bnd_weights=_view(v.bnd_weights, (v.nbnd, 3), np.float64),
-                     node_to_mg=n2mg, n_axis=v.n_axis, volumes=vols)
+                     node_to_mg=n2mg, n_axis=v.n_axis, volumes=vols, owner=self)
 
     def levels(self):
         return [self.level(l) for l in range(self.num_levels)]

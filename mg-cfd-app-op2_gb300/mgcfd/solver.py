@@ -15,7 +15,7 @@ Q_VARIABLES, Q_FLUXES, Q_STEP_FACTORS, Q_VOLUMES, Q_RESIDUALS, Q_OLD_VARIABLES =
 
 
 def options(precision="fp64", increment="auto", renumber="spatial", use_graph=True, measure_mem_bound=False,
-            block_size=0, time_kernels=False) -> _lib.SolverOptions:
+            block_size=0, time_kernels=False, host_setup=False) -> _lib.SolverOptions:
     o = _lib.SolverOptions()
     _lib.load().mgcfd_solver_default_options(C.byref(o))
     o.precision = PRECISION[precision]
@@ -25,6 +25,7 @@ def options(precision="fp64", increment="auto", renumber="spatial", use_graph=Tr
     o.measure_mem_bound = int(measure_mem_bound)
     o.block_size = int(block_size)
     o.time_kernels = int(time_kernels)
+    o.host_setup = int(host_setup)
     return o
 
 
@@ -52,6 +53,12 @@ class Solver:
 
     def run(self, ncycles: int) -> None:
         _lib.check(self._lib.mgcfd_solver_run(self._h, ncycles))
+
+    def step(self):
+        """One smoothing step plus its transfer; returns (level smoothed, cycles done)."""
+        lvl, cyc = C.c_int32(), C.c_int64()
+        _lib.check(self._lib.mgcfd_solver_step(self._h, C.byref(lvl), C.byref(cyc)))
+        return lvl.value, cyc.value
 
     def synchronize(self) -> int:
         """Waits; returns the status code (0 = ok) without raising."""

@@ -1,0 +1,71 @@
+"""Tables built on the GPU (device_setup.cu) equal the host reference
+implementation (setup.cpp) exactly: permutations, edge order and
+orientation, CSR offsets and lists, boundary rows, multigrid maps, and the
+volumes and weights (both follow the reference's sequential order).  Only the
+1/vol and cube root of the volume are computed on the device in both paths."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import mgcfd
+from mgcfd import _lib
+
+pytestmark = pytest.mark.gpu
+
+TABLES = {0: ("PERM", np.int32), 1: ("EDGES", np.int32), 2: ("WEIGHTS", np.float64), 3: ("VOLUMES", np.float64),
+          4: ("INV_VOL", np.float64), 5: ("CBRT_VOL", np.float64), 6: ("BIDX", np.int32), 7: ("BDATA", np.float64),
+          8: ("N2MG", np.int32), 9: ("DVEC", np.float64), 10: ("CH_OFF", np.int32), 11: ("CH_LIST", np.int32),
+          12: ("A_OFF", np.int32), 13: ("B_OFF", np.int32), 14: ("B_LIST", np.int32)}
+
+
+def table(solver, level, t):
+    lib = _lib.load()
+    n = C.c_int64()
+    _lib.check(lib.mgcfd_solver_table(solver._h, level, t, None, 0, C.byref(n)))
+    dt = TABLES[t][1]
+    out = np.empty(n.value // np.dtype(dt).itemsize, dtype=dt)
+    if n.value:
+        _lib.check(lib.mgcfd_solver_table(solver._h, level, t, out.ctypes.data, n.value, C.byref(n)))
+    return out
+
+
+@pytest.mark.parametrize("n,nl,renumber", [(11, 3, "spatial"), (16, 4, "spatial"), (9, 2, "none"), (24, 3, "spatial")])
+def test_device_tables_equal_host_tables(n, nl, renumber):
+    mesh = mgcfd.HostMesh.generate(n, nl, 300 + n)
+    dev = mgcfd.Solver(mesh, 0.8, 3.0, increment="gather", renumber=renumber)
+    host = mgcfd.Solver(mesh, 0.8, 3.0, increment="gather", renumber=renumber, host_setup=True)
+    for l in range(nl):
+        for t, (name, _) in TABLES.items():
+            a, b = table(dev, l, t), table(host, l, t)
+            assert a.shape == b.shape, (l, name)
+            np.testing.assert_array_equal(a, b, err_msg=f"level {l} table {name}")
+
+
+def test_device_setup_rejects_out_of_range_maps():
+    mesh = mgcfd.HostMesh.generate(8, 2, 1)
+    levels = mesh.levels()
+    bad = [mgcfd.Level(**{k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in L.__dict__.items()
+                          if k != "owner"}) for L in levels]
+    bad[0].edge_to_nodes[5, 1] = bad[0].nnodes + 7
+    with pytest.raises(_lib.MgcfdError, match="out of range"):
+        mgcfd.Solver(bad, 0.5, 3.0)
+    bad[0].edge_to_nodes[5, 1] = 0
+    bad[0].node_to_mg[3] = -2
+    with pytest.raises(_lib.MgcfdError, match="out of range"):
+        mgcfd.Solver(bad, 0.5, 3.0)
+
+
+def test_legacy_mesh_on_device(tmp_path):
+    import oracle as O
+    from parity import STATE_TOL, state_error
+    mesh = mgcfd.HostMesh.generate(10, 3, 8)
+    mesh.write(str(tmp_path), "m_", legacy_datasets=True)
+    legacy = mgcfd.HostMesh.load("input.dat", str(tmp_path), legacy=True)
+    ref = O.OracleRun(legacy.levels())
+    assert ref.run(0.6, 2.0, 3)[0] == 0
+    s = mgcfd.Solver(legacy, 0.6, 2.0)
+    s.run(3)
+    assert s.synchronize() == 0
+    for l in range(3):
+        assert state_error(s.fetch(l), ref.get(l, O.Q_VARIABLES)) <= STATE_TOL

@@ -141,8 +141,8 @@ def test_legacy_volumes_match_oracle():
 def test_nan_state_reports_bad_values():
     mesh = mgcfd.HostMesh.generate(8, 2, 3)
     levels = mesh.levels()
-    bad = [mgcfd.Level(**{k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in L.__dict__.items()})
-           for L in levels]
+    bad = [mgcfd.Level(**{k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in L.__dict__.items()
+                          if k != "owner"}) for L in levels]
     bad[0].edge_weights[0, :] = np.nan  # poisons the flux of two nodes at level 0
     s = mgcfd.Solver(bad, 0.5, 3.0)
     s.run(2)
