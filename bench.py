@@ -8,6 +8,8 @@ Mach 0.8, angle of attack 3 degrees, FP64.  One step = one V-cycle
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
                   [--precision fp64|mixed] [--increment atomic|gather] [--n 200]
+  python bench.py --mode batch     # 64 uneven meshes in one launch per stage
+  python bench.py --mode serve     # Poisson request stream, p50/p99 latency
 
 Prints one JSON line.  `value` is V-cycles/s with the mesh resident in HBM,
 `e2e` is V-cycles/s through the host-buffer entry point mgcfd_solve (mesh
@@ -224,7 +226,7 @@ def run_gb300(args):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64" if args.precision == "fp64" else "f32-flux/f64-accumulate",
-        "data": "synthetic: seeded jittered 200^3 lattice, permuted ids (SURVEY 8d generator)",
+        "data": "synthetic: seeded jittered 200^3 lattice, permuted ids",
         "config": {"workload": f"{args.n}^3 jittered lattice, {NLEVELS} levels, Mach {MACH}, AoA {AOA} deg, "
                                f"{N} nodes / {E} edges on level 0",
                    "precision": args.precision, "increment": args.increment, "renumber": args.renumber,
@@ -295,6 +297,141 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_batch(args):
+    """Batched solves: 64 meshes (lattice edge log-uniform 16..96, Mach U(0.3, 0.8),
+    AoA U(0, 6) degrees, 3 levels, 20 V-cycles) solved in one batch against 64
+    sequential plain solves.  Every solve is timed through the host-buffer API:
+    upload, device setup, the V-cycles and the download of level 0."""
+    import numpy as np
+    import torch  # noqa: F401  (CUDA context for the timers below)
+
+    import mgcfd
+    from mgcfd import autotune
+    rng = np.random.default_rng(3)
+    nm = args.batch_meshes
+    sizes = np.exp(rng.uniform(np.log(16), np.log(96), nm)).round().astype(int)
+    machs = rng.uniform(0.3, 0.8, nm).tolist()
+    aoas = rng.uniform(0.0, 6.0, nm).tolist()
+    meshes = [mgcfd.HostMesh.generate(int(n), 3, 1000 + i) for i, n in enumerate(sizes)]
+    cycles = 20
+    total_nodes = sum(m.level(0).nnodes for m in meshes)
+
+    def solve_batch(**o):
+        b = mgcfd.Batch(meshes, machs, aoas, **o)
+        b.run(cycles)
+        assert b.synchronize() == 0
+        outs = [b.fetch_mesh(m, 0) for m in range(nm)]
+        b.close()
+        return outs
+
+    def solve_sequential(**o):
+        outs = []
+        for m in range(nm):
+            s = mgcfd.Solver(meshes[m], machs[m], aoas[m], **o)
+            s.run(cycles)
+            assert s.synchronize() == 0
+            outs.append(s.fetch(0))
+            s.close()
+        return outs
+
+    line = {"metric": f"batched solves/s ({nm} meshes, 16^3-96^3 lattices, 3 levels, {cycles} V-cycles)",
+            "unit": "solves/s", "higher_is_better": True, "n_gpus": 1, "data": "synthetic: seeded lattices",
+            "config": {"workload": f"{nm} meshes, {total_nodes} level-0 nodes in total, sizes {sizes.min()}^3.."
+                                   f"{sizes.max()}^3"}}
+    t0 = time.perf_counter()
+    solve_sequential(precision="fp64")  # warm-up pass (pool, graphs, clocks)
+    line["warmup_s"] = round(time.perf_counter() - t0, 3)
+    t0 = time.perf_counter()
+    seq = solve_sequential(precision="fp64")
+    t_seq = time.perf_counter() - t0
+    results = {"sequential_fp64": nm / t_seq}
+    for prec in ("fp64", "mixed"):
+        t0 = time.perf_counter()
+        best, timings = autotune.tune_batch(meshes, machs, aoas, precision=prec)
+        t_tune = time.perf_counter() - t0
+        solve_batch(**best)
+        t0 = time.perf_counter()
+        outs = solve_batch(**best)
+        dt = time.perf_counter() - t0
+        results[f"batched_{prec}"] = nm / dt
+        err = max(float(np.max(np.abs(a - b) / np.maximum(np.abs(b).max(axis=0), 1e-300))) for a, b in zip(outs, seq))
+        line[f"batched_{prec}_tuning"] = {"chosen": best, "ms_per_cycle": {f"{k[0]}/{k[1]}": round(v, 3)
+                                                                           for k, v in timings.items()},
+                                          "tuning_s": round(t_tune, 3), "max_rel_err_vs_fp64_sequential": err}
+    line["value"] = round(results["batched_fp64"], 3)
+    line["results_solves_per_s"] = {k: round(v, 3) for k, v in results.items()}
+    line["speedup_batched_fp64_vs_sequential"] = round(results["batched_fp64"] / results["sequential_fp64"], 3)
+    line["speedup_batched_mixed_vs_sequential_fp64"] = round(results["batched_mixed"] / results["sequential_fp64"], 3)
+    print(json.dumps(line), flush=True)
+
+
+def run_serve(args):
+    """Serving: a Poisson stream of requests (node count log-uniform in
+    20K..4M, Mach U(0.3, 0.85), AoA U(0, 6) degrees, 3 or 4 levels, until the
+    level-0 density residual falls to 1e-6 of its first value or 50 V-cycles)
+    served under a 150 GB HBM budget; p50/p99 latency and solves/s for the
+    mixed-precision and FP64 forms on the same stream and arrival rates."""
+    import threading
+
+    import numpy as np
+
+    import mgcfd
+    rng = np.random.default_rng(11)
+    pool = []
+    for i in range(args.serve_pool):
+        nodes = float(np.exp(rng.uniform(np.log(20e3), np.log(4e6))))
+        n = max(8, int(round(nodes ** (1.0 / 3.0))))
+        pool.append(mgcfd.HostMesh.generate(n, int(rng.integers(3, 5)), 500 + i))
+    R = args.serve_requests
+    picks = rng.integers(0, len(pool), R)
+    machs = rng.uniform(0.3, 0.85, R)
+    aoas = rng.uniform(0.0, 6.0, R)
+    gaps = rng.exponential(1.0, R)  # unit-rate inter-arrival times, scaled per rate
+
+    def serve(precision, rate):
+        srv = mgcfd.Server(hbm_budget_gb=150.0, max_active=args.serve_slots, precision=precision,
+                           increment="gather" if precision == "mixed" else "atomic", max_cycles=50,
+                           residual_drop=1e-6)
+        t_start = time.perf_counter()
+        arrivals = np.cumsum(gaps / rate)
+
+        def feeder():
+            for k in range(R):
+                delay = t_start + arrivals[k] - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                srv.submit(pool[picks[k]], float(machs[k]), float(aoas[k]))
+
+        th = threading.Thread(target=feeder)
+        th.start()
+        th.join()
+        srv.drain(3600)
+        t_end = time.perf_counter()
+        res = [r for r, _ in srv.poll()]
+        st = srv.stats()
+        srv.close()
+        lat = np.array([r["finish_s"] - r["submit_s"] for r in res])
+        ok = sum(1 for r in res if r["status"] == 0)
+        return {"rate_per_s": rate, "solves_per_s": round(len(res) / (t_end - t_start), 3),
+                "p50_ms": round(1e3 * float(np.percentile(lat, 50)), 2),
+                "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 2), "ok": ok, "failed": len(res) - ok,
+                "mean_cycles": round(float(np.mean([r["cycles"] for r in res])), 2),
+                "peak_active": int(st["peak_active"]), "peak_budget_gb": round(st["peak_bytes"] / 2 ** 30, 2)}
+
+    # Capacity probe: everything at once, FP64.
+    cap = serve("fp64", 1e9)["solves_per_s"]
+    rates = [round(f * cap, 3) for f in (0.5, 0.9, 1.5)]
+    out = {"fp64": [serve("fp64", r) for r in rates], "mixed": [serve("mixed", r) for r in rates]}
+    line = {"metric": "served solves/s and p50/p99 latency (Poisson stream)", "unit": "solves/s",
+            "higher_is_better": True, "n_gpus": 1, "data": "synthetic: seeded lattices",
+            "config": {"workload": f"{R} requests over a pool of {len(pool)} meshes "
+                                   f"({min(m.level(0).nnodes for m in pool)}..{max(m.level(0).nnodes for m in pool)} "
+                                   "nodes, 3-4 levels), HBM budget 150 GB", "slots": args.serve_slots,
+                       "fp64_capacity_solves_per_s": cap},
+            "value": max(x["solves_per_s"] for x in out["mixed"]), "by_precision": out}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -308,11 +445,20 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-cycles", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mode", default="plain", choices=["plain", "batch", "serve"])
+    ap.add_argument("--batch-meshes", type=int, default=64)
+    ap.add_argument("--serve-requests", type=int, default=200)
+    ap.add_argument("--serve-pool", type=int, default=16)
+    ap.add_argument("--serve-slots", type=int, default=16)
     args = ap.parse_args()
     if args.warmup < 0 or args.steps < 1:
         ap.error("need --steps >= 1 and --warmup >= 0")
     if args.impl == "reference":
         run_reference(args)
+    elif args.mode == "batch":
+        run_batch(args)
+    elif args.mode == "serve":
+        run_serve(args)
     else:
         run_gb300(args)
 

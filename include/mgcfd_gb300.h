@@ -111,6 +111,22 @@ int mgcfd_host_mesh_num_levels(const mgcfd_host_mesh* mesh);
 int mgcfd_host_mesh_level(const mgcfd_host_mesh* mesh, int level, mgcfd_level_view* out);
 void mgcfd_host_mesh_destroy(mgcfd_host_mesh* mesh);
 
+/* Mesh renumbering as a standalone step.  Replaces the reference's -n option
+ * (config.h:119,366; op_renumber(p_edge_to_nodes[0]) at euler3d.cpp:377, a
+ * Scotch reordering of the level-0 nodes inside OP2) with the solver's own
+ * orders, method = MGCFD_RENUMBER_SPATIAL (Morton curve of the coordinates)
+ * or MGCFD_RENUMBER_RCM (reverse Cuthill-McKee of the edge graph).
+ *
+ * mgcfd_renumber_nodes writes perm_out[new] = old for one node set.
+ * mgcfd_host_mesh_renumber returns a new mesh with every level relabelled:
+ * node data permuted, edge endpoints and boundary entries mapped through the
+ * inverse permutation (edges keep their direction and are ordered by the new
+ * (min, max) endpoint pair, boundary entries by node; ties keep input order),
+ * and node-->mg_node mapped on both sides.  The input mesh is not changed. */
+int mgcfd_renumber_nodes(int method, int32_t nnodes, const double* coords, int32_t nedges,
+                         const int32_t* edge_to_nodes, int32_t* perm_out);
+int mgcfd_host_mesh_renumber(const mgcfd_host_mesh* mesh, int method, mgcfd_host_mesh** out);
+
 /* HDF5 subset used by the reference's files (op_decl_*_hdf5 and
  * op_fetch_data_hdf5_file in euler3d.cpp).  dims receives up to 2 extents. */
 int mgcfd_h5_dataset_shape(const char* path, const char* name, int64_t dims[2], int* rank);
@@ -226,7 +242,8 @@ enum {
 
 typedef struct mgcfd_solver_options {
   int32_t precision;         /* MGCFD_PRECISION_*                                   */
-  int32_t increment;         /* MGCFD_INCREMENT_*                                   */
+  int32_t increment;         /* MGCFD_INCREMENT_*; AUTO = ATOMIC for FP64 and GATHER
+                                for MIXED (the faster of the two on GB300)         */
   int32_t renumber;          /* MGCFD_RENUMBER_*                                    */
   int32_t use_graph;         /* capture one V-cycle as a CUDA graph and replay it  */
   int32_t measure_mem_bound; /* also run unstructured_stream each RK stage (-b)   */
@@ -257,6 +274,24 @@ void mgcfd_solver_default_options(mgcfd_solver_options* opt);
  * flow to freestream.  `stream` is used for every later launch. */
 int mgcfd_solver_create(int32_t nlevels, const mgcfd_level_view* levels, double mach, double aoa_deg,
                         const mgcfd_solver_options* opt, void* stream, mgcfd_solver** out);
+/* Batched solves (many independent meshes in one launch per stage): the
+ * meshes are concatenated per level, each renumbered on its own, and every
+ * kernel of the V-cycle covers all of them.  All meshes need the same number
+ * of levels; each has its own Mach number and angle of attack, its own
+ * min_dt (euler3d.cpp:476-479 per mesh) and its own outcome: a mesh that hits
+ * min_dt < 0 or NaN/Inf is marked failed (mgcfd_solver_mesh_status) while the
+ * others continue.  levels[m] points at mesh m's nlevels level views.  The
+ * returned solver works with every mgcfd_solver_* call; fetch returns the
+ * concatenated level, fetch_mesh one mesh. */
+int mgcfd_batch_create(int32_t nmeshes, int32_t nlevels, const mgcfd_level_view* const* levels, const double* mach,
+                       const double* aoa_deg, const mgcfd_solver_options* opt, void* stream, mgcfd_solver** out);
+int mgcfd_solver_num_meshes(const mgcfd_solver* s);
+/* Copy one mesh's quantity of one level to host memory in that mesh's input order. */
+int mgcfd_solver_fetch_mesh(mgcfd_solver* s, int32_t mesh, int32_t level, int32_t quantity, double* host_out);
+/* Synchronises; returns mesh `mesh`'s status (MGCFD_OK, MGCFD_ERR_NEGATIVE_DT
+ * or MGCFD_ERR_BAD_VALUES) and its last level-0 residual norms (all
+ * variables as euler3d.cpp:537, and density only); either output may be NULL. */
+int mgcfd_solver_mesh_status(mgcfd_solver* s, int32_t mesh, double* rms_l0, double* rho_rms_l0);
 /* Back to the state right after create (freestream, counters zeroed). */
 int mgcfd_solver_reset(mgcfd_solver* s);
 /* Enqueue `ncycles` V-cycles (euler3d.cpp:458-641).  Asynchronous. */
@@ -298,6 +333,64 @@ enum {
 int mgcfd_solver_table(mgcfd_solver* s, int32_t level, int32_t table, void* host_out, int64_t capacity_bytes,
                        int64_t* bytes);
 void mgcfd_solver_destroy(mgcfd_solver* s);
+
+/* ------------------------------------------------------------------------ */
+/* Serving: solves of different meshes and freestream conditions arrive at  */
+/* any time and run concurrently on one GPU (continuous batching at V-cycle */
+/* granularity).  A worker thread admits queued requests in arrival order    */
+/* when a slot (CUDA stream) is free and the HBM budget covers the request's */
+/* estimated footprint, advances every admitted request one V-cycle at a    */
+/* time, and retires it when its level-0 density residual has dropped below */
+/* residual_drop times its first value, it fails (min_dt < 0, NaN/Inf), or  */
+/* max_cycles is reached.  A request's arithmetic is that of a solver       */
+/* running alone, so with MGCFD_INCREMENT_GATHER its result is identical    */
+/* alone and in any mix.                                                     */
+typedef struct mgcfd_server_options {
+  int64_t hbm_budget_bytes;  /* admission budget for all active requests          */
+  int32_t max_active;        /* concurrent requests (one stream each)              */
+  int32_t precision;         /* MGCFD_PRECISION_*                                  */
+  int32_t increment;         /* MGCFD_INCREMENT_*                                  */
+  int32_t max_cycles;        /* V-cycles per request at most                       */
+  double residual_drop;      /* stop when rho_rms <= residual_drop * first rho_rms */
+  int32_t reserved[8];
+} mgcfd_server_options;
+
+typedef struct mgcfd_request_result {
+  int64_t id;
+  int32_t status;            /* MGCFD_OK, _NEGATIVE_DT, _BAD_VALUES, _BUDGET, ... */
+  int32_t cycles;            /* V-cycles run                                       */
+  double submit_s, admit_s, finish_s;  /* seconds since the server started       */
+  double rho_rms_first, rho_rms_last;  /* level-0 density residual norms         */
+  int64_t reserved[2];
+} mgcfd_request_result;
+
+typedef struct mgcfd_server_stats {
+  int64_t submitted, completed, failed;
+  int64_t active, pending;
+  int64_t used_bytes, peak_bytes, peak_active;
+  int64_t reserved[4];
+} mgcfd_server_stats;
+
+typedef struct mgcfd_server mgcfd_server;
+
+void mgcfd_server_default_options(mgcfd_server_options* opt);
+int mgcfd_server_create(const mgcfd_server_options* opt, mgcfd_server** out);
+/* Queue a solve.  The level arrays must stay valid until the request has
+ * completed; out_variables_l0 (may be NULL) receives the final level-0
+ * variables [N0][5] in input order. */
+int mgcfd_server_submit(mgcfd_server* server, int32_t nlevels, const mgcfd_level_view* levels, double mach,
+                        double aoa_deg, double* out_variables_l0, int64_t* id);
+/* Move up to `capacity` completed results into out; *count receives how many. */
+int mgcfd_server_poll(mgcfd_server* server, mgcfd_request_result* out, int32_t capacity, int32_t* count);
+/* Wait until no request is queued or running (MGCFD_ERR_TIMEOUT after timeout_s). */
+int mgcfd_server_drain(mgcfd_server* server, double timeout_s);
+int mgcfd_server_get_stats(mgcfd_server* server, mgcfd_server_stats* out);
+/* Finishes every queued and running request, then frees the server. */
+void mgcfd_server_destroy(mgcfd_server* server);
+/* The device footprint the server charges against hbm_budget_bytes for a
+ * request on this mesh (state, tables and setup scratch at its peak). */
+int mgcfd_request_estimate_bytes(int32_t nlevels, const mgcfd_level_view* levels, int32_t precision,
+                                 int32_t increment, int64_t* bytes);
 
 /* One full solve through host buffers: upload the mesh, initialise, run
  * ncycles V-cycles, download every level's variables (file order) into

@@ -21,9 +21,10 @@
 //     and the weight is kept as h = -w/2 so the central term needs no
 //     multiplication by -1/2 (exact: a power-of-two scaling).
 //
-// Every operation is still an IEEE FP64 operation; results differ from the
-// reference only by rounding (relative 1e-16 per operation), far inside the
-// 1e-10 parity bar.
+// Every operation is an FP64 operation; all are IEEE-rounded except the two
+// square roots of node_prim (x * rsqrt(x), within about two ulp).  Results
+// differ from the reference only by rounding (relative 1e-16 per operation),
+// far inside the 1e-10 parity bar.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -41,6 +42,16 @@ struct NodePrim {
   double rinv;                   // 1 / rho
 };
 
+// sqrt(x) as x * rsqrt(x) for positive finite x: about 8 FMA-equivalents on
+// GB300 instead of about 10 for the correctly rounded square root, accurate
+// to about two ulp.  Zero, negative, infinite and NaN inputs (recognised from
+// the bit pattern on the integer pipe) take the IEEE square root, so the
+// special cases are exactly those of sqrt().
+__device__ __forceinline__ double sqrt_fast(double x) {
+  const long long b = __double_as_longlong(x);
+  return (b > 0 && b < 0x7ff0000000000000ll) ? x * rsqrt(x) : sqrt(x);
+}
+
 // inlined_funcs.h:98-130 with one reciprocal instead of three divisions.
 __device__ __forceinline__ NodePrim node_prim(double rho, double mx, double my, double mz, double rhoE) {
   NodePrim n;
@@ -49,7 +60,7 @@ __device__ __forceinline__ NodePrim node_prim(double rho, double mx, double my, 
   const double ux = mx * n.rinv, uy = my * n.rinv, uz = mz * n.rinv;
   const double q2 = ux * ux + uy * uy + uz * uz;
   n.p = kGammaM1 * (rhoE - 0.5 * rho * q2);
-  n.s = sqrt(q2) + sqrt(kGammaD * n.p * n.rinv);
+  n.s = sqrt_fast(q2) + sqrt_fast(kGammaD * n.p * n.rinv);
   return n;
 }
 
@@ -86,6 +97,71 @@ __device__ __forceinline__ void farfield_flux(const NodePrim& b, double wx, doub
   f[2] = 0.5 * (ffw[2] + (b.my * uw + b.p * wy));
   f[3] = 0.5 * (ffw[3] + (b.mz * uw + b.p * wz));
   f[4] = 0.5 * (ffw[4] + (b.rhoE + b.p) * uw);
+}
+
+// IEEE 754 binary32 <-> binary64 conversions on the integer pipe.
+//
+// On GB300 a cvt between float and double issues on the FP64 pipe at about
+// 1.6 FMA-equivalents each, which makes the mixed-precision path's format
+// changes cost as much as its FP64 arithmetic.  These build the result's bit
+// pattern from the operand's fields with integer operations instead
+// (IEEE 754-2008 section 3.4 encodings; binary64 exponent = binary32
+// exponent + 896), and give the same bits as the hardware conversion:
+//   f2d_bits: exact widening; zeros, subnormals (renormalised with a leading
+//             zero count), infinities and NaNs (payload kept, quiet bit kept)
+//             included;
+//   d2f_bits: narrowing with round-to-nearest-even on the 29 dropped bits;
+//             overflow rounds to infinity, NaNs keep the top payload bits and
+//             become quiet; results in the binary32 subnormal range are
+//             rounded with the same rule from the full 53-bit significand.
+__device__ __forceinline__ double f2d_bits(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t sign = u & 0x80000000u;
+  const uint32_t a = u & 0x7fffffffu;
+  uint32_t hi, lo;
+  if (a - 0x00800000u < 0x7f000000u) {  // normal: exponent field 1..254
+    hi = sign | ((a >> 3) + (896u << 20));
+    lo = u << 29;
+  } else if (a >= 0x7f800000u) {         // infinity or NaN
+    hi = sign | 0x7ff00000u | ((a & 0x7fffffu) >> 3);
+    lo = u << 29;
+  } else if (a == 0u) {
+    hi = sign;
+    lo = 0u;
+  } else {                               // subnormal: a = m * 2^-149, m < 2^23
+    const int s = __clz(a) - 8;          // a << s has bit 23 set
+    const uint32_t m = (a << s) & 0x7fffffu;
+    hi = sign | ((uint32_t)(897 - s) << 20) | (m >> 3);
+    lo = m << 29;
+  }
+  return __hiloint2double((int)hi, (int)lo);
+}
+
+__device__ __forceinline__ float d2f_bits(double d) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(d);
+  const uint32_t sign = (uint32_t)(u >> 32) & 0x80000000u;
+  const int de = (int)((u >> 52) & 0x7ff);
+  const unsigned long long m = u & 0xfffffffffffffull;
+  uint32_t r;
+  if (de > 896 && de < 1151) {           // binary32 normal range before rounding
+    const uint32_t rest = (uint32_t)(m & 0x1fffffffu);
+    r = ((uint32_t)(de - 896) << 23) | (uint32_t)(m >> 29);
+    r += (rest > 0x10000000u || (rest == 0x10000000u && (r & 1u))) ? 1u : 0u;  // carries into the exponent
+  } else if (de == 2047) {               // infinity or NaN
+    r = 0x7f800000u | (m ? (0x400000u | (uint32_t)(m >> 29)) : 0u);
+  } else if (de >= 1151) {               // beyond binary32: infinity
+    r = 0x7f800000u;
+  } else {                               // subnormal or zero in binary32
+    const int k = 926 - de;              // value / 2^-149 = full >> k, k >= 30
+    const unsigned long long full = (de ? (1ull << 52) : 0ull) | m;
+    if (k >= 64) {
+      r = 0u;
+    } else {
+      const unsigned long long q = full >> k, rem = full & ((1ull << k) - 1ull), half = 1ull << (k - 1);
+      r = (uint32_t)q + ((rem > half || (rem == half && (q & 1ull))) ? 1u : 0u);
+    }
+  }
+  return __uint_as_float(sign | r);
 }
 
 // Order-preserving map from double to uint64 (for atomicMin on doubles).

@@ -205,7 +205,7 @@ __global__ void k_edge_keys(int32_t ne, int32_t nn, const int32_t* __restrict__ 
   flip[e] = f;
 }
 
-__global__ void k_edge_finalize(int32_t ne, const unsigned long long* __restrict__ key,
+__global__ void k_edge_finalize(int32_t ne, int32_t node_off, const unsigned long long* __restrict__ key,
                                 const int32_t* __restrict__ order, const double* __restrict__ w,
                                 const unsigned char* __restrict__ flip, double sc, int2* __restrict__ e2n,
                                 double* __restrict__ w4, int32_t* __restrict__ acnt, int32_t* __restrict__ bcnt) {
@@ -213,7 +213,7 @@ __global__ void k_edge_finalize(int32_t ne, const unsigned long long* __restrict
   if (k >= ne) return;
   const int64_t e = order[k];
   const int32_t a = (int32_t)(key[k] >> 32), b = (int32_t)(key[k] & 0xffffffffu);
-  e2n[k] = make_int2(a, b);
+  e2n[k] = make_int2(a + node_off, b + node_off);
   double x = w[3 * e], y = w[3 * e + 1], z = w[3 * e + 2];
   if (flip[e]) { x = -x; y = -y; z = -z; }
   const double mag = __dsqrt_rn(sq3(x, y, z));
@@ -225,11 +225,11 @@ __global__ void k_edge_finalize(int32_t ne, const unsigned long long* __restrict
   atomicAdd(bcnt + b, 1);
 }
 
-__global__ void k_b_pairs(int32_t ne, const int2* __restrict__ e2n, int32_t* __restrict__ key,
+__global__ void k_b_pairs(int32_t ne, const int2* __restrict__ e2n, int32_t node_off, int32_t* __restrict__ key,
                           int32_t* __restrict__ val) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= ne) return;
-  key[k] = e2n[k].y;
+  key[k] = e2n[k].y - node_off;
   val[k] = (int32_t)k;
 }
 
@@ -259,7 +259,8 @@ __global__ void k_bnd_keys(int32_t nb, int32_t nn, const int32_t* __restrict__ b
 // Folded boundary rows (flux.h:14-39 is linear in the weight), entries in order.
 __global__ void k_bnd_fold(int32_t nn, const int32_t* __restrict__ off, const int32_t* __restrict__ entries,
                            const int32_t* __restrict__ grp, const double* __restrict__ bwt,
-                           const int32_t* __restrict__ row_of, mgcfd_freestream ff, int32_t* __restrict__ bidx,
+                           const int32_t* __restrict__ row_of, int32_t row_off, mgcfd_freestream ff,
+                           int32_t* __restrict__ bidx,
                            double* __restrict__ bdata) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nn) return;
@@ -271,7 +272,7 @@ __global__ void k_bnd_fold(int32_t nn, const int32_t* __restrict__ off, const in
     double* dst = grp[k] <= 2 ? wwall : wff;
     for (int c = 0; c < 3; c++) dst[c] = __dadd_rn(dst[c], __dmul_rn(bwt[3 * (int64_t)k + c], 1e-7));
   }
-  const int32_t r = row_of[i];
+  const int32_t r = row_of[i] + row_off;
   bidx[i] = r;
   double* row = bdata + 12 * (int64_t)r;
   for (int c = 0; c < 3; c++) { row[c] = wff[c]; row[3 + c] = wwall[c]; }
@@ -292,7 +293,8 @@ __global__ void k_nonempty(int32_t nn, const int32_t* __restrict__ off, int32_t*
 
 // ---- multigrid ----------------------------------------------------------------
 
-__global__ void k_mg(int32_t nf, int32_t nc, const int32_t* __restrict__ perm_f, const int32_t* __restrict__ n2mg_in,
+__global__ void k_mg(int32_t nf, int32_t nc, int32_t coarse_off, const int32_t* __restrict__ perm_f,
+                     const int32_t* __restrict__ n2mg_in,
                      const int32_t* __restrict__ inv_c, const double* __restrict__ xf, const double* __restrict__ xc,
                      int32_t* __restrict__ n2mg, double* __restrict__ dvec, int32_t* __restrict__ key,
                      int32_t* __restrict__ val, int32_t* __restrict__ cnt, unsigned* __restrict__ err) {
@@ -308,7 +310,7 @@ __global__ void k_mg(int32_t nf, int32_t nc, const int32_t* __restrict__ perm_f,
     dy = fabs(__dsub_rn(xf[3 * (int64_t)fin + 1], xc[3 * (int64_t)cin + 1]));
     dz = fabs(__dsub_rn(xf[3 * (int64_t)fin + 2], xc[3 * (int64_t)cin + 2]));
   }
-  n2mg[f] = c;
+  n2mg[f] = c + coarse_off;
   dvec[4 * f + 0] = dx;
   dvec[4 * f + 1] = dy;
   dvec[4 * f + 2] = dz;
@@ -344,16 +346,27 @@ int offsets(Temp& tmp, int32_t* cnt, int32_t* off, int64_t n, cudaStream_t s) {
   return MGCFD_OK;
 }
 
+// Per mesh and level: the arrays kept until the multigrid tables are built.
 struct LevelTmp {
-  int32_t* perm = nullptr;  // lives in DevLevel
-  int32_t* inv = nullptr;
+  int32_t* perm = nullptr;  // local new id -> local input id
+  int32_t* inv = nullptr;   // local input id -> local new id
   double* xyz = nullptr;
   int32_t* n2mg_in = nullptr;
 };
 
+__global__ void k_offset_copy(int32_t n, const int32_t* __restrict__ src, int32_t add, int32_t* __restrict__ dst) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = src[i] + add;
+}
+
+__global__ void k_fill(int32_t n, int32_t value, int32_t* __restrict__ dst) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = value;
+}
+
 }  // namespace
 
-int device_prepare(mgcfd_solver* s, int32_t nlevels, const mgcfd_level_view* lv) {
+int device_prepare(mgcfd_solver* s, const std::vector<MeshInput>& meshes) {
   cudaStream_t st = s->stream;
   Temp tmp(st);
   unsigned* err = nullptr;
@@ -361,149 +374,187 @@ int device_prepare(mgcfd_solver* s, int32_t nlevels, const mgcfd_level_view* lv)
   if (r) return r;
   CK(cudaMemsetAsync(err, 0, sizeof(unsigned), st));
   const bool mixed = s->opt.precision == MGCFD_PRECISION_MIXED;
-  std::vector<LevelTmp> lt((size_t)nlevels);
-  const double sc = s->ff.smoothing_coefficient;
+  const int nseg = (int)meshes.size();
+  const int nlevels = (int)s->L.size();
+  std::vector<std::vector<LevelTmp>> lt((size_t)nseg, std::vector<LevelTmp>((size_t)nlevels));
+  s->seg_noff.assign((size_t)nlevels, std::vector<int32_t>((size_t)nseg + 1, 0));
+  std::vector<std::vector<int32_t>> seg_eoff((size_t)nlevels, std::vector<int32_t>((size_t)nseg + 1, 0));
+  for (int l = 0; l < nlevels; l++)
+    for (int m = 0; m < nseg; m++) {
+      const mgcfd_level_view& v = meshes[(size_t)m].levels[l];
+      s->seg_noff[(size_t)l][(size_t)m + 1] = s->seg_noff[(size_t)l][(size_t)m] + v.nnodes;
+      seg_eoff[(size_t)l][(size_t)m + 1] = seg_eoff[(size_t)l][(size_t)m] + v.nedges;
+    }
 
   for (int l = 0; l < nlevels; l++) {
-    const mgcfd_level_view& v = lv[l];
     DevLevel& D = s->L[(size_t)l];
-    const int32_t n = v.nnodes, ne = v.nedges, nb = v.nbnd;
-    D.n = n; D.ne = ne;
-    // Upload the input arrays.
-    int32_t *e2n_in, *b2n_in, *grp_in;
-    double *ewt_in, *bwt_in;
-    if ((r = tmp.get(&lt[l].xyz, 3 * (size_t)n)) || (r = tmp.get(&e2n_in, 2 * (size_t)ne)) ||
-        (r = tmp.get(&ewt_in, 3 * (size_t)ne)) || (r = tmp.get(&b2n_in, (size_t)nb)) ||
-        (r = tmp.get(&grp_in, (size_t)nb)) || (r = tmp.get(&bwt_in, 3 * (size_t)nb)))
+    const int32_t N = s->seg_noff[(size_t)l][(size_t)nseg], NE = seg_eoff[(size_t)l][(size_t)nseg];
+    int64_t NB = 0;
+    for (int m = 0; m < nseg; m++) NB += meshes[(size_t)m].levels[l].nbnd;
+    D.n = N; D.ne = NE; D.nb = (int32_t)NB;
+    if ((r = s->alloc(&D.perm, (size_t)N)) || (r = s->alloc(&D.vol, (size_t)N)) ||
+        (r = s->alloc(&D.inv_vol, (size_t)N)) || (r = s->alloc(&D.cbrt_vol, (size_t)N)) ||
+        (r = s->alloc(&D.e2n, (size_t)NE)) || (r = s->alloc(&D.bidx, (size_t)N)) ||
+        (r = s->alloc(&D.bdata, 12 * (size_t)(NB > 0 ? NB : 1))))
       return r;
-    CK(cudaMemcpyAsync(lt[l].xyz, v.coords, 24 * (size_t)n, cudaMemcpyHostToDevice, st));
-    if (ne) {
-      CK(cudaMemcpyAsync(e2n_in, v.edge_to_nodes, 8 * (size_t)ne, cudaMemcpyHostToDevice, st));
-      CK(cudaMemcpyAsync(ewt_in, v.edge_weights, 24 * (size_t)ne, cudaMemcpyHostToDevice, st));
-    }
-    if (nb) {
-      CK(cudaMemcpyAsync(b2n_in, v.bnd_to_node, 4 * (size_t)nb, cudaMemcpyHostToDevice, st));
-      CK(cudaMemcpyAsync(grp_in, v.bnd_group, 4 * (size_t)nb, cudaMemcpyHostToDevice, st));
-      CK(cudaMemcpyAsync(bwt_in, v.bnd_weights, 24 * (size_t)nb, cudaMemcpyHostToDevice, st));
-    }
-    if (v.node_to_mg) {
-      if ((r = tmp.get(&lt[l].n2mg_in, (size_t)n))) return r;
-      CK(cudaMemcpyAsync(lt[l].n2mg_in, v.node_to_mg, 4 * (size_t)n, cudaMemcpyHostToDevice, st));
-    }
-
-    // Node order.
-    if ((r = s->alloc(&D.perm, (size_t)n)) || (r = tmp.get(&lt[l].inv, (size_t)n))) return r;
-    if (s->opt.renumber == MGCFD_RENUMBER_SPATIAL) {
-      unsigned long long *box, *key, *key2;
-      int32_t* val;
-      if ((r = tmp.get(&box, 6)) || (r = tmp.get(&key, (size_t)n)) || (r = tmp.get(&key2, (size_t)n)) ||
-          (r = tmp.get(&val, (size_t)n)))
-        return r;
-      CK(cudaMemsetAsync(box, 0xff, 3 * sizeof(unsigned long long), st));
-      CK(cudaMemsetAsync(box + 3, 0, 3 * sizeof(unsigned long long), st));
-      k_bbox<<<nblk(n), T, 0, st>>>(n, lt[l].xyz, box);
-      k_morton<<<nblk(n), T, 0, st>>>(n, lt[l].xyz, box, key, val);
-      if ((r = sort_pairs(tmp, key, key2, val, D.perm, n, 63, st))) return r;
-    } else {
-      k_iota<<<nblk(n), T, 0, st>>>(n, D.perm);
-    }
-    k_inverse<<<nblk(n), T, 0, st>>>(n, D.perm, lt[l].inv);
-
-    // Geometry and volumes.
-    double *tv, *wd, *vol_in;
-    if ((r = tmp.get(&tv, (size_t)ne)) || (r = tmp.get(&wd, 3 * (size_t)ne)) || (r = tmp.get(&vol_in, (size_t)n)))
+    double* w4all = nullptr;
+    if (mixed) { if ((r = tmp.get(&w4all, 4 * (size_t)NE))) return r; }
+    else { if ((r = s->alloc(&D.w4, (size_t)NE))) return r; w4all = reinterpret_cast<double*>(D.w4); }
+    if (s->gather && ((r = s->alloc(&D.a_off, (size_t)N + 1)) || (r = s->alloc(&D.b_off, (size_t)N + 1)) ||
+                      (r = s->alloc(&D.b_list, (size_t)NE))))
       return r;
-    if (ne) k_edge_geometry<<<nblk(ne), T, 0, st>>>(ne, n, e2n_in, lt[l].xyz, ewt_in, v.volumes != nullptr, tv, wd, err);
-    if (v.volumes) {
-      CK(cudaMemcpyAsync(vol_in, v.volumes, 8 * (size_t)n, cudaMemcpyHostToDevice, st));
-    } else {
-      int32_t *ikey, *ival, *ikey2, *ival2, *cnt, *off;
-      if ((r = tmp.get(&ikey, 2 * (size_t)ne)) || (r = tmp.get(&ival, 2 * (size_t)ne)) ||
-          (r = tmp.get(&ikey2, 2 * (size_t)ne)) || (r = tmp.get(&ival2, 2 * (size_t)ne)) ||
-          (r = tmp.get(&cnt, (size_t)n + 1)) || (r = tmp.get(&off, (size_t)n + 1)))
-        return r;
-      CK(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * ((size_t)n + 1), st));
-      if (ne) k_incidence<<<nblk(ne), T, 0, st>>>(ne, n, e2n_in, ikey, ival, cnt);
-      if ((r = sort_pairs(tmp, ikey, ikey2, ival, ival2, 2 * (int64_t)ne, bits_for(n), st))) return r;
-      if ((r = offsets(tmp, cnt, off, n, st))) return r;
-      k_volumes<<<nblk(n), T, 0, st>>>(n, off, ival2, tv, vol_in);
-    }
-    if ((r = s->alloc(&D.vol, (size_t)n)) || (r = s->alloc(&D.inv_vol, (size_t)n)) ||
-        (r = s->alloc(&D.cbrt_vol, (size_t)n)))
-      return r;
-    k_node_constants<<<nblk(n), T, 0, st>>>(n, D.perm, vol_in, D.vol, D.inv_vol, D.cbrt_vol);
+    if (nseg > 1 && (r = s->alloc(&D.mesh_id, (size_t)N))) return r;
+    int32_t row_off = 0;
 
-    // Edges: orientation, order, weights, CSR.
-    {
-      unsigned long long *key, *key2;
-      int32_t *val, *order, *acnt, *bcnt;
-      unsigned char* flip;
-      double* w4;
-      if ((r = tmp.get(&key, (size_t)ne)) || (r = tmp.get(&key2, (size_t)ne)) || (r = tmp.get(&val, (size_t)ne)) ||
-          (r = tmp.get(&order, (size_t)ne)) || (r = tmp.get(&flip, (size_t)ne)) ||
-          (r = tmp.get(&acnt, (size_t)n + 1)) || (r = tmp.get(&bcnt, (size_t)n + 1)) ||
-          (r = s->alloc(&D.e2n, (size_t)ne)))
+    for (int m = 0; m < nseg; m++) {
+      const mgcfd_level_view& v = meshes[(size_t)m].levels[l];
+      const mgcfd_freestream& ff = meshes[(size_t)m].ff;
+      const double sc = ff.smoothing_coefficient;
+      LevelTmp& T_ = lt[(size_t)m][(size_t)l];
+      const int32_t n = v.nnodes, ne = v.nedges, nb = v.nbnd;
+      const int32_t noff = s->seg_noff[(size_t)l][(size_t)m], eoff = seg_eoff[(size_t)l][(size_t)m];
+      // Upload the input arrays.
+      int32_t *e2n_in, *b2n_in, *grp_in;
+      double *ewt_in, *bwt_in;
+      if ((r = tmp.get(&T_.xyz, 3 * (size_t)n)) || (r = tmp.get(&e2n_in, 2 * (size_t)ne)) ||
+          (r = tmp.get(&ewt_in, 3 * (size_t)ne)) || (r = tmp.get(&b2n_in, (size_t)nb)) ||
+          (r = tmp.get(&grp_in, (size_t)nb)) || (r = tmp.get(&bwt_in, 3 * (size_t)nb)))
         return r;
-      if (mixed) { if ((r = tmp.get(&w4, 4 * (size_t)ne))) return r; }
-      else { if ((r = s->alloc(&D.w4, (size_t)ne))) return r; w4 = reinterpret_cast<double*>(D.w4); }
-      CK(cudaMemsetAsync(acnt, 0, sizeof(int32_t) * ((size_t)n + 1), st));
-      CK(cudaMemsetAsync(bcnt, 0, sizeof(int32_t) * ((size_t)n + 1), st));
+      CK(cudaMemcpyAsync(T_.xyz, v.coords, 24 * (size_t)n, cudaMemcpyHostToDevice, st));
       if (ne) {
-        k_edge_keys<<<nblk(ne), T, 0, st>>>(ne, n, e2n_in, lt[l].inv, key, val, flip);
-        if ((r = sort_pairs(tmp, key, key2, val, order, ne, 32 + bits_for(n), st))) return r;
-        k_edge_finalize<<<nblk(ne), T, 0, st>>>(ne, key2, order, wd, flip, sc, D.e2n, w4, acnt, bcnt);
+        CK(cudaMemcpyAsync(e2n_in, v.edge_to_nodes, 8 * (size_t)ne, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(ewt_in, v.edge_weights, 24 * (size_t)ne, cudaMemcpyHostToDevice, st));
       }
-      if (mixed) {
-        if ((r = s->alloc(&D.w4f, (size_t)ne))) return r;
-        if (ne) k_to_float<<<nblk(4 * (int64_t)ne), T, 0, st>>>(4 * (int64_t)ne, w4, reinterpret_cast<float*>(D.w4f));
-        if (s->opt.measure_mem_bound) {
-          if ((r = s->alloc(&D.w4, (size_t)ne))) return r;
-          if (ne) CK(cudaMemcpyAsync(D.w4, w4, 32 * (size_t)ne, cudaMemcpyDeviceToDevice, st));
-        }
+      if (nb) {
+        CK(cudaMemcpyAsync(b2n_in, v.bnd_to_node, 4 * (size_t)nb, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(grp_in, v.bnd_group, 4 * (size_t)nb, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(bwt_in, v.bnd_weights, 24 * (size_t)nb, cudaMemcpyHostToDevice, st));
       }
-      if (s->gather) {
-        int32_t *bkey, *bval, *bkey2;
-        if ((r = s->alloc(&D.a_off, (size_t)n + 1)) || (r = s->alloc(&D.b_off, (size_t)n + 1)) ||
-            (r = s->alloc(&D.b_list, (size_t)ne)) || (r = tmp.get(&bkey, (size_t)ne)) ||
-            (r = tmp.get(&bval, (size_t)ne)) || (r = tmp.get(&bkey2, (size_t)ne)))
+      if (v.node_to_mg) {
+        if ((r = tmp.get(&T_.n2mg_in, (size_t)n))) return r;
+        CK(cudaMemcpyAsync(T_.n2mg_in, v.node_to_mg, 4 * (size_t)n, cudaMemcpyHostToDevice, st));
+      }
+      if (nseg > 1) k_fill<<<nblk(n), T, 0, st>>>(n, m, D.mesh_id + noff);
+
+      // Node order (local to the mesh).
+      if ((r = tmp.get(&T_.perm, (size_t)n)) || (r = tmp.get(&T_.inv, (size_t)n))) return r;
+      if (s->opt.renumber == MGCFD_RENUMBER_SPATIAL) {
+        unsigned long long *box, *key, *key2;
+        int32_t* val;
+        if ((r = tmp.get(&box, 6)) || (r = tmp.get(&key, (size_t)n)) || (r = tmp.get(&key2, (size_t)n)) ||
+            (r = tmp.get(&val, (size_t)n)))
           return r;
-        if ((r = offsets(tmp, acnt, D.a_off, n, st)) || (r = offsets(tmp, bcnt, D.b_off, n, st))) return r;
+        CK(cudaMemsetAsync(box, 0xff, 3 * sizeof(unsigned long long), st));
+        CK(cudaMemsetAsync(box + 3, 0, 3 * sizeof(unsigned long long), st));
+        k_bbox<<<nblk(n), T, 0, st>>>(n, T_.xyz, box);
+        k_morton<<<nblk(n), T, 0, st>>>(n, T_.xyz, box, key, val);
+        if ((r = sort_pairs(tmp, key, key2, val, T_.perm, n, 63, st))) return r;
+      } else {
+        k_iota<<<nblk(n), T, 0, st>>>(n, T_.perm);
+      }
+      k_inverse<<<nblk(n), T, 0, st>>>(n, T_.perm, T_.inv);
+      k_offset_copy<<<nblk(n), T, 0, st>>>(n, T_.perm, noff, D.perm + noff);
+
+      // Geometry and volumes.
+      double *tv, *wd, *vol_in;
+      if ((r = tmp.get(&tv, (size_t)ne)) || (r = tmp.get(&wd, 3 * (size_t)ne)) || (r = tmp.get(&vol_in, (size_t)n)))
+        return r;
+      if (ne) k_edge_geometry<<<nblk(ne), T, 0, st>>>(ne, n, e2n_in, T_.xyz, ewt_in, v.volumes != nullptr, tv, wd, err);
+      if (v.volumes) {
+        CK(cudaMemcpyAsync(vol_in, v.volumes, 8 * (size_t)n, cudaMemcpyHostToDevice, st));
+      } else {
+        int32_t *ikey, *ival, *ikey2, *ival2, *cnt, *off;
+        if ((r = tmp.get(&ikey, 2 * (size_t)ne)) || (r = tmp.get(&ival, 2 * (size_t)ne)) ||
+            (r = tmp.get(&ikey2, 2 * (size_t)ne)) || (r = tmp.get(&ival2, 2 * (size_t)ne)) ||
+            (r = tmp.get(&cnt, (size_t)n + 1)) || (r = tmp.get(&off, (size_t)n + 1)))
+          return r;
+        CK(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * ((size_t)n + 1), st));
+        if (ne) k_incidence<<<nblk(ne), T, 0, st>>>(ne, n, e2n_in, ikey, ival, cnt);
+        if ((r = sort_pairs(tmp, ikey, ikey2, ival, ival2, 2 * (int64_t)ne, bits_for(n), st))) return r;
+        if ((r = offsets(tmp, cnt, off, n, st))) return r;
+        k_volumes<<<nblk(n), T, 0, st>>>(n, off, ival2, tv, vol_in);
+      }
+      k_node_constants<<<nblk(n), T, 0, st>>>(n, T_.perm, vol_in, D.vol + noff, D.inv_vol + noff, D.cbrt_vol + noff);
+
+      // Edges: orientation, order, weights, CSR.
+      {
+        unsigned long long *key, *key2;
+        int32_t *val, *order, *acnt, *bcnt;
+        unsigned char* flip;
+        if ((r = tmp.get(&key, (size_t)ne)) || (r = tmp.get(&key2, (size_t)ne)) || (r = tmp.get(&val, (size_t)ne)) ||
+            (r = tmp.get(&order, (size_t)ne)) || (r = tmp.get(&flip, (size_t)ne)) ||
+            (r = tmp.get(&acnt, (size_t)n + 1)) || (r = tmp.get(&bcnt, (size_t)n + 1)))
+          return r;
+        CK(cudaMemsetAsync(acnt, 0, sizeof(int32_t) * ((size_t)n + 1), st));
+        CK(cudaMemsetAsync(bcnt, 0, sizeof(int32_t) * ((size_t)n + 1), st));
         if (ne) {
-          k_b_pairs<<<nblk(ne), T, 0, st>>>(ne, D.e2n, bkey, bval);
-          if ((r = sort_pairs(tmp, bkey, bkey2, bval, D.b_list, ne, bits_for(n), st))) return r;
+          k_edge_keys<<<nblk(ne), T, 0, st>>>(ne, n, e2n_in, T_.inv, key, val, flip);
+          if ((r = sort_pairs(tmp, key, key2, val, order, ne, 32 + bits_for(n), st))) return r;
+          k_edge_finalize<<<nblk(ne), T, 0, st>>>(ne, noff, key2, order, wd, flip, sc, D.e2n + eoff,
+                                                  w4all + 4 * (size_t)eoff, acnt, bcnt);
         }
+        if (s->gather) {
+          int32_t *aoff, *boff, *bkey, *bval, *bkey2, *blist;
+          if ((r = tmp.get(&aoff, (size_t)n + 1)) || (r = tmp.get(&boff, (size_t)n + 1)) ||
+              (r = tmp.get(&bkey, (size_t)ne)) || (r = tmp.get(&bval, (size_t)ne)) ||
+              (r = tmp.get(&bkey2, (size_t)ne)) || (r = tmp.get(&blist, (size_t)ne)))
+            return r;
+          if ((r = offsets(tmp, acnt, aoff, n, st)) || (r = offsets(tmp, bcnt, boff, n, st))) return r;
+          k_offset_copy<<<nblk(n), T, 0, st>>>(n, aoff, eoff, D.a_off + noff);
+          k_offset_copy<<<nblk(n), T, 0, st>>>(n, boff, eoff, D.b_off + noff);
+          if (ne) {
+            k_b_pairs<<<nblk(ne), T, 0, st>>>(ne, D.e2n + eoff, noff, bkey, bval);
+            if ((r = sort_pairs(tmp, bkey, bkey2, bval, blist, ne, bits_for(n), st))) return r;
+            k_offset_copy<<<nblk(ne), T, 0, st>>>(ne, blist, eoff, D.b_list + eoff);
+          }
+        }
+      }
+
+      // Boundary entries folded per node.
+      {
+        int32_t *key, *val, *key2, *val2, *cnt, *off, *flag, *row;
+        if ((r = tmp.get(&key, (size_t)nb)) || (r = tmp.get(&val, (size_t)nb)) || (r = tmp.get(&key2, (size_t)nb)) ||
+            (r = tmp.get(&val2, (size_t)nb)) || (r = tmp.get(&cnt, (size_t)n + 1)) ||
+            (r = tmp.get(&off, (size_t)n + 1)) || (r = tmp.get(&flag, (size_t)n + 1)) ||
+            (r = tmp.get(&row, (size_t)n + 1)))
+          return r;
+        CK(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * ((size_t)n + 1), st));
+        if (nb) {
+          k_bnd_keys<<<nblk(nb), T, 0, st>>>(nb, n, b2n_in, grp_in, T_.inv, key, val, cnt, err);
+          if ((r = sort_pairs(tmp, key, key2, val, val2, nb, bits_for(n), st))) return r;
+        }
+        if ((r = offsets(tmp, cnt, off, n, st))) return r;
+        CK(cudaMemsetAsync(flag, 0, sizeof(int32_t) * ((size_t)n + 1), st));
+        k_nonempty<<<nblk(n), T, 0, st>>>(n, off, flag);
+        if ((r = offsets(tmp, flag, row, n, st))) return r;
+        k_bnd_fold<<<nblk(n), T, 0, st>>>(n, off, val2, grp_in, bwt_in, row, row_off, ff, D.bidx + noff, D.bdata);
+        int32_t rows = 0;
+        CK(cudaMemcpyAsync(&rows, row + n, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        row_off += rows;
       }
     }
-
-    // Boundary entries folded per node.
-    {
-      int32_t *key, *val, *key2, *val2, *cnt, *off, *flag, *row;
-      if ((r = tmp.get(&key, (size_t)nb)) || (r = tmp.get(&val, (size_t)nb)) || (r = tmp.get(&key2, (size_t)nb)) ||
-          (r = tmp.get(&val2, (size_t)nb)) || (r = tmp.get(&cnt, (size_t)n + 1)) ||
-          (r = tmp.get(&off, (size_t)n + 1)) || (r = tmp.get(&flag, (size_t)n + 1)) ||
-          (r = tmp.get(&row, (size_t)n + 1)) || (r = s->alloc(&D.bidx, (size_t)n)) ||
-          (r = s->alloc(&D.bdata, 12 * (size_t)(nb > 0 ? nb : 1))))
-        return r;
-      CK(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * ((size_t)n + 1), st));
-      if (nb) {
-        k_bnd_keys<<<nblk(nb), T, 0, st>>>(nb, n, b2n_in, grp_in, lt[l].inv, key, val, cnt, err);
-        if ((r = sort_pairs(tmp, key, key2, val, val2, nb, bits_for(n), st))) return r;
+    D.nbrows = row_off;
+    if (s->gather) {
+      k_fill<<<1, 1, 0, st>>>(1, NE, D.a_off + N);
+      k_fill<<<1, 1, 0, st>>>(1, NE, D.b_off + N);
+    }
+    if (mixed) {
+      if ((r = s->alloc(&D.w4f, (size_t)NE))) return r;
+      if (NE) k_to_float<<<nblk(4 * (int64_t)NE), T, 0, st>>>(4 * (int64_t)NE, w4all, reinterpret_cast<float*>(D.w4f));
+      if (s->opt.measure_mem_bound) {
+        if ((r = s->alloc(&D.w4, (size_t)NE))) return r;
+        if (NE) CK(cudaMemcpyAsync(D.w4, w4all, 32 * (size_t)NE, cudaMemcpyDeviceToDevice, st));
       }
-      if ((r = offsets(tmp, cnt, off, n, st))) return r;
-      CK(cudaMemsetAsync(flag, 0, sizeof(int32_t) * ((size_t)n + 1), st));
-      k_nonempty<<<nblk(n), T, 0, st>>>(n, off, flag);
-      if ((r = offsets(tmp, flag, row, n, st))) return r;
-      k_bnd_fold<<<nblk(n), T, 0, st>>>(n, off, val2, grp_in, bwt_in, row, s->ff, D.bidx, D.bdata);
-      CK(cudaMemcpyAsync(&D.nbrows, row + n, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
     }
     // Per-level state.
-    if ((r = s->alloc(&D.rec, 8 * (size_t)n)) || (r = s->alloc(&D.old, 5 * (size_t)n)) ||
-        (r = s->alloc(&D.res, 5 * (size_t)n)))
+    if ((r = s->alloc(&D.rec, 8 * (size_t)N)) || (r = s->alloc(&D.old, 5 * (size_t)N)) ||
+        (r = s->alloc(&D.res, 5 * (size_t)N)))
       return r;
-    if (mixed && (r = s->alloc(&D.rec32, 8 * (size_t)n))) return r;
-    if (s->gather) { if ((r = s->alloc(&D.fe, 5 * (size_t)ne))) return r; }
-    else if ((r = s->alloc(&D.flux, 5 * (size_t)n))) return r;
-    if (s->opt.measure_mem_bound && (r = s->alloc(&D.dummy, 5 * (size_t)n))) return r;
+    if (mixed && (r = s->alloc(&D.rec32, 8 * (size_t)N))) return r;
+    if (s->gather) { if ((r = s->alloc(&D.fe, 5 * (size_t)NE))) return r; }
+    else if ((r = s->alloc(&D.flux, 5 * (size_t)N))) return r;
+    if (s->opt.measure_mem_bound && (r = s->alloc(&D.dummy, 5 * (size_t)N))) return r;
     CK(cudaGetLastError());
   }
 
@@ -511,26 +562,34 @@ int device_prepare(mgcfd_solver* s, int32_t nlevels, const mgcfd_level_view* lv)
   for (int l = 0; l + 1 < nlevels; l++) {
     DevLevel& F = s->L[(size_t)l];
     DevLevel& Cl = s->L[(size_t)l + 1];
-    const int32_t nf = F.n, nc = Cl.n;
-    int32_t *key, *val, *key2, *cnt;
-    Cl.nfine = nf;
-    if ((r = s->alloc(&F.n2mg, (size_t)nf)) || (r = s->alloc(&F.dvec, (size_t)nf)) ||
-        (r = s->alloc(&Cl.ch_off, (size_t)nc + 1)) || (r = s->alloc(&Cl.ch_list, (size_t)nf)) ||
-        (r = tmp.get(&key, (size_t)nf)) || (r = tmp.get(&val, (size_t)nf)) || (r = tmp.get(&key2, (size_t)nf)) ||
-        (r = tmp.get(&cnt, (size_t)nc + 1)))
+    if ((r = s->alloc(&F.n2mg, (size_t)F.n)) || (r = s->alloc(&F.dvec, (size_t)F.n)) ||
+        (r = s->alloc(&Cl.ch_off, (size_t)Cl.n + 1)) || (r = s->alloc(&Cl.ch_list, (size_t)F.n)))
       return r;
-    CK(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * ((size_t)nc + 1), st));
-    k_mg<<<nblk(nf), T, 0, st>>>(nf, nc, F.perm, lt[l].n2mg_in, lt[l + 1].inv, lt[l].xyz, lt[l + 1].xyz, F.n2mg,
-                                 reinterpret_cast<double*>(F.dvec), key, val, cnt, err);
-    if ((r = sort_pairs(tmp, key, key2, val, Cl.ch_list, nf, bits_for(nc), st))) return r;
-    if ((r = offsets(tmp, cnt, Cl.ch_off, nc, st))) return r;
+    Cl.nfine = F.n;
+    for (int m = 0; m < nseg; m++) {
+      const int32_t nf = meshes[(size_t)m].levels[l].nnodes, nc = meshes[(size_t)m].levels[l + 1].nnodes;
+      const int32_t noff_f = s->seg_noff[(size_t)l][(size_t)m], noff_c = s->seg_noff[(size_t)l + 1][(size_t)m];
+      int32_t *key, *val, *key2, *cnt, *off, *list;
+      if ((r = tmp.get(&key, (size_t)nf)) || (r = tmp.get(&val, (size_t)nf)) || (r = tmp.get(&key2, (size_t)nf)) ||
+          (r = tmp.get(&cnt, (size_t)nc + 1)) || (r = tmp.get(&off, (size_t)nc + 1)) || (r = tmp.get(&list, (size_t)nf)))
+        return r;
+      CK(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * ((size_t)nc + 1), st));
+      const LevelTmp& TF = lt[(size_t)m][(size_t)l];
+      const LevelTmp& TC = lt[(size_t)m][(size_t)l + 1];
+      k_mg<<<nblk(nf), T, 0, st>>>(nf, nc, noff_c, TF.perm, TF.n2mg_in, TC.inv, TF.xyz, TC.xyz, F.n2mg + noff_f,
+                                   reinterpret_cast<double*>(F.dvec) + 4 * (size_t)noff_f, key, val, cnt, err);
+      if ((r = sort_pairs(tmp, key, key2, val, list, nf, bits_for(nc), st))) return r;
+      if ((r = offsets(tmp, cnt, off, nc, st))) return r;
+      k_offset_copy<<<nblk(nf), T, 0, st>>>(nf, list, noff_f, Cl.ch_list + noff_f);
+      k_offset_copy<<<nblk(nc), T, 0, st>>>(nc, off, noff_f, Cl.ch_off + noff_c);
+    }
+    k_fill<<<1, 1, 0, st>>>(1, F.n, Cl.ch_off + Cl.n);
   }
   CK(cudaGetLastError());
   unsigned h_err = 0;
   CK(cudaMemcpyAsync(&h_err, err, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   if (h_err) return set_error(MGCFD_ERR_INVALID, "mesh has " + std::to_string(h_err) + " map entries out of range");
-  for (int l = 0; l < nlevels; l++) s->L[(size_t)l].nb = lv[l].nbnd;
   return MGCFD_OK;
 }
 

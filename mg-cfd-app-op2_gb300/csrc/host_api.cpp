@@ -26,9 +26,6 @@ void clear_error() { g_last_error.clear(); }
 
 }  // namespace mgcfd
 
-struct mgcfd_host_mesh {
-  mgcfd::HostMesh mesh;
-};
 
 using mgcfd::set_error;
 

@@ -61,3 +61,8 @@ bool write_mesh_files(const HostMesh& mesh, const std::string& dir, const std::s
                       bool legacy_datasets, std::string* err);
 
 }  // namespace mgcfd
+
+// The opaque mgcfd_host_mesh handle of the C ABI.
+struct mgcfd_host_mesh {
+  mgcfd::HostMesh mesh;
+};

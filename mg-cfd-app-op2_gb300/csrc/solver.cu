@@ -45,7 +45,7 @@ using namespace mgcfd;
 
 namespace {
 
-constexpr int kNodeThreads = 256;
+constexpr int kNodeThreads = 128;
 
 
 
@@ -123,6 +123,15 @@ __global__ void k_vol_constants(int32_t n, const double* __restrict__ vol, doubl
   cbrt_vol[i] = cbrt(vol[i]);
 }
 
+// Freestream state of each node's own mesh (batched solvers).
+__global__ void k_init_state_seg(int32_t n, double* __restrict__ rec, const int32_t* __restrict__ mesh_id,
+                                 const double* __restrict__ ffvar) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double* v = ffvar + 5 * (int64_t)mesh_id[i];
+  store_rec(rec, i, node_prim(v[0], v[1], v[2], v[3], v[4]));
+}
+
 // Freestream state into rec (initialize_variables_kernel, misc.h:10-16).
 __global__ void k_init_state(int32_t n, double* __restrict__ rec, double v0, double v1, double v2, double v3,
                              double v4) {
@@ -131,16 +140,24 @@ __global__ void k_init_state(int32_t n, double* __restrict__ rec, double v0, dou
   store_rec(rec, i, node_prim(v0, v1, v2, v3, v4));
 }
 
+// Per-mesh block reductions for batched solvers (SEG): the nodes of a block
+// are contiguous, so their mesh ids are nondecreasing and differ from the
+// first node's id by less than the block size; each mesh of the block gets
+// one shared slot and one global atomic.
+
 // copy_double_kernel + calculate_dt_kernel + get_min_dt_kernel (block part).
-template <bool MIXED>
+template <bool MIXED, bool SEG>
 __global__ void __launch_bounds__(kNodeThreads) k_step_begin(int32_t n, double* __restrict__ rec,
                                                              float* __restrict__ rec32, double* __restrict__ old,
                                                              const double* __restrict__ cbrt_vol,
                                                              unsigned long long* __restrict__ dt_key,
-                                                             const DevStatus* __restrict__ st) {
+                                                             const DevStatus* __restrict__ st,
+                                                             const int32_t* __restrict__ mesh_id) {
   __shared__ double smin[kNodeThreads / 32];
   __shared__ int s_halt;
+  __shared__ unsigned long long s_key[SEG ? kNodeThreads : 1];
   if (threadIdx.x == 0) s_halt = st->halt;
+  if (SEG) s_key[threadIdx.x] = ~0ull;
   __syncthreads();
   if (s_halt) return;  // block-uniform: the reduction below synchronises
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -156,6 +173,13 @@ __global__ void __launch_bounds__(kNodeThreads) k_step_begin(int32_t n, double* 
     o[0] = x.x; o[1] = x.y; o[2] = x.z; o[3] = x.w; o[4] = e;
     const double dt = 0.5 * (cbrt_vol[i] / p.s);  // time_stepping_kernels.h:31
     if (dt < m) m = dt;                            // NaN never wins, as in get_min_dt_kernel
+  }
+  if (SEG) {
+    const int32_t m0 = mesh_id[(int64_t)blockIdx.x * blockDim.x];
+    if (i < n && m < DBL_MAX) atomicMin(&s_key[mesh_id[i] - m0], dkey(m));
+    __syncthreads();
+    if (s_key[threadIdx.x] != ~0ull) atomicMin(dt_key + m0 + threadIdx.x, s_key[threadIdx.x]);
+    return;
   }
   m = warp_min(m);
   if ((threadIdx.x & 31) == 0) smin[threadIdx.x >> 5] = m;
@@ -269,8 +293,13 @@ struct UpdateArgs {
   const int32_t* bidx;
   const double* bdata;
   double* res;
-  const unsigned long long* dt_key;
+  const unsigned long long* dt_key;  // plain: the level's key; batched: the level's per-mesh keys
   DevStatus* st;
+  const int32_t* mesh_id;            // batched only
+  int* seg_neg;
+  int* seg_bad;
+  double* seg_rms;
+  double* seg_rho;
 };
 
 // Boundary flux of one node (flux.h:14-39 summed over the node's entries).
@@ -286,24 +315,43 @@ __device__ __forceinline__ void add_boundary(const NodePrim& p, const double* __
 }
 
 // compute_bnd_node_flux_kernel + time_step_kernel (+ residual_kernel,
-// calc_rms_kernel and count_bad_vals in the last stage).
-template <bool GATHER, bool LAST, bool MIXED>
+// calc_rms_kernel and count_bad_vals in the last stage).  Plain solvers stop
+// everything on min_dt < 0 or NaN/Inf (the reference aborts); batched
+// solvers mark the failing mesh and leave the others running.
+template <bool GATHER, bool LAST, bool MIXED, bool SEG>
 __global__ void __launch_bounds__(kNodeThreads) k_update(UpdateArgs A) {
   __shared__ double srms[kNodeThreads / 32];
+  __shared__ double srho[kNodeThreads / 32];
   __shared__ int sbad[kNodeThreads / 32];
   __shared__ int s_halt;
+  __shared__ double s_sum[SEG && LAST ? kNodeThreads : 1];
+  __shared__ double s_rho[SEG && LAST ? kNodeThreads : 1];
+  __shared__ int s_bad[SEG && LAST ? kNodeThreads : 1];
   if (threadIdx.x == 0) s_halt = A.st->halt;
+  if (SEG && LAST) { s_sum[threadIdx.x] = 0.0; s_rho[threadIdx.x] = 0.0; s_bad[threadIdx.x] = 0; }
   __syncthreads();
   if (s_halt) return;  // block-uniform: the reduction below synchronises
-  const double min_dt = dkey_inv(*A.dt_key);
-  if (min_dt < 0.0) {  // euler3d.cpp:480: abort before the step factor is used
-    if (threadIdx.x == 0) { A.st->neg_dt = 1; atomicOr(&A.st->halt, 1); }
-    return;
-  }
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  double r2 = 0.0;
+  int32_t mid = 0;
+  double min_dt;
+  if (SEG) {
+    mid = i < A.n ? A.mesh_id[i] : 0;
+    min_dt = dkey_inv(A.dt_key[mid]);
+  } else {
+    min_dt = dkey_inv(*A.dt_key);
+    if (min_dt < 0.0) {  // euler3d.cpp:480: abort before the step factor is used
+      if (threadIdx.x == 0) { A.st->neg_dt = 1; atomicOr(&A.st->halt, 1); }
+      return;
+    }
+  }
+  double r2 = 0.0, rr = 0.0;
   int bad = 0;
-  if (i < A.n) {
+  bool active = i < A.n;
+  if (SEG && active && min_dt < 0.0) {
+    atomicOr(A.seg_neg + mid, 1);
+    active = false;
+  }
+  if (active) {
     double F[5];
     if (GATHER) {
 #pragma unroll
@@ -348,6 +396,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_update(UpdateArgs A) {
         const double d = v[k] - o[k];
         rs[k] = d;
         r2 += d * d;
+        if (k == 0) rr = d * d;
         if (isnan(v[k]) || isinf(v[k])) bad++;
       }
     } else if (MIXED) {
@@ -358,22 +407,40 @@ __global__ void __launch_bounds__(kNodeThreads) k_update(UpdateArgs A) {
     } else {
       store_rec(A.rec, i, node_prim(v[0], v[1], v[2], v[3], v[4]));
     }
+  } else if (SEG && LAST && i < A.n) {
+    bad = 0;  // a mesh stopped by min_dt < 0 keeps its state
   }
-  if (LAST) {
-    if (!A.level0) return;
-    r2 = warp_sum(r2);
-    bad = warp_sum_int(bad);
-    if ((threadIdx.x & 31) == 0) { srms[threadIdx.x >> 5] = r2; sbad[threadIdx.x >> 5] = bad; }
+  if (!LAST || !A.level0) return;
+  if (SEG) {
+    const int32_t m0 = A.mesh_id[(int64_t)blockIdx.x * blockDim.x];
+    if (i < A.n) {
+      if (r2 != 0.0) atomicAdd(&s_sum[mid - m0], r2);
+      if (rr != 0.0) atomicAdd(&s_rho[mid - m0], rr);
+      if (bad) atomicAdd(&s_bad[mid - m0], bad);
+    }
     __syncthreads();
-    if (threadIdx.x < 32) {
-      r2 = threadIdx.x < kNodeThreads / 32 ? srms[threadIdx.x] : 0.0;
-      bad = threadIdx.x < kNodeThreads / 32 ? sbad[threadIdx.x] : 0;
-      r2 = warp_sum(r2);
-      bad = warp_sum_int(bad);
-      if (threadIdx.x == 0) {
-        atomicAdd(&A.st->rms_acc, r2);
-        if (bad) { atomicAdd(&A.st->bad_count, bad); atomicOr(&A.st->halt, 1); }
-      }
+    const int t = threadIdx.x;
+    if (s_sum[t] != 0.0) atomicAdd(A.seg_rms + m0 + t, s_sum[t]);
+    if (s_rho[t] != 0.0) atomicAdd(A.seg_rho + m0 + t, s_rho[t]);
+    if (s_bad[t]) atomicAdd(A.seg_bad + m0 + t, s_bad[t]);
+    return;
+  }
+  r2 = warp_sum(r2);
+  rr = warp_sum(rr);
+  bad = warp_sum_int(bad);
+  if ((threadIdx.x & 31) == 0) { srms[threadIdx.x >> 5] = r2; srho[threadIdx.x >> 5] = rr; sbad[threadIdx.x >> 5] = bad; }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    r2 = threadIdx.x < kNodeThreads / 32 ? srms[threadIdx.x] : 0.0;
+    rr = threadIdx.x < kNodeThreads / 32 ? srho[threadIdx.x] : 0.0;
+    bad = threadIdx.x < kNodeThreads / 32 ? sbad[threadIdx.x] : 0;
+    r2 = warp_sum(r2);
+    rr = warp_sum(rr);
+    bad = warp_sum_int(bad);
+    if (threadIdx.x == 0) {
+      atomicAdd(&A.st->rms_acc, r2);
+      atomicAdd(&A.st->rho_acc, rr);
+      if (bad) { atomicAdd(&A.st->bad_count, bad); atomicOr(&A.st->halt, 1); }
     }
   }
 }
@@ -414,20 +481,25 @@ __global__ void k_prolong(int32_t nf, const int32_t* __restrict__ n2mg, const do
   for (int k = 0; k < 5; k++) r[k] -= dd[k] * (cres[5 * c + k] - fres[5 * i + k]);
 }
 
-// Fetch helpers: scatter renumbered rows back to input order.
-__global__ void k_unpermute(int32_t n, int32_t width, int32_t stride, const double* __restrict__ src,
+// Fetch helpers: scatter the renumbered rows [off, off + n) back to input
+// order (rows of one mesh, or of the whole level when off = 0).
+__global__ void k_unpermute(int32_t n, int32_t off, int32_t width, int32_t stride, const double* __restrict__ src,
                             const int32_t* __restrict__ perm, double* __restrict__ dst) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (int64_t)n * width) return;
-  const int64_t i = t / width, k = t % width;
-  dst[(int64_t)perm[i] * width + k] = src[i * stride + k];
+  const int64_t i = off + t / width, k = t % width;
+  dst[(int64_t)(perm[i] - off) * width + k] = src[i * stride + k];
 }
 
-__global__ void k_step_factors(int32_t n, const double* __restrict__ vol, const unsigned long long* dt_key,
+// time_stepping_kernels.h:63 with each node's own mesh's last min_dt.
+__global__ void k_step_factors(int32_t n, int32_t off, const double* __restrict__ vol,
+                               const unsigned long long* __restrict__ keys, const int32_t* __restrict__ mesh_id,
                                const int32_t* __restrict__ perm, double* __restrict__ dst) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  dst[perm[i]] = dkey_inv(*dt_key) / vol[i];  // time_stepping_kernels.h:63
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int64_t i = off + t;
+  const unsigned long long k = keys[mesh_id ? mesh_id[i] : 0];
+  dst[perm[i] - off] = dkey_inv(k) / vol[i];
 }
 
 }  // namespace
@@ -442,19 +514,43 @@ int grid(int64_t n, int threads) { return (int)((n + threads - 1) / threads); }
 
 int edge_threads(const mgcfd_solver* s) { return s->opt.block_size > 0 ? s->opt.block_size : 128; }
 
+// Launchers indexed by the kernels' compile-time variants.
+template <bool G, bool L, bool M, bool S>
+void launch_update(int grid_n, cudaStream_t st, const UpdateArgs& A) {
+  k_update<G, L, M, S><<<grid_n, kNodeThreads, 0, st>>>(A);
+}
+using UpdateFn = void (*)(int, cudaStream_t, const UpdateArgs&);
+const UpdateFn kUpdate[16] = {
+    launch_update<0, 0, 0, 0>, launch_update<0, 0, 0, 1>, launch_update<0, 0, 1, 0>, launch_update<0, 0, 1, 1>,
+    launch_update<0, 1, 0, 0>, launch_update<0, 1, 0, 1>, launch_update<0, 1, 1, 0>, launch_update<0, 1, 1, 1>,
+    launch_update<1, 0, 0, 0>, launch_update<1, 0, 0, 1>, launch_update<1, 0, 1, 0>, launch_update<1, 0, 1, 1>,
+    launch_update<1, 1, 0, 0>, launch_update<1, 1, 0, 1>, launch_update<1, 1, 1, 0>, launch_update<1, 1, 1, 1>};
+
+template <bool M, bool S>
+void launch_step_begin(const DevLevel& D, unsigned long long* key, const DevStatus* st, cudaStream_t stream) {
+  k_step_begin<M, S><<<grid(D.n, kNodeThreads), kNodeThreads, 0, stream>>>(D.n, D.rec, D.rec32, D.old, D.cbrt_vol,
+                                                                            key, st, D.mesh_id);
+}
+using StepFn = void (*)(const DevLevel&, unsigned long long*, const DevStatus*, cudaStream_t);
+const StepFn kStepBegin[4] = {launch_step_begin<0, 0>, launch_step_begin<0, 1>, launch_step_begin<1, 0>,
+                              launch_step_begin<1, 1>};
+
 // One smoothing step at `level` (euler3d.cpp:467-550).
 int enqueue_smooth(mgcfd_solver* s, int level) {
   DevLevel& D = s->L[(size_t)level];
   const bool mixed = s->opt.precision == MGCFD_PRECISION_MIXED;
   const bool timing = s->opt.time_kernels && level == 0;
-  CK(cudaMemsetAsync(&s->st->dt_key[level], 0xff, sizeof(unsigned long long), s->stream));
-  if (level == 0) CK(cudaMemsetAsync(&s->st->rms_acc, 0, sizeof(double), s->stream));
-  if (mixed)
-    k_step_begin<true><<<grid(D.n, kNodeThreads), kNodeThreads, 0, s->stream>>>(D.n, D.rec, D.rec32, D.old, D.cbrt_vol,
-                                                                                 &s->st->dt_key[level], s->st);
-  else
-    k_step_begin<false><<<grid(D.n, kNodeThreads), kNodeThreads, 0, s->stream>>>(D.n, D.rec, D.rec32, D.old, D.cbrt_vol,
-                                                                                  &s->st->dt_key[level], s->st);
+  const bool seg = s->nseg > 1;
+  unsigned long long* key = seg ? s->seg_keys + (size_t)level * s->nseg : &s->st->dt_key[level];
+  CK(cudaMemsetAsync(key, 0xff, sizeof(unsigned long long) * (size_t)s->nseg, s->stream));
+  if (level == 0) {
+    CK(cudaMemsetAsync(&s->st->rms_acc, 0, 2 * sizeof(double), s->stream));  // rms_acc, rho_acc
+    if (seg) {
+      CK(cudaMemsetAsync(s->seg_rms, 0, sizeof(double) * (size_t)s->nseg, s->stream));
+      CK(cudaMemsetAsync(s->seg_rho, 0, sizeof(double) * (size_t)s->nseg, s->stream));
+    }
+  }
+  kStepBegin[(mixed ? 2 : 0) | (seg ? 1 : 0)](D, key, s->st, s->stream);
   s->launches++;
   const int et = edge_threads(s);
   for (int rk = 0; rk < kRK; rk++) {
@@ -486,20 +582,11 @@ int enqueue_smooth(mgcfd_solver* s, int level) {
     A.n = D.n; A.level0 = level == 0; A.inv_div = 1.0 / (double)(kRK + 1 - rk);
     A.rec = D.rec; A.rec32 = D.rec32; A.old = D.old; A.flux = D.flux; A.fe = D.fe;
     A.a_off = D.a_off; A.b_off = D.b_off; A.b_list = D.b_list; A.inv_vol = D.inv_vol; A.bidx = D.bidx;
-    A.bdata = D.bdata; A.res = D.res; A.dt_key = &s->st->dt_key[level]; A.st = s->st;
-    const int gn = grid(D.n, kNodeThreads);
+    A.bdata = D.bdata; A.res = D.res; A.dt_key = key; A.st = s->st;
+    A.mesh_id = D.mesh_id; A.seg_neg = s->seg_neg; A.seg_bad = s->seg_bad; A.seg_rms = s->seg_rms;
+    A.seg_rho = s->seg_rho;
     const bool last = rk == kRK - 1;
-    if (s->gather) {
-      if (last && mixed) k_update<true, true, true><<<gn, kNodeThreads, 0, s->stream>>>(A);
-      else if (last) k_update<true, true, false><<<gn, kNodeThreads, 0, s->stream>>>(A);
-      else if (mixed) k_update<true, false, true><<<gn, kNodeThreads, 0, s->stream>>>(A);
-      else k_update<true, false, false><<<gn, kNodeThreads, 0, s->stream>>>(A);
-    } else {
-      if (last && mixed) k_update<false, true, true><<<gn, kNodeThreads, 0, s->stream>>>(A);
-      else if (last) k_update<false, true, false><<<gn, kNodeThreads, 0, s->stream>>>(A);
-      else if (mixed) k_update<false, false, true><<<gn, kNodeThreads, 0, s->stream>>>(A);
-      else k_update<false, false, false><<<gn, kNodeThreads, 0, s->stream>>>(A);
-    }
+    kUpdate[(s->gather ? 8 : 0) | (last ? 4 : 0) | (mixed ? 2 : 0) | (seg ? 1 : 0)](grid(D.n, kNodeThreads), s->stream, A);
     s->launches++;
     if (s->opt.measure_mem_bound && D.ne > 0) {
       k_stream<<<grid(D.ne, et), et, 0, s->stream>>>(D.ne, D.e2n, D.w4, D.rec, D.dummy, s->st);
@@ -564,6 +651,14 @@ int collect_timings(mgcfd_solver* s) {
 }
 
 int read_status(mgcfd_solver* s) {
+  if (s->nseg > 1) {  // batched: per-mesh outcome, the batch itself keeps going
+    std::vector<int> neg((size_t)s->nseg), bad((size_t)s->nseg);
+    CK(cudaMemcpy(neg.data(), s->seg_neg, sizeof(int) * neg.size(), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(bad.data(), s->seg_bad, sizeof(int) * bad.size(), cudaMemcpyDeviceToHost));
+    for (int m = 0; m < s->nseg; m++)
+      s->seg_status[(size_t)m] = neg[(size_t)m] ? MGCFD_ERR_NEGATIVE_DT : bad[(size_t)m] ? MGCFD_ERR_BAD_VALUES : MGCFD_OK;
+    return MGCFD_OK;
+  }
   DevStatus h;
   CK(cudaMemcpy(&h, s->st, sizeof(h), cudaMemcpyDeviceToHost));
   if (h.neg_dt) {
@@ -589,7 +684,10 @@ int read_status(mgcfd_solver* s) {
 int init_state(mgcfd_solver* s) {
   const double* v = s->ff.ff_variable;
   for (auto& D : s->L) {
-    k_init_state<<<grid(D.n, kNodeThreads), kNodeThreads, 0, s->stream>>>(D.n, D.rec, v[0], v[1], v[2], v[3], v[4]);
+    if (s->nseg > 1)
+      k_init_state_seg<<<grid(D.n, kNodeThreads), kNodeThreads, 0, s->stream>>>(D.n, D.rec, D.mesh_id, s->seg_ffvar);
+    else
+      k_init_state<<<grid(D.n, kNodeThreads), kNodeThreads, 0, s->stream>>>(D.n, D.rec, v[0], v[1], v[2], v[3], v[4]);
     CK(cudaMemsetAsync(D.old, 0, sizeof(double) * 5 * (size_t)D.n, s->stream));
     CK(cudaMemsetAsync(D.res, 0, sizeof(double) * 5 * (size_t)D.n, s->stream));
     if (D.flux) CK(cudaMemsetAsync(D.flux, 0, sizeof(double) * 5 * (size_t)D.n, s->stream));
@@ -597,6 +695,15 @@ int init_state(mgcfd_solver* s) {
   }
   CK(cudaMemsetAsync(s->st, 0, sizeof(DevStatus), s->stream));
   CK(cudaMemsetAsync(s->st->dt_key, 0xff, sizeof(s->st->dt_key), s->stream));
+  if (s->nseg > 1) {
+    const size_t ns = (size_t)s->nseg;
+    CK(cudaMemsetAsync(s->seg_keys, 0xff, sizeof(unsigned long long) * kMaxLevels * ns, s->stream));
+    CK(cudaMemsetAsync(s->seg_neg, 0, sizeof(int) * ns, s->stream));
+    CK(cudaMemsetAsync(s->seg_bad, 0, sizeof(int) * ns, s->stream));
+    CK(cudaMemsetAsync(s->seg_rms, 0, sizeof(double) * ns, s->stream));
+    CK(cudaMemsetAsync(s->seg_rho, 0, sizeof(double) * ns, s->stream));
+  }
+  s->seg_status.assign((size_t)s->nseg, MGCFD_OK);
   CK(cudaGetLastError());
   s->cycle = 0; s->level = 0; s->up = true; s->steps = 0; s->launches = 0;
   s->flux_ms = 0.0; s->flux_sweeps = 0; s->status = MGCFD_OK;
@@ -640,7 +747,8 @@ extern "C" int mgcfd_solver_create(int32_t nlevels, const mgcfd_level_view* leve
     return set_error(MGCFD_ERR_INVALID, "unknown precision");
   if (s->opt.block_size < 0 || s->opt.block_size > 1024 || (s->opt.block_size % 32) != 0)
     return set_error(MGCFD_ERR_INVALID, "block_size must be 0 or a multiple of 32 up to 1024");
-  s->gather = s->opt.increment == MGCFD_INCREMENT_GATHER;
+  s->gather = s->opt.increment == MGCFD_INCREMENT_GATHER ||
+              (s->opt.increment == MGCFD_INCREMENT_AUTO && s->opt.precision == MGCFD_PRECISION_MIXED);
   s->stream = static_cast<cudaStream_t>(stream);
   CK(cudaGetDevice(&s->device));
   if (!s->stream) {
@@ -667,10 +775,12 @@ extern "C" int mgcfd_solver_create(int32_t nlevels, const mgcfd_level_view* leve
   const bool host_setup = s->opt.host_setup || s->opt.renumber == MGCFD_RENUMBER_RCM;
   if (!host_setup) {
     if ((r = validate_views(nlevels, levels, false))) return r;
-    if ((r = device_prepare(s.get(), nlevels, levels))) return r;
+    if ((r = device_prepare(s.get(), {MeshInput{levels, s->ff}}))) return r;
   }
   std::vector<PreparedLevel> P;
   if (host_setup) {
+    s->seg_noff.assign((size_t)nlevels, std::vector<int32_t>(2, 0));
+    for (int l = 0; l < nlevels; l++) s->seg_noff[(size_t)l][1] = levels[l].nnodes;
     try {
       r = prepare_mesh(nlevels, levels, s->ff, s->opt.renumber, &P);
     } catch (const std::bad_alloc&) {
@@ -723,6 +833,62 @@ extern "C" int mgcfd_solver_create(int32_t nlevels, const mgcfd_level_view* leve
     CK(cudaStreamSynchronize(s->stream));
   }
   if ((r = s->alloc(&s->st, 1)) || (r = s->alloc(&s->fetch_buf, 5 * max_n))) return r;
+  if ((r = init_state(s.get()))) return r;
+  CK(cudaStreamSynchronize(s->stream));
+  *out = s.release();
+  return MGCFD_OK;
+}
+
+extern "C" int mgcfd_batch_create(int32_t nmeshes, int32_t nlevels, const mgcfd_level_view* const* levels,
+                                  const double* mach, const double* aoa_deg, const mgcfd_solver_options* opt,
+                                  void* stream, mgcfd_solver** out) {
+  if (!out) return set_error(MGCFD_ERR_INVALID, "mgcfd_batch_create: null output");
+  *out = nullptr;
+  if (nmeshes < 1 || !levels || !mach || !aoa_deg) return set_error(MGCFD_ERR_INVALID, "mgcfd_batch_create: no meshes");
+  if (nlevels < 1 || nlevels > kMaxLevels) return set_error(MGCFD_ERR_INVALID, "mgcfd_batch_create: 1..16 levels supported");
+  std::unique_ptr<mgcfd_solver, void (*)(mgcfd_solver*)> s(new (std::nothrow) mgcfd_solver(), free_solver);
+  if (!s) return set_error(MGCFD_ERR_NOMEM, "host allocation failed");
+  if (opt) s->opt = *opt; else mgcfd_solver_default_options(&s->opt);
+  if (s->opt.precision != MGCFD_PRECISION_FP64 && s->opt.precision != MGCFD_PRECISION_MIXED)
+    return set_error(MGCFD_ERR_INVALID, "unknown precision");
+  if (s->opt.block_size < 0 || s->opt.block_size > 1024 || (s->opt.block_size % 32) != 0)
+    return set_error(MGCFD_ERR_INVALID, "block_size must be 0 or a multiple of 32 up to 1024");
+  if (s->opt.renumber == MGCFD_RENUMBER_RCM || s->opt.host_setup)
+    return set_error(MGCFD_ERR_INVALID, "batched solvers are set up on the device (renumber none or spatial)");
+  s->gather = s->opt.increment == MGCFD_INCREMENT_GATHER ||
+              (s->opt.increment == MGCFD_INCREMENT_AUTO && s->opt.precision == MGCFD_PRECISION_MIXED);
+  s->stream = static_cast<cudaStream_t>(stream);
+  CK(cudaGetDevice(&s->device));
+  if (!s->stream) {
+    CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+    s->owns_stream = true;
+  }
+  int r;
+  std::vector<MeshInput> meshes((size_t)nmeshes);
+  s->seg_ff.resize((size_t)nmeshes);
+  std::vector<double> ffvar(5 * (size_t)nmeshes);
+  int64_t total0 = 0;
+  for (int m = 0; m < nmeshes; m++) {
+    if ((r = validate_views(nlevels, levels[m], false))) return r;
+    mgcfd_freestream_init(mach[m], aoa_deg[m], &s->seg_ff[(size_t)m]);
+    meshes[(size_t)m] = MeshInput{levels[m], s->seg_ff[(size_t)m]};
+    for (int k = 0; k < 5; k++) ffvar[5 * (size_t)m + k] = s->seg_ff[(size_t)m].ff_variable[k];
+    total0 += levels[m][0].nnodes;
+  }
+  if (total0 > 2147483647ll) return set_error(MGCFD_ERR_INVALID, "batch too large for int32 node ids");
+  s->ff = s->seg_ff[0];
+  s->nseg = nmeshes;
+  s->L.resize((size_t)nlevels);
+  if ((r = device_prepare(s.get(), meshes))) return r;
+  size_t max_n = 0;
+  for (auto& D : s->L) max_n = std::max(max_n, (size_t)D.n);
+  const size_t ns = (size_t)nmeshes;
+  if ((r = s->alloc(&s->st, 1)) || (r = s->alloc(&s->fetch_buf, 5 * max_n)) ||
+      (r = s->alloc(&s->seg_keys, kMaxLevels * ns)) || (r = s->alloc(&s->seg_neg, ns)) ||
+      (r = s->alloc(&s->seg_bad, ns)) || (r = s->alloc(&s->seg_rms, ns)) || (r = s->alloc(&s->seg_rho, ns)) ||
+      (r = s->upload(&s->seg_ffvar, ffvar.data(), 5 * ns)))
+    return r;
+  CK(cudaStreamSynchronize(s->stream));  // ffvar host buffer
   if ((r = init_state(s.get()))) return r;
   CK(cudaStreamSynchronize(s->stream));
   *out = s.release();
@@ -789,42 +955,76 @@ extern "C" int mgcfd_solver_synchronize(mgcfd_solver* s) {
   return read_status(s);
 }
 
-extern "C" int mgcfd_solver_fetch(mgcfd_solver* s, int32_t level, int32_t q, double* host_out) {
-  if (!s || !host_out) return set_error(MGCFD_ERR_INVALID, "mgcfd_solver_fetch: null argument");
-  if (level < 0 || level >= (int)s->L.size()) return set_error(MGCFD_ERR_INVALID, "mgcfd_solver_fetch: bad level");
+namespace {
+int fetch_rows(mgcfd_solver* s, int32_t level, int32_t q, int32_t off, int32_t n, double* host_out) {
   DevLevel& D = s->L[(size_t)level];
   const int T = 256;
   int width = 5;
+  const unsigned long long* keys = s->nseg > 1 ? s->seg_keys + (size_t)level * s->nseg : &s->st->dt_key[level];
   switch (q) {
     case MGCFD_Q_VARIABLES:
-      k_unpermute<<<grid((int64_t)D.n * 5, T), T, 0, s->stream>>>(D.n, 5, 8, D.rec, D.perm, s->fetch_buf);
+      k_unpermute<<<grid((int64_t)n * 5, T), T, 0, s->stream>>>(n, off, 5, 8, D.rec, D.perm, s->fetch_buf);
       break;
     case MGCFD_Q_FLUXES:
-      if (D.flux) k_unpermute<<<grid((int64_t)D.n * 5, T), T, 0, s->stream>>>(D.n, 5, 5, D.flux, D.perm, s->fetch_buf);
-      else CK(cudaMemsetAsync(s->fetch_buf, 0, sizeof(double) * 5 * (size_t)D.n, s->stream));
+      if (D.flux) k_unpermute<<<grid((int64_t)n * 5, T), T, 0, s->stream>>>(n, off, 5, 5, D.flux, D.perm, s->fetch_buf);
+      else CK(cudaMemsetAsync(s->fetch_buf, 0, sizeof(double) * 5 * (size_t)n, s->stream));
       break;
     case MGCFD_Q_RESIDUALS:
-      k_unpermute<<<grid((int64_t)D.n * 5, T), T, 0, s->stream>>>(D.n, 5, 5, D.res, D.perm, s->fetch_buf);
+      k_unpermute<<<grid((int64_t)n * 5, T), T, 0, s->stream>>>(n, off, 5, 5, D.res, D.perm, s->fetch_buf);
       break;
     case MGCFD_Q_OLD_VARIABLES:
-      k_unpermute<<<grid((int64_t)D.n * 5, T), T, 0, s->stream>>>(D.n, 5, 5, D.old, D.perm, s->fetch_buf);
+      k_unpermute<<<grid((int64_t)n * 5, T), T, 0, s->stream>>>(n, off, 5, 5, D.old, D.perm, s->fetch_buf);
       break;
     case MGCFD_Q_VOLUMES:
       width = 1;
-      k_unpermute<<<grid(D.n, T), T, 0, s->stream>>>(D.n, 1, 1, D.vol, D.perm, s->fetch_buf);
+      k_unpermute<<<grid(n, T), T, 0, s->stream>>>(n, off, 1, 1, D.vol, D.perm, s->fetch_buf);
       break;
     case MGCFD_Q_STEP_FACTORS:
       width = 1;
-      k_step_factors<<<grid(D.n, T), T, 0, s->stream>>>(D.n, D.vol, &s->st->dt_key[level], D.perm, s->fetch_buf);
+      k_step_factors<<<grid(n, T), T, 0, s->stream>>>(n, off, D.vol, keys, D.mesh_id, D.perm, s->fetch_buf);
       break;
     default:
       return set_error(MGCFD_ERR_INVALID, "mgcfd_solver_fetch: unknown quantity");
   }
   CK(cudaGetLastError());
-  CK(cudaMemcpyAsync(host_out, s->fetch_buf, sizeof(double) * (size_t)width * (size_t)D.n, cudaMemcpyDeviceToHost,
+  CK(cudaMemcpyAsync(host_out, s->fetch_buf, sizeof(double) * (size_t)width * (size_t)n, cudaMemcpyDeviceToHost,
                      s->stream));
   CK(cudaStreamSynchronize(s->stream));
   return MGCFD_OK;
+}
+}  // namespace
+
+extern "C" int mgcfd_solver_fetch(mgcfd_solver* s, int32_t level, int32_t q, double* host_out) {
+  if (!s || !host_out) return set_error(MGCFD_ERR_INVALID, "mgcfd_solver_fetch: null argument");
+  if (level < 0 || level >= (int)s->L.size()) return set_error(MGCFD_ERR_INVALID, "mgcfd_solver_fetch: bad level");
+  return fetch_rows(s, level, q, 0, s->L[(size_t)level].n, host_out);
+}
+
+extern "C" int mgcfd_solver_fetch_mesh(mgcfd_solver* s, int32_t mesh, int32_t level, int32_t q, double* host_out) {
+  if (!s || !host_out) return set_error(MGCFD_ERR_INVALID, "mgcfd_solver_fetch_mesh: null argument");
+  if (level < 0 || level >= (int)s->L.size()) return set_error(MGCFD_ERR_INVALID, "mgcfd_solver_fetch_mesh: bad level");
+  if (mesh < 0 || mesh >= s->nseg) return set_error(MGCFD_ERR_INVALID, "mgcfd_solver_fetch_mesh: bad mesh");
+  const int32_t off = s->seg_noff[(size_t)level][(size_t)mesh];
+  return fetch_rows(s, level, q, off, s->seg_noff[(size_t)level][(size_t)mesh + 1] - off, host_out);
+}
+
+extern "C" int mgcfd_solver_num_meshes(const mgcfd_solver* s) { return s ? s->nseg : 0; }
+
+extern "C" int mgcfd_solver_mesh_status(mgcfd_solver* s, int32_t mesh, double* rms_l0, double* rho_rms_l0) {
+  if (!s || mesh < 0 || mesh >= s->nseg) return set_error(MGCFD_ERR_INVALID, "mgcfd_solver_mesh_status: bad mesh");
+  int r = mgcfd_solver_synchronize(s);
+  if (r && s->nseg > 1) return r;
+  double acc[2] = {0.0, 0.0};
+  const double n0 = (double)(s->seg_noff[0][(size_t)mesh + 1] - s->seg_noff[0][(size_t)mesh]);
+  if (s->nseg > 1) {
+    CK(cudaMemcpy(&acc[0], s->seg_rms + mesh, sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&acc[1], s->seg_rho + mesh, sizeof(double), cudaMemcpyDeviceToHost));
+  } else {
+    CK(cudaMemcpy(acc, &s->st->rms_acc, 2 * sizeof(double), cudaMemcpyDeviceToHost));
+  }
+  if (rms_l0) *rms_l0 = std::sqrt(acc[0] / n0);      // euler3d.cpp:537
+  if (rho_rms_l0) *rho_rms_l0 = std::sqrt(acc[1] / n0);
+  return s->nseg > 1 ? s->seg_status[(size_t)mesh] : r;
 }
 
 extern "C" int mgcfd_solver_get_stats(mgcfd_solver* s, mgcfd_solver_stats* o) {

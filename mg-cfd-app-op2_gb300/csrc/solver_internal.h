@@ -29,6 +29,7 @@ struct DevStatus {
   int bad_count;                           // NaN/Inf count at level 0
   int pad;
   double rms_acc;                          // sum of residual^2, last level-0 step
+  double rho_acc;                          // its density part
 };
 
 struct DevLevel {
@@ -58,6 +59,7 @@ struct DevLevel {
   int32_t* ch_off = nullptr;
   int32_t* ch_list = nullptr;
   int32_t* perm = nullptr;
+  int32_t* mesh_id = nullptr;  // [n] mesh of each node (batched solvers only)
 };
 
 struct mgcfd_solver {
@@ -71,6 +73,17 @@ struct mgcfd_solver {
   DevStatus* st = nullptr;
   double* fetch_buf = nullptr;
   int64_t device_bytes = 0;
+  // Batched solvers: nseg meshes concatenated per level (nseg == 1: plain).
+  int nseg = 1;
+  std::vector<std::vector<int32_t>> seg_noff;    // [level][nseg + 1] node offsets
+  std::vector<mgcfd_freestream> seg_ff;          // per mesh
+  unsigned long long* seg_keys = nullptr;        // [kMaxLevels][nseg] min_dt keys
+  int* seg_neg = nullptr;                        // [nseg] min_dt < 0 seen
+  int* seg_bad = nullptr;                        // [nseg] NaN/Inf count at level 0
+  double* seg_rms = nullptr;                     // [nseg] sum of residual^2, last level-0 step
+  double* seg_rho = nullptr;                     // [nseg] its density part
+  double* seg_ffvar = nullptr;                   // [nseg][5] freestream states
+  std::vector<int> seg_status;                   // host copy after synchronize
   // V-cycle state (euler3d.cpp:452-457).
   int64_t cycle = 0;
   int level = 0;
@@ -110,7 +123,12 @@ struct mgcfd_solver {
 };
 
 namespace mgcfd {
-// Builds every per-level device table of `s` from the host level views on the
-// GPU (device_setup.cu).  Same results as prepare_mesh() in setup.cpp.
-int device_prepare(mgcfd_solver* s, int32_t nlevels, const mgcfd_level_view* levels);
+struct MeshInput {
+  const mgcfd_level_view* levels;  // s->L.size() levels
+  mgcfd_freestream ff;
+};
+// Builds every per-level device table of `s` on the GPU from one or more
+// meshes (concatenated per level, each renumbered on its own), device_setup.cu.
+// For one mesh the results equal prepare_mesh() in setup.cpp.
+int device_prepare(mgcfd_solver* s, const std::vector<MeshInput>& meshes);
 }  // namespace mgcfd

@@ -3,6 +3,7 @@
 Outputs (all git-ignored, rebuilt when a source is newer than the output):
   mg-cfd-app-op2_gb300/lib/libmgcfd_gb300.so   the product: CUDA kernels + C ABI
   mg-cfd-app-op2_gb300/bin/euler3d_gb300        euler3d-compatible command line driver
+  mg-cfd-app-op2_gb300/bin/mgcfd_renumber       standalone mesh renumbering tool
   oracle/_build/liboracle.so                    the oracle (C restatement), test-only
   oracle/_build/mgcfd_oracle_run                the oracle as a timed CPU baseline, test-only
   oracle/_ref/euler3d_ref                       reference euler3d.cpp against the OP2
@@ -27,6 +28,8 @@ CSRC = PKG / "csrc"
 INCLUDE = ROOT / "include"
 LIB = PKG / "lib" / "libmgcfd_gb300.so"
 CLI = PKG / "bin" / "euler3d_gb300"
+RENUMBER_CLI = PKG / "bin" / "mgcfd_renumber"
+TOOLS = {"euler3d_gb300.cpp": CLI, "mgcfd_renumber.cpp": RENUMBER_CLI}
 OBJ = PKG / "_build"
 ORACLE = ROOT / "oracle"
 ORACLE_LIB = ORACLE / "_build" / "liboracle.so"
@@ -77,7 +80,7 @@ def _headers():
 
 
 def library_sources():
-    return sorted(CSRC.glob("*.cu")), sorted(p for p in CSRC.glob("*.cpp") if p.name != "euler3d_gb300.cpp")
+    return sorted(CSRC.glob("*.cu")), sorted(p for p in CSRC.glob("*.cpp") if p.name not in TOOLS)
 
 
 def build_library(force: bool = False, jobs: int | None = None) -> Path:
@@ -106,11 +109,12 @@ def build_library(force: bool = False, jobs: int | None = None) -> Path:
                 f.result()
     if force or jobs_list or _stale(LIB, objs):
         _run([nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lpthread"])
-    cli_src = CSRC / "euler3d_gb300.cpp"
-    if cli_src.exists() and (force or _stale(CLI, [cli_src, LIB] + hdrs)):
-        CLI.parent.mkdir(parents=True, exist_ok=True)
-        _run(["g++", *CXX_FLAGS, str(cli_src), "-o", str(CLI), f"-L{LIB.parent}", "-lmgcfd_gb300",
-              f"-Wl,-rpath,{LIB.parent}", "-Wl,-rpath,$ORIGIN/../lib"])
+    for name, exe in TOOLS.items():
+        src = CSRC / name
+        if src.exists() and (force or _stale(exe, [src, LIB] + hdrs)):
+            exe.parent.mkdir(parents=True, exist_ok=True)
+            _run(["g++", *CXX_FLAGS, str(src), "-o", str(exe), f"-L{LIB.parent}", "-lmgcfd_gb300",
+                  f"-Wl,-rpath,{LIB.parent}", "-Wl,-rpath,$ORIGIN/../lib"])
     _write_stamp(OBJ)
     return LIB
 

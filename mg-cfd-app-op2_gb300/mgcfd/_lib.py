@@ -42,6 +42,24 @@ class SolverStats(C.Structure):
                 ("rms_l0", C.c_double), ("status", C.c_int32), ("ncolors_reserved", C.c_int32)]
 
 
+class ServerOptions(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_int64), ("max_active", C.c_int32), ("precision", C.c_int32),
+                ("increment", C.c_int32), ("max_cycles", C.c_int32), ("residual_drop", C.c_double),
+                ("reserved", C.c_int32 * 8)]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [("id", C.c_int64), ("status", C.c_int32), ("cycles", C.c_int32), ("submit_s", C.c_double),
+                ("admit_s", C.c_double), ("finish_s", C.c_double), ("rho_rms_first", C.c_double),
+                ("rho_rms_last", C.c_double), ("reserved", C.c_int64 * 2)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("failed", C.c_int64), ("active", C.c_int64),
+                ("pending", C.c_int64), ("used_bytes", C.c_int64), ("peak_bytes", C.c_int64),
+                ("peak_active", C.c_int64), ("reserved", C.c_int64 * 4)]
+
+
 OK = 0
 ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_IO, ERR_NEGATIVE_DT, ERR_BAD_VALUES, ERR_TIMEOUT, ERR_BUDGET = range(1, 9)
 
@@ -61,6 +79,8 @@ SIGNATURES = {
     "mgcfd_host_mesh_num_levels": (C.c_int, [_vp]),
     "mgcfd_host_mesh_level": (C.c_int, [_vp, C.c_int, _pp(LevelView)]),
     "mgcfd_host_mesh_destroy": (None, [_vp]),
+    "mgcfd_renumber_nodes": (C.c_int, [C.c_int, _i32, c_double_p, _i32, c_int32_p, c_int32_p]),
+    "mgcfd_host_mesh_renumber": (C.c_int, [_vp, C.c_int, C.POINTER(_vp)]),
     "mgcfd_h5_dataset_shape": (C.c_int, [C.c_char_p, C.c_char_p, _pp(C.c_int64), _pp(C.c_int)]),
     "mgcfd_h5_read_f64": (C.c_int, [C.c_char_p, C.c_char_p, c_double_p, C.c_int64]),
     "mgcfd_h5_read_i32": (C.c_int, [C.c_char_p, C.c_char_p, c_int32_p, C.c_int64]),
@@ -98,6 +118,20 @@ SIGNATURES = {
     "mgcfd_solver_get_stats": (C.c_int, [_vp, _pp(SolverStats)]),
     "mgcfd_solver_destroy": (None, [_vp]),
     "mgcfd_solver_table": (C.c_int, [_vp, _i32, _i32, _vp, C.c_int64, _pp(C.c_int64)]),
+    "mgcfd_batch_create": (C.c_int, [_i32, _i32, _pp(_pp(LevelView)), _pp(C.c_double), _pp(C.c_double),
+                                     _pp(SolverOptions), _vp, _pp(_vp)]),
+    "mgcfd_solver_num_meshes": (C.c_int, [_vp]),
+    "mgcfd_solver_fetch_mesh": (C.c_int, [_vp, _i32, _i32, _i32, c_double_p]),
+    "mgcfd_solver_mesh_status": (C.c_int, [_vp, _i32, _pp(C.c_double), _pp(C.c_double)]),
+    "mgcfd_server_default_options": (None, [_pp(ServerOptions)]),
+    "mgcfd_server_create": (C.c_int, [_pp(ServerOptions), _pp(_vp)]),
+    "mgcfd_server_submit": (C.c_int, [_vp, _i32, _pp(LevelView), C.c_double, C.c_double, c_double_p,
+                                      _pp(C.c_int64)]),
+    "mgcfd_server_poll": (C.c_int, [_vp, _pp(RequestResult), _i32, _pp(_i32)]),
+    "mgcfd_server_drain": (C.c_int, [_vp, C.c_double]),
+    "mgcfd_server_get_stats": (C.c_int, [_vp, _pp(ServerStats)]),
+    "mgcfd_server_destroy": (None, [_vp]),
+    "mgcfd_request_estimate_bytes": (C.c_int, [_i32, _pp(LevelView), _i32, _i32, _pp(C.c_int64)]),
     "mgcfd_solve": (C.c_int, [_i32, _pp(LevelView), C.c_double, C.c_double, _i32, _pp(SolverOptions),
                               _pp(c_double_p)]),
 }

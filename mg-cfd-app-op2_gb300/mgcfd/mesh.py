@@ -45,6 +45,21 @@ def _view(ptr, shape, dtype):
     return np.frombuffer(buf, dtype=dtype).reshape(shape)
 
 
+RENUMBER_METHODS = {"none": 0, "spatial": 1, "rcm": 2}
+
+
+def renumber_nodes(method: str, coords: np.ndarray, edge_to_nodes: np.ndarray | None = None) -> np.ndarray:
+    """perm[new] = old for one node set (mgcfd_renumber_nodes)."""
+    lib = _lib.load()
+    coords = np.ascontiguousarray(coords, dtype=np.float64)
+    e2n = np.ascontiguousarray(edge_to_nodes if edge_to_nodes is not None else np.zeros((0, 2)), dtype=np.int32)
+    perm = np.empty(len(coords), dtype=np.int32)
+    _lib.check(lib.mgcfd_renumber_nodes(RENUMBER_METHODS[method], len(coords), coords.ctypes.data_as(_lib.c_double_p),
+                                        len(e2n), e2n.ctypes.data_as(_lib.c_int32_p),
+                                        perm.ctypes.data_as(_lib.c_int32_p)))
+    return perm
+
+
 class HostMesh:
     """Owner of a native mgcfd_host_mesh; level arrays are zero-copy views."""
 
@@ -70,6 +85,13 @@ class HostMesh:
     def write(self, directory: str, prefix: str = "mesh_", legacy_datasets: bool = False) -> None:
         _lib.check(self._lib.mgcfd_host_mesh_write(self._h, str(directory).encode(), prefix.encode(),
                                                    int(legacy_datasets)))
+
+    def renumber(self, method: str = "spatial") -> "HostMesh":
+        """A relabelled copy of the mesh (mgcfd_host_mesh_renumber): nodes in
+        Morton ("spatial") or reverse Cuthill-McKee ("rcm") order on every level."""
+        h = C.c_void_p()
+        _lib.check(self._lib.mgcfd_host_mesh_renumber(self._h, RENUMBER_METHODS[method], C.byref(h)))
+        return HostMesh(h)
 
     @property
     def num_levels(self) -> int:

@@ -100,3 +100,46 @@ def solve(levels, mach, aoa_deg, ncycles, **opts):
     o = options(**opts)
     _lib.check(lib.mgcfd_solve(len(levels), views, mach, aoa_deg, ncycles, C.byref(o), ptrs))
     return outs
+
+
+class Batch(Solver):
+    """Many independent meshes solved together, one launch per V-cycle stage
+    (mgcfd_batch_create).  Each mesh has its own Mach number, angle of attack,
+    min_dt and outcome."""
+
+    def __init__(self, meshes, machs, aoas, stream: int | None = None, **opts):
+        self._lib = _lib.load()
+        level_lists = [m.levels() if isinstance(m, HostMesh) else m for m in meshes]
+        nl = len(level_lists[0])
+        if any(len(L) != nl for L in level_lists):
+            raise ValueError("all meshes of a batch need the same number of levels")
+        self._keep = (meshes, level_lists)
+        self._views = [level_views_from_arrays(L) for L in level_lists]
+        ptrs = (C.POINTER(_lib.LevelView) * len(meshes))(*[C.cast(v, C.POINTER(_lib.LevelView)) for v in self._views])
+        self._mesh_nn = [[L.nnodes for L in levels] for levels in level_lists]
+        self._nn = [sum(nn[l] for nn in self._mesh_nn) for l in range(nl)]
+        mach = (C.c_double * len(meshes))(*machs)
+        aoa = (C.c_double * len(meshes))(*aoas)
+        self.options = options(**opts)
+        h = C.c_void_p()
+        _lib.check(self._lib.mgcfd_batch_create(len(meshes), nl, ptrs, mach, aoa, C.byref(self.options),
+                                                C.c_void_p(stream) if stream else None, C.byref(h)))
+        self._h = h
+
+    @property
+    def num_meshes(self) -> int:
+        return len(self._mesh_nn)
+
+    def fetch_mesh(self, mesh: int, level: int, quantity: int = Q_VARIABLES) -> np.ndarray:
+        n = self._mesh_nn[mesh][level]
+        width = 1 if quantity in (Q_STEP_FACTORS, Q_VOLUMES) else 5
+        out = np.empty((n, width) if width > 1 else (n,), dtype=np.float64)
+        _lib.check(self._lib.mgcfd_solver_fetch_mesh(self._h, mesh, level, quantity,
+                                                     out.ctypes.data_as(_lib.c_double_p)))
+        return out
+
+    def mesh_status(self, mesh: int):
+        """(status, rms_l0, density_rms_l0) of one mesh after synchronising."""
+        rms, rho = C.c_double(), C.c_double()
+        st = self._lib.mgcfd_solver_mesh_status(self._h, mesh, C.byref(rms), C.byref(rho))
+        return st, rms.value, rho.value

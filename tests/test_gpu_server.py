@@ -1,0 +1,113 @@
+"""Serving loop: continuous admission under an HBM budget, overlapping
+requests, and identical results alone and in the mix (GPU)."""
+import time
+
+import numpy as np
+import pytest
+
+import mgcfd
+from mgcfd import server
+import oracle as O
+from parity import STATE_TOL, state_error
+
+pytestmark = pytest.mark.gpu
+
+CASES = [(14, 3, 1, 0.4, 1.0), (9, 2, 2, 0.8, 5.0), (18, 3, 3, 0.6, 3.0), (11, 3, 4, 0.3, 0.0), (20, 4, 5, 0.7, 2.0)]
+
+
+@pytest.fixture(scope="module")
+def meshes():
+    return [mgcfd.HostMesh.generate(n, nl, seed) for n, nl, seed, _, _ in CASES]
+
+
+def run_requests(srv, meshes, idx):
+    ids = {srv.submit(meshes[i], CASES[i][3], CASES[i][4], want_result=True): i for i in idx}
+    srv.drain(300)
+    out = {}
+    for res, var in srv.poll():
+        out[ids[res["id"]]] = (res, var)
+    return out
+
+
+def test_alone_equals_mix_bitwise_with_gather(meshes):
+    alone = {}
+    for i in range(len(CASES)):
+        srv = mgcfd.Server(max_active=1, increment="gather", max_cycles=4)
+        alone.update(run_requests(srv, meshes, [i]))
+        srv.close()
+    srv = mgcfd.Server(max_active=4, increment="gather", max_cycles=4)
+    mix = run_requests(srv, meshes, range(len(CASES)))
+    st = srv.stats()
+    srv.close()
+    assert st["completed"] == len(CASES) and st["failed"] == 0 and st["peak_active"] >= 2
+    for i in range(len(CASES)):
+        ra, va = alone[i]
+        rm, vm = mix[i]
+        assert ra["status"] == rm["status"] == 0 and ra["cycles"] == rm["cycles"] == 4
+        np.testing.assert_array_equal(va, vm)
+        ref = O.OracleRun(meshes[i].levels())
+        assert ref.run(CASES[i][3], CASES[i][4], 4)[0] == 0
+        assert state_error(vm, ref.get(0, O.Q_VARIABLES)) <= STATE_TOL
+
+
+def test_alone_equals_mix_within_tolerance_with_atomics(meshes):
+    srv = mgcfd.Server(max_active=1, increment="atomic", max_cycles=3)
+    alone = run_requests(srv, meshes, range(3))
+    srv.close()
+    srv = mgcfd.Server(max_active=3, increment="atomic", max_cycles=3)
+    mix = run_requests(srv, meshes, range(3))
+    srv.close()
+    for i in range(3):
+        assert state_error(mix[i][1], alone[i][1]) <= STATE_TOL
+
+
+def test_budget_admits_one_at_a_time_and_rejects_oversized(meshes):
+    small = mgcfd.HostMesh.generate(10, 2, 8)
+    one = server.estimate_bytes(small)
+    assert server.estimate_bytes(meshes[4]) > 1.5 * one
+    srv = mgcfd.Server(hbm_budget_gb=1.5 * one / 2 ** 30, max_active=8, max_cycles=2)  # room for one small request
+    ids = [srv.submit(small, 0.5, 1.0) for _ in range(4)]
+    big = srv.submit(meshes[4], 0.5, 1.0)
+    srv.drain(300)
+    results = {r["id"]: r for r, _ in srv.poll()}
+    st = srv.stats()
+    srv.close()
+    assert st["peak_active"] == 1
+    assert all(results[i]["status"] == 0 for i in ids)
+    assert results[big]["status"] == mgcfd._lib.ERR_BUDGET
+    # admitted strictly one after another
+    spans = sorted((results[i]["admit_s"], results[i]["finish_s"]) for i in ids)
+    assert all(spans[k + 1][0] >= spans[k][1] - 1e-6 for k in range(len(spans) - 1))
+
+
+def test_later_arrival_overlaps_running_request(meshes):
+    big = mgcfd.HostMesh.generate(48, 3, 2)
+    srv = mgcfd.Server(max_active=4, max_cycles=400, residual_drop=0.0)
+    first = srv.submit(big, 0.5, 1.0)
+    t0 = time.perf_counter()
+    while srv.stats()["active"] == 0 and time.perf_counter() - t0 < 60:
+        time.sleep(0.001)
+    second = srv.submit(meshes[0], 0.6, 2.0)
+    srv.drain(300)
+    res = {r["id"]: r for r, _ in srv.poll()}
+    srv.close()
+    assert res[first]["status"] == res[second]["status"] == 0
+    assert res[second]["admit_s"] < res[first]["finish_s"]  # joined while the first was running
+
+
+def test_failing_request_does_not_disturb_others(meshes):
+    levels = meshes[1].levels()
+    bad = [mgcfd.Level(**{k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in L.__dict__.items()
+                          if k != "owner"}) for L in levels]
+    bad[0].edge_weights[3, :] = np.nan
+    srv = mgcfd.Server(max_active=4, increment="gather", max_cycles=3)
+    good = srv.submit(meshes[0], CASES[0][3], CASES[0][4], want_result=True)
+    broken = srv.submit(bad, 0.5, 1.0)
+    srv.drain(300)
+    res = {r["id"]: (r, v) for r, v in srv.poll()}
+    srv.close()
+    assert res[broken][0]["status"] == mgcfd._lib.ERR_BAD_VALUES
+    assert res[good][0]["status"] == 0
+    ref = O.OracleRun(meshes[0].levels())
+    assert ref.run(CASES[0][3], CASES[0][4], 3)[0] == 0
+    assert state_error(res[good][1], ref.get(0, O.Q_VARIABLES)) <= STATE_TOL
