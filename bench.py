@@ -38,9 +38,22 @@ MACH, AOA, NLEVELS, SEED = 0.8, 3.0, 4, 20240501
 E2E_CYCLES = 25
 
 
-def algorithmic_flux_bytes(nnodes: int, nedges: int) -> int:
-    """Per level-0 flux sweep: 24 B weights + 8 B map per edge; 80 B state
-    read, 40 B flux read and 40 B flux written per node."""
+def algorithmic_flux_bytes(nnodes: int, nedges: int, precision: str = "fp64", increment: str = "atomic") -> int:
+    """Bytes one level-0 flux sweep must move at least.
+
+    FP64: 24 B weights + 8 B map per edge; 80 B state read, 40 B flux read
+    and 40 B flux written per node (the reference's own model of the loop
+    plus the map and the read half of the increment).
+    Mixed, edge kernel: 16 B FP32 weights + 8 B map read and 20 B FP32 edge
+    flux written per edge; 32 B FP32 primitives read per node.
+    Mixed, fused stage (flux and time step in one node kernel): per edge the
+    a-side weights + map (24 B) and the b-side copies (20 B); per node the
+    FP32 primitives read (32 B), old state (40 B), 1/vol, boundary index and
+    CSR offsets (20 B), state written (40 B) and next primitives written (32 B)."""
+    if precision == "mixed" and increment == "fused":
+        return 44 * nedges + 164 * nnodes
+    if precision == "mixed":
+        return 44 * nedges + 32 * nnodes
     return 32 * nedges + 120 * nnodes
 
 
@@ -108,13 +121,6 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def dist_setup():
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return world, rank, local
-
-
 def run_gb300(args):
     import ctypes as C
 
@@ -124,26 +130,23 @@ def run_gb300(args):
     import mgcfd
     from mgcfd import _lib
 
-    world, rank, local = dist_setup()
+    from mgcfd import replicas
+    world, rank, local = replicas.world()
     torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    dist = replicas.init()
 
     mesh = mgcfd.HostMesh.generate(args.n, NLEVELS, SEED)
     L0 = mesh.level(0)
     N, E = L0.nnodes, L0.nedges
     solver = mgcfd.Solver(mesh, MACH, AOA, precision=args.precision, increment=args.increment,
-                          renumber=args.renumber, time_kernels=True)
+                          renumber=args.renumber, accumulation=args.accumulation, time_kernels=True)
     solver.run(args.warmup)
     if solver.synchronize() != 0:
         raise RuntimeError(_lib.load().mgcfd_last_error().decode())
     st0 = solver.stats()
 
     def barrier():
-        if dist:
-            dist.barrier()
+        replicas.barrier(dist)
 
     barrier()
     torch.cuda.synchronize()
@@ -157,13 +160,26 @@ def run_gb300(args):
     if status != 0:
         raise RuntimeError(_lib.load().mgcfd_last_error().decode())
     st1 = solver.stats()
-    elapsed = t1 - t0
-    if dist:
-        t = torch.tensor([elapsed], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
+    value, elapsed = replicas.job_throughput(args.steps, t1 - t0, dist, device="cuda")
     flux_ms = (st1.flux_ms_l0 - st0.flux_ms_l0) / max(1, st1.flux_sweeps_l0 - st0.flux_sweeps_l0)
     launches = int(st1.kernel_launches - st0.kernel_launches)
+    precision_error = None
+    if args.precision == "mixed":
+        # Final level-0 state against an FP64 solve of the same cycles:
+        # per-variable max and L2 relative error (density, 3 momenta, energy).
+        got = solver.fetch(0)
+        ref_solver = mgcfd.Solver(mesh, MACH, AOA, precision="fp64", renumber=args.renumber)
+        ref_solver.run(args.warmup + args.steps)
+        if ref_solver.synchronize() != 0:
+            raise RuntimeError(_lib.load().mgcfd_last_error().decode())
+        ref = ref_solver.fetch(0)
+        ref_solver.close()
+        d = got - ref
+        precision_error = {
+            "variables": ["rho", "rho_u", "rho_v", "rho_w", "rho_E"],
+            "max_rel": [float(np.max(np.abs(d[:, k])) / np.max(np.abs(ref[:, k]))) for k in range(5)],
+            "l2_rel": [float(np.linalg.norm(d[:, k]) / np.linalg.norm(ref[:, k])) for k in range(5)],
+            "cycles": args.warmup + args.steps, "against": "FP64 solve of the same mesh and cycles"}
     solver.close()
 
     # End to end through the host-buffer entry point, pinned host memory.
@@ -181,7 +197,8 @@ def run_gb300(args):
     outs = [torch.empty((L.nnodes, 5), dtype=torch.float64).pin_memory() for L in levels]
     views = mgcfd.level_views_from_arrays(hl)
     out_ptrs = (_lib.c_double_p * len(outs))(*[C.cast(o.data_ptr(), _lib.c_double_p) for o in outs])
-    opts = mgcfd.options(precision=args.precision, increment=args.increment, renumber=args.renumber)
+    opts = mgcfd.options(precision=args.precision, increment=args.increment, renumber=args.renumber,
+                         accumulation=args.accumulation)
     lib = _lib.load()
     h2d = sum(a.nbytes for L in hl for a in (L.coords, L.edge_to_nodes, L.bnd_to_node, L.bnd_group, L.edge_weights,
                                               L.bnd_weights) + ((L.node_to_mg,) if L.node_to_mg is not None else ()))
@@ -194,11 +211,7 @@ def run_gb300(args):
         _lib.check(lib.mgcfd_solve(len(hl), views, MACH, AOA, E2E_CYCLES, C.byref(opts), out_ptrs))
     te1 = time.perf_counter()
     barrier()
-    e2e_elapsed = te1 - te0
-    if dist:
-        t = torch.tensor([e2e_elapsed], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_elapsed = float(t.item())
+    e2e_value, e2e_elapsed = replicas.job_throughput(e2e_steps * E2E_CYCLES, te1 - te0, dist, device="cuda")
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -209,11 +222,20 @@ def run_gb300(args):
             dist.destroy_process_group()
         return
     peak, peak_kind = measured_peaks()
-    bytes_per_sweep = algorithmic_flux_bytes(N, E)
+    inc = args.increment if args.increment != "auto" else ("fused" if args.precision == "mixed" else "atomic")
+    bytes_per_sweep = algorithmic_flux_bytes(N, E, args.precision, inc)
     achieved = bytes_per_sweep / (flux_ms * 1e-3) / 1e9
-    prof = committed_profile(f"flux_edge_{args.precision}_{args.increment}.json") or {}
-    traffic = prof.get("dram_bytes_per_launch_scaled_to_bench")
-    value = world * args.steps / elapsed
+    prof = committed_profile(f"flux_edge_{args.precision}_{inc}.json") or {}
+    traffic = prof.get("dram_bytes_per_launch_scaled_to_bench") if args.n == 200 else None
+    fp64_roof = None
+    if prof.get("fp64"):
+        # The FP64 flux sweep is bound by FP64 issue, not HBM: the same launch
+        # against the measured FP64 FMA rate.
+        f = prof["fp64"]
+        ach = f["ops_per_edge"] * E / (flux_ms * 1e-3) / 1e9
+        fp64_roof = {"bound": "fp64", "achieved": round(ach, 1), "peak": f["peak_gops"], "unit": "G FP64 op/s",
+                     "frac": round(ach / f["peak_gops"], 4), "ops_per_edge": f["ops_per_edge"],
+                     "peak_source": f["peak_source"], "ncu_fp64_pipe_busy": f["pipe_busy_ncu"]}
     line = {
         "metric": "MG V-cycles/s at 8M nodes (200^3, 4 levels)",
         "value": round(value, 3),
@@ -229,19 +251,22 @@ def run_gb300(args):
         "data": "synthetic: seeded jittered 200^3 lattice, permuted ids",
         "config": {"workload": f"{args.n}^3 jittered lattice, {NLEVELS} levels, Mach {MACH}, AoA {AOA} deg, "
                                f"{N} nodes / {E} edges on level 0",
-                   "precision": args.precision, "increment": args.increment, "renumber": args.renumber,
+                   "precision": args.precision, "increment": inc, "renumber": args.renumber,
+                   "accumulation": args.accumulation if args.precision == "mixed" else "fp64",
                    "l2": "inputs larger than L2 (level-0 state and edges ~2.4 GB), no flush",
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
-                     "kernel": "k_flux (level-0 edge flux sweep)", "flux_ms_per_launch": round(flux_ms, 4),
+                     "kernel": ("k_update fused stage (level-0 edge fluxes + time step)" if inc == "fused"
+                                else "k_flux (level-0 edge flux sweep)"), "flux_ms_per_launch": round(flux_ms, 4),
                      "algorithmic_bytes_per_launch": bytes_per_sweep, "peak_source": peak_kind,
-                     "fp64": prof.get("fp64")},
-        "e2e": {"value": round(world * e2e_steps * E2E_CYCLES / e2e_elapsed, 3), "unit": "cycles/s",
+                     "fp64": fp64_roof},
+        "e2e": {"value": round(e2e_value, 3), "unit": "cycles/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "step": f"mgcfd_solve: upload mesh, setup, {E2E_CYCLES} V-cycles, download all levels",
                 "steps": e2e_steps},
         "gpu_launches": launches,
+        "precision_error": precision_error,
         "clocks": clocks.summary(),
         "cpu_baseline": cpu,
     }
@@ -259,13 +284,18 @@ def cpu_baseline(levels, cycles):
     run = O.OracleRun(levels)
     run.run(MACH, AOA, 1, nthreads=threads)  # warm-up: colouring, page faults
     st, secs = run.run(MACH, AOA, cycles, nthreads=threads)
+    # The sequential form (the reference's OP2 seq order, one core), one V-cycle.
+    st1, secs1 = run.run(MACH, AOA, 1, nthreads=1)
     run.close()
     return {"value": round(cycles / secs, 4), "unit": "cycles/s", "cores": threads, "kind": "port",
-            "sample": f"{cycles} V-cycles of the same 8M-node 4-level mesh, OpenMP over coloured edges"}
+            "sample": f"{cycles} V-cycles of the same 8M-node 4-level mesh, OpenMP over coloured edges",
+            "seq_1core": {"value": round(1.0 / secs1, 4), "unit": "cycles/s", "cores": 1,
+                          "sample": "1 V-cycle, sequential edge order"}}
 
 
 def run_reference(args):
-    world, rank, local = dist_setup()
+    from mgcfd import replicas
+    world, rank, local = replicas.world()
     if rank != 0:
         return
     import mgcfd
@@ -358,6 +388,14 @@ def run_batch(args):
         line[f"batched_{prec}_tuning"] = {"chosen": best, "ms_per_cycle": {f"{k[0]}/{k[1]}": round(v, 3)
                                                                            for k, v in timings.items()},
                                           "tuning_s": round(t_tune, 3), "max_rel_err_vs_fp64_sequential": err}
+        if prec == "mixed":  # the same batch with compensated FP32-pair node sums
+            pair = dict(best, accumulation="pair32")
+            solve_batch(**pair)
+            t0 = time.perf_counter()
+            outs = solve_batch(**pair)
+            results["batched_mixed_pair32"] = nm / (time.perf_counter() - t0)
+            line["batched_mixed_pair32_max_rel_err_vs_fp64_sequential"] = max(
+                float(np.max(np.abs(a - b) / np.maximum(np.abs(b).max(axis=0), 1e-300))) for a, b in zip(outs, seq))
     line["value"] = round(results["batched_fp64"], 3)
     line["results_solves_per_s"] = {k: round(v, 3) for k, v in results.items()}
     line["speedup_batched_fp64_vs_sequential"] = round(results["batched_fp64"] / results["sequential_fp64"], 3)
@@ -366,11 +404,17 @@ def run_batch(args):
 
 
 def run_serve(args):
-    """Serving: a Poisson stream of requests (node count log-uniform in
-    20K..4M, Mach U(0.3, 0.85), AoA U(0, 6) degrees, 3 or 4 levels, until the
-    level-0 density residual falls to 1e-6 of its first value or 50 V-cycles)
-    served under a 150 GB HBM budget; p50/p99 latency and solves/s for the
-    mixed-precision and FP64 forms on the same stream and arrival rates."""
+    """Serving: a Poisson stream of requests, each a seeded lattice mesh with
+    node count log-uniform in 20K..4M (a pool of distinct meshes drawn per
+    request), Mach U(0.3, 0.85), AoA U(0, 6) degrees, 3 or 4 levels, run until
+    the level-0 density residual falls to 1e-6 of its first value or 50
+    V-cycles, under a 150 GB HBM budget.  Three forms serve the same stream:
+      plain_fp64    one FP64 solve at a time (the plain path),
+      served_fp64   FP64, up to --serve-slots requests overlapping,
+      served_mixed  mixed precision, up to --serve-slots requests overlapping.
+    Capacity is solves/s with every request queued at once; then each form
+    serves Poisson arrivals at rates that are multiples of the plain path's
+    capacity, reporting p50/p99 latency (submit to result) and solves/s."""
     import threading
 
     import numpy as np
@@ -387,20 +431,26 @@ def run_serve(args):
     machs = rng.uniform(0.3, 0.85, R)
     aoas = rng.uniform(0.0, 6.0, R)
     gaps = rng.exponential(1.0, R)  # unit-rate inter-arrival times, scaled per rate
+    # plain_fp64 is the plain path: one FP64 solve at a time, each uploading and
+    # setting up its mesh.  The served forms overlap requests and keep meshes
+    # resident between requests (same pool mesh = same mesh key).
+    forms = {"plain_fp64": dict(max_active=1, precision="fp64"),
+             "served_fp64": dict(max_active=args.serve_slots, precision="fp64"),
+             "served_mixed": dict(max_active=args.serve_slots, precision="mixed"),
+             "served_mixed_pair32": dict(max_active=args.serve_slots, precision="mixed", accumulation="pair32")}
+    resident = {"plain_fp64": False, "served_fp64": True, "served_mixed": True, "served_mixed_pair32": True}
 
-    def serve(precision, rate):
-        srv = mgcfd.Server(hbm_budget_gb=150.0, max_active=args.serve_slots, precision=precision,
-                           increment="gather" if precision == "mixed" else "atomic", max_cycles=50,
-                           residual_drop=1e-6)
+    def serve(form, rate):
+        srv = mgcfd.Server(hbm_budget_gb=150.0, max_cycles=50, residual_drop=1e-6, **forms[form])
         t_start = time.perf_counter()
-        arrivals = np.cumsum(gaps / rate)
+        arrivals = np.cumsum(gaps / rate) if rate else np.zeros(R)
 
         def feeder():
             for k in range(R):
                 delay = t_start + arrivals[k] - time.perf_counter()
                 if delay > 0:
                     time.sleep(delay)
-                srv.submit(pool[picks[k]], float(machs[k]), float(aoas[k]))
+                srv.submit(pool[picks[k]], float(machs[k]), float(aoas[k]), resident=resident[form])
 
         th = threading.Thread(target=feeder)
         th.start()
@@ -412,24 +462,50 @@ def run_serve(args):
         srv.close()
         lat = np.array([r["finish_s"] - r["submit_s"] for r in res])
         ok = sum(1 for r in res if r["status"] == 0)
-        return {"rate_per_s": rate, "solves_per_s": round(len(res) / (t_end - t_start), 3),
+        return {"rate_per_s": round(rate, 3) if rate else "all at once",
+                "solves_per_s": round(len(res) / (t_end - t_start), 3),
                 "p50_ms": round(1e3 * float(np.percentile(lat, 50)), 2),
                 "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 2), "ok": ok, "failed": len(res) - ok,
                 "mean_cycles": round(float(np.mean([r["cycles"] for r in res])), 2),
-                "peak_active": int(st["peak_active"]), "peak_budget_gb": round(st["peak_bytes"] / 2 ** 30, 2)}
+                "peak_active": int(st["peak_active"]), "peak_budget_gb": round(st["peak_bytes"] / 2 ** 30, 2),
+                "resident_mesh_hits": int(st["cache_hits"])}
 
-    # Capacity probe: everything at once, FP64.
-    cap = serve("fp64", 1e9)["solves_per_s"]
-    rates = [round(f * cap, 3) for f in (0.5, 0.9, 1.5)]
-    out = {"fp64": [serve("fp64", r) for r in rates], "mixed": [serve("mixed", r) for r in rates]}
-    line = {"metric": "served solves/s and p50/p99 latency (Poisson stream)", "unit": "solves/s",
-            "higher_is_better": True, "n_gpus": 1, "data": "synthetic: seeded lattices",
+    serve("served_mixed", 0)  # warm-up: CUDA context, memory pool, module load
+    capacity = {f: serve(f, 0) for f in forms}
+    plain_cap = capacity["plain_fp64"]["solves_per_s"]
+    rates = [f * plain_cap for f in args.serve_rate_multiples]
+    sweep = {f: [serve(f, r) for r in rates] for f in forms}
+    cap = {f: capacity[f]["solves_per_s"] for f in forms}
+    line = {"metric": "served solves/s and p50/p99 latency (Poisson stream), vs the plain FP64 path",
+            "unit": "solves/s", "higher_is_better": True, "n_gpus": 1,
+            "data": "synthetic: seeded jittered lattices",
             "config": {"workload": f"{R} requests over a pool of {len(pool)} meshes "
                                    f"({min(m.level(0).nnodes for m in pool)}..{max(m.level(0).nnodes for m in pool)} "
-                                   "nodes, 3-4 levels), HBM budget 150 GB", "slots": args.serve_slots,
-                       "fp64_capacity_solves_per_s": cap},
-            "value": max(x["solves_per_s"] for x in out["mixed"]), "by_precision": out}
+                                   "level-0 nodes, 3-4 levels), 50 V-cycles or residual drop 1e-6, "
+                                   "HBM budget 150 GB",
+                       "slots": args.serve_slots, "rate_multiples_of_plain_capacity": args.serve_rate_multiples},
+            "value": cap["served_mixed"], "capacity_solves_per_s": cap,
+            "speedup_served_mixed_vs_plain_fp64": round(cap["served_mixed"] / cap["plain_fp64"], 3),
+            "speedup_served_mixed_pair32_vs_plain_fp64": round(cap["served_mixed_pair32"] / cap["plain_fp64"], 3),
+            "speedup_served_fp64_vs_plain_fp64": round(cap["served_fp64"] / cap["plain_fp64"], 3),
+            "capacity_runs": capacity, "sweep": sweep}
     print(json.dumps(line), flush=True)
+
+
+def run_rates(args):
+    """Issue rates of the arithmetic the kernels are built from (FP64/FP32
+    FMA, reciprocal, square root, rsqrt, format conversions, FP64 atomics,
+    device copy), measured on this GPU: the denominators of the FP64 cost
+    model the kernels are designed against."""
+    from mgcfd import _build
+    src = _build.CSRC / "probes" / "fp64_rates.cu"
+    exe = _build.OBJ / "fp64_rates"
+    exe.parent.mkdir(parents=True, exist_ok=True)
+    subprocess.run([_build._nvcc(), *_build.ARCH, "-O3", "-std=c++17", f"-I{_build.CSRC}", str(src), "-o", str(exe)],
+                   check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    d = json.loads(out)
+    print(json.dumps({"metric": "arithmetic issue rates", "unit": "G/s", "n_gpus": 1, "rates": d}), flush=True)
 
 
 def main():
@@ -439,16 +515,20 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
-    ap.add_argument("--increment", default="atomic", choices=["atomic", "gather"])
+    ap.add_argument("--increment", default="auto", choices=["auto", "atomic", "gather", "fused"],
+                    help="auto: FP64 atomics for fp64, the fused node-centric stage for mixed")
     ap.add_argument("--renumber", default="spatial", choices=["none", "spatial", "rcm"])
+    ap.add_argument("--accumulation", default="fp64", choices=["fp64", "pair32"],
+                    help="mixed precision node sums: FP64 adds, or compensated FP32 pairs")
     ap.add_argument("--n", type=int, default=200)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-cycles", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--mode", default="plain", choices=["plain", "batch", "serve"])
+    ap.add_argument("--mode", default="plain", choices=["plain", "batch", "serve", "rates"])
     ap.add_argument("--batch-meshes", type=int, default=64)
     ap.add_argument("--serve-requests", type=int, default=200)
-    ap.add_argument("--serve-pool", type=int, default=16)
+    ap.add_argument("--serve-pool", type=int, default=24)
+    ap.add_argument("--serve-rate-multiples", type=float, nargs="+", default=[0.5, 0.9, 2.0])
     ap.add_argument("--serve-slots", type=int, default=16)
     args = ap.parse_args()
     if args.warmup < 0 or args.steps < 1:
@@ -459,6 +539,8 @@ def main():
         run_batch(args)
     elif args.mode == "serve":
         run_serve(args)
+    elif args.mode == "rates":
+        run_rates(args)
     else:
         run_gb300(args)
 

@@ -229,8 +229,21 @@ int mgcfd_op_count_differences(int32_t nnodes, const double* test, const double*
 /* ------------------------------------------------------------------------ */
 /* Device-resident multigrid solver.                                        */
 enum { MGCFD_PRECISION_FP64 = 0, MGCFD_PRECISION_MIXED = 1 };
-enum { MGCFD_INCREMENT_AUTO = 0, MGCFD_INCREMENT_ATOMIC = 1, MGCFD_INCREMENT_GATHER = 2 };
+/* How the edge fluxes reach the nodes.  ATOMIC: each edge adds +f / -f to its
+ * end nodes with FP64 atomics.  GATHER: each edge stores f, then each node
+ * sums its edges' f in a fixed order (deterministic).  FUSED (mixed precision
+ * only): one node-centric kernel per RK stage computes the FP32 flux of every
+ * edge at both of its end nodes from the same inputs in the same order, sums
+ * them exactly as GATHER does and applies the time step -- GATHER's results
+ * bit for bit, with no per-edge flux array and one launch per stage. */
+enum { MGCFD_INCREMENT_AUTO = 0, MGCFD_INCREMENT_ATOMIC = 1, MGCFD_INCREMENT_GATHER = 2, MGCFD_INCREMENT_FUSED = 3 };
 enum { MGCFD_RENUMBER_NONE = 0, MGCFD_RENUMBER_SPATIAL = 1, MGCFD_RENUMBER_RCM = 2 };
+/* Node-residual accumulation in mixed precision.  FP64: every FP32 edge flux
+ * is widened exactly and added in FP64.  PAIR32: the fluxes enter an
+ * unevaluated FP32 pair (hi, lo) through error-free TwoSum steps (Knuth,
+ * TAOCP vol. 2, 4.2.2) and the pair is added once in FP64 -- within 2^-48 of
+ * the exact sum, and no FP64 add per edge. */
+enum { MGCFD_ACCUM_FP64 = 0, MGCFD_ACCUM_PAIR32 = 1 };
 enum {
   MGCFD_Q_VARIABLES = 0,    /* [N][5] */
   MGCFD_Q_FLUXES = 1,       /* [N][5] */
@@ -242,8 +255,8 @@ enum {
 
 typedef struct mgcfd_solver_options {
   int32_t precision;         /* MGCFD_PRECISION_*                                   */
-  int32_t increment;         /* MGCFD_INCREMENT_*; AUTO = ATOMIC for FP64 and GATHER
-                                for MIXED (the faster of the two on GB300)         */
+  int32_t increment;         /* MGCFD_INCREMENT_*; AUTO = ATOMIC for FP64 and FUSED
+                                for MIXED (the fastest of each on GB300)           */
   int32_t renumber;          /* MGCFD_RENUMBER_*                                    */
   int32_t use_graph;         /* capture one V-cycle as a CUDA graph and replay it  */
   int32_t measure_mem_bound; /* also run unstructured_stream each RK stage (-b)   */
@@ -251,7 +264,9 @@ typedef struct mgcfd_solver_options {
   int32_t time_kernels;      /* record CUDA events around level-0 flux sweeps      */
   int32_t host_setup;        /* build the mesh tables on the host instead of the GPU
                                 (always on for MGCFD_RENUMBER_RCM); same results      */
-  int32_t reserved[8];
+  int32_t accumulation;      /* MGCFD_ACCUM_*: how mixed precision sums the FP32
+                                edge fluxes of a node (gather increment only)      */
+  int32_t reserved[7];
 } mgcfd_solver_options;
 
 typedef struct mgcfd_solver_stats {
@@ -352,7 +367,8 @@ typedef struct mgcfd_server_options {
   int32_t increment;         /* MGCFD_INCREMENT_*                                  */
   int32_t max_cycles;        /* V-cycles per request at most                       */
   double residual_drop;      /* stop when rho_rms <= residual_drop * first rho_rms */
-  int32_t reserved[8];
+  int32_t accumulation;      /* MGCFD_ACCUM_* for mixed precision                 */
+  int32_t reserved[7];
 } mgcfd_server_options;
 
 typedef struct mgcfd_request_result {
@@ -367,8 +383,10 @@ typedef struct mgcfd_request_result {
 typedef struct mgcfd_server_stats {
   int64_t submitted, completed, failed;
   int64_t active, pending;
-  int64_t used_bytes, peak_bytes, peak_active;
-  int64_t reserved[4];
+  int64_t used_bytes, peak_bytes, peak_active;  /* used_bytes includes idle cached solvers */
+  int64_t cache_hits;                           /* requests that reused a resident mesh   */
+  int64_t cached_solvers;                       /* idle solvers held for reuse            */
+  int64_t reserved[2];
 } mgcfd_server_stats;
 
 typedef struct mgcfd_server mgcfd_server;
@@ -377,9 +395,11 @@ void mgcfd_server_default_options(mgcfd_server_options* opt);
 int mgcfd_server_create(const mgcfd_server_options* opt, mgcfd_server** out);
 /* Queue a solve.  The level arrays must stay valid until the request has
  * completed; out_variables_l0 (may be NULL) receives the final level-0
- * variables [N0][5] in input order. */
+ * variables [N0][5] in input order.  mesh_key != 0 names the mesh: requests
+ * with the same key reuse its resident device tables (the caller guarantees
+ * the arrays are the same mesh); 0 uploads and sets up the mesh afresh. */
 int mgcfd_server_submit(mgcfd_server* server, int32_t nlevels, const mgcfd_level_view* levels, double mach,
-                        double aoa_deg, double* out_variables_l0, int64_t* id);
+                        double aoa_deg, int64_t mesh_key, double* out_variables_l0, int64_t* id);
 /* Move up to `capacity` completed results into out; *count receives how many. */
 int mgcfd_server_poll(mgcfd_server* server, mgcfd_request_result* out, int32_t capacity, int32_t* count);
 /* Wait until no request is queued or running (MGCFD_ERR_TIMEOUT after timeout_s). */

@@ -81,9 +81,14 @@ __device__ __forceinline__ void edge_flux(const NodePrim& a, const NodePrim& b, 
   f[4] = fac * (a.rhoE - b.rhoE) + ((a.rhoE + a.p) * uha + (b.rhoE + b.p) * uhb);
 }
 
-// -x by flipping the sign bit with an integer operation.
+// -x by flipping the sign bit of the high word with an integer instruction.
+// Written as inline PTX so the compiler cannot turn it back into a
+// floating-point negation, which would issue on the FP64 pipe.
 __device__ __forceinline__ double negate(double x) {
-  return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ull);
+  int hi = __double2hiint(x);
+  const int lo = __double2loint(x);
+  asm("xor.b32 %0, %0, 0x80000000;" : "+r"(hi));
+  return __hiloint2double(hi, lo);
 }
 
 // flux_wall.elem_func:49-76 (far field, groups 3..7) for one boundary entry:
@@ -173,6 +178,41 @@ __device__ __forceinline__ double dkey_inv(unsigned long long k) {
   if (k == ~0ull) return 1.7976931348623157e308;  // nothing reduced yet: DBL_MAX
   unsigned long long u = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
   return __longlong_as_double((long long)u);
+}
+
+// hi + lo += x with Knuth's error-free TwoSum (TAOCP vol. 2, 4.2.2,
+// theorem B): s = hi + x exactly equals s + e, and e joins lo.  Plain FP32
+// adds (no contraction or reassociation applies to adds).
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
+  const float s = hi + x;
+  const float bb = s - hi;
+  const float e = (hi - (s - bb)) + (x - bb);
+  hi = s;
+  lo += e;
+}
+
+// Key of a dt value for the min_dt reduction, or ~0 when the value takes no
+// part: get_min_dt_kernel (time_stepping_kernels.h:34-41) keeps its DBL_MAX
+// start unless dt < it, so NaN, +inf and DBL_MAX itself never win.  Integer
+// operations only.
+__device__ __forceinline__ unsigned long long dt_candidate_key(double dt) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(dt);
+  const unsigned long long k = dkey(dt);
+  const bool nan = (b & 0x7fffffffffffffffull) > 0x7ff0000000000000ull;
+  return (!nan && k < 0xffefffffffffffffull) ? k : ~0ull;  // 0xffef.. = dkey(DBL_MAX)
+}
+
+// NaN or infinity, from the exponent field (count_bad_vals, validation.h:102-115).
+__device__ __forceinline__ bool not_finite(double x) {
+  return ((unsigned long long)__double_as_longlong(x) & 0x7ff0000000000000ull) == 0x7ff0000000000000ull;
+}
+
+__device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = w < v ? w : v;
+  }
+  return v;
 }
 
 __device__ __forceinline__ double warp_min(double v) {

@@ -552,7 +552,11 @@ int device_prepare(mgcfd_solver* s, const std::vector<MeshInput>& meshes) {
         (r = s->alloc(&D.res, 5 * (size_t)N)))
       return r;
     if (mixed && (r = s->alloc(&D.rec32, 8 * (size_t)N))) return r;
-    if (s->gather) { if ((r = s->alloc(&D.fe, 5 * (size_t)NE))) return r; }
+    if (s->fused) {
+      if ((r = build_fused_tables(s, D))) return r;
+    } else if (s->gather) {
+      if (mixed ? (r = s->alloc(&D.fe32, 5 * (size_t)NE)) : (r = s->alloc(&D.fe, 5 * (size_t)NE))) return r;
+    }
     else if ((r = s->alloc(&D.flux, 5 * (size_t)N))) return r;
     if (s->opt.measure_mem_bound && (r = s->alloc(&D.dummy, 5 * (size_t)N))) return r;
     CK(cudaGetLastError());

@@ -1,26 +1,45 @@
 // Serving loop: flow solves of different meshes and freestream conditions
 // arrive at any time and run concurrently on one GPU.
 //
-// A worker thread owns all GPU work.  Requests wait in a FIFO until a slot
-// (a CUDA stream) is free and the HBM budget admits their estimated footprint;
-// admission builds the request's device solver on its slot's stream.  Every
-// active request then advances one V-cycle at a time: the cycle (a CUDA graph
-// launch), an asynchronous copy of the solver's device status block to pinned
-// host memory and an event.  When the event has completed the worker reads the
-// level-0 density residual and decides: stop (converged, failed, or the cycle
-// limit reached: fetch the result, free the solver, release slot and budget)
-// or enqueue the next cycle.  Requests therefore join and leave at V-cycle
-// boundaries and their kernels overlap on the device (continuous batching at
-// V-cycle granularity).  Each request's arithmetic is exactly that of a solver
-// running alone, so with the deterministic gather increment a result is
-// bit-identical alone and in any mix.
+// Two host threads share the work:
+//   * the host-work thread admits requests and retires them.  Requests wait
+//     in a FIFO until a slot (a CUDA stream) is free and the HBM budget covers
+//     their estimated footprint; admission builds the request's device solver
+//     on its slot's stream (upload, device setup), installs the device-side
+//     stop rule and enqueues the first V-cycles.  Retirement copies the final
+//     level-0 state out, frees the solver and releases slot and budget.
+//   * the progress thread keeps every active request's stream fed.  Cycles
+//     are enqueued in chunks of kChunk V-cycles (CUDA graph launches), each
+//     followed by an asynchronous copy of the solver's status block to pinned
+//     memory and an event; up to kDepth chunks are in flight per request, so
+//     the stream never waits for the host between chunks.
+// The stop rule runs on the device at the end of every V-cycle (k_cycle_end):
+// it counts cycles, records the level-0 density residual norm and, once the
+// norm has dropped to residual_drop times the first cycle's or max_cycles is
+// reached, stops the solver's kernels, so cycles enqueued beyond that point
+// do no work and the solve ends exactly where a host-driven loop would have
+// stopped it.  min_dt < 0 and NaN/Inf stop it the same way with an error.
+//
+// Meshes stay resident: a request submitted with a nonzero mesh key leaves its
+// solver (mesh tables and state buffers) in an idle cache when it retires,
+// charged to the budget, and the next request with that key reuses it after
+// re-initialising state and far-field terms for its own freestream
+// (solver_retarget): no upload and no setup.  Idle solvers are evicted, least
+// recently used first, when a new mesh needs their budget.
+//
+// Requests therefore join and leave at V-cycle boundaries and their kernels
+// overlap on the device (continuous batching at V-cycle granularity).  Each
+// request's arithmetic is exactly that of a solver running alone, so with the
+// deterministic gather increment a result is bit-identical alone and in any
+// mix.
 #include <algorithm>
 #include <chrono>
-#include <memory>
 #include <cmath>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <list>
+#include <memory>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -32,8 +51,12 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
+constexpr int kChunk = 4;  // V-cycles per enqueued chunk
+constexpr int kDepth = 2;  // chunks in flight per request
+
 struct Request {
   int64_t id = 0;
+  int64_t key = 0;        // mesh key (0: no reuse)
   std::vector<mgcfd_level_view> levels;
   double mach = 0, aoa = 0;
   double* out = nullptr;  // level-0 variables [N0][5] on completion, may be NULL
@@ -41,8 +64,12 @@ struct Request {
   double t_submit = 0, t_admit = -1, t_finish = -1;
   mgcfd_solver* solver = nullptr;
   int slot = -1;
+  int enqueued = 0;      // V-cycles enqueued so far
+  int inflight = 0;      // chunks not yet seen complete
+  int next_buf = 0;      // status buffer of the next chunk
+  int oldest_buf = 0;    // status buffer of the oldest chunk in flight
+  bool ending = false;   // no more chunks: waiting for the ones in flight
   int cycles = 0;
-  bool inflight = false;
   double rho_first = -1, rho_last = -1;
   int status = MGCFD_OK;
 };
@@ -52,51 +79,71 @@ struct Request {
 struct mgcfd_server {
   mgcfd_server_options opt{};
   int device = 0;
-  std::thread worker;
+  std::thread host_worker, progress_worker;
   std::mutex mu;
   std::condition_variable cv;
   std::deque<Request*> pending;
   std::vector<Request*> active;
+  std::deque<Request*> retiring;
   std::vector<mgcfd_request_result> done;
+  struct Idle {
+    int64_t key;
+    mgcfd_solver* solver;
+    int64_t estimate;
+  };
+  std::list<Idle> idle_cache;  // front = most recently used
   bool stop = false;
+  int admitting = 0;  // requests between pending and active
+  int retiring_now = 0;  // requests taken for retirement whose record is not yet published
   int64_t next_id = 1;
   int64_t used = 0;
-  std::vector<cudaStream_t> streams;
-  std::vector<cudaEvent_t> events;
+  std::vector<cudaEvent_t> events;  // [slot][kDepth]
   std::vector<int> slot_free;
-  DevStatus* pinned = nullptr;  // one status block per slot
+  DevStatus* pinned = nullptr;      // [slot][kDepth] status blocks
   Clock::time_point t0;
   mgcfd_server_stats stats{};
-  std::string worker_error;
 
   double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
+  bool idle() const {
+    return pending.empty() && active.empty() && retiring.empty() && admitting == 0 && retiring_now == 0;
+  }
 };
 
 namespace {
 
 // Device bytes a request may need at its peak (setup scratch included).
 int64_t estimate_bytes(const std::vector<mgcfd_level_view>& lv, int precision, int increment) {
+  const bool mixed = precision == MGCFD_PRECISION_MIXED;
+  const bool fused = increment == MGCFD_INCREMENT_FUSED || (increment == MGCFD_INCREMENT_AUTO && mixed);
+  const bool gather = fused || increment == MGCFD_INCREMENT_GATHER;
   int64_t b = 1 << 20;
   for (const auto& v : lv) {
     const int64_t n = v.nnodes, e = v.nedges, nb = v.nbnd;
     int64_t node = 8 * 8 + 5 * 8 * 3 + 8 * 3 + 4 * 4 + 32;   // rec, old/res/flux, vol constants, maps, dvec
     int64_t edge = 8 + 32;                                    // e2n, w4
-    if (precision == MGCFD_PRECISION_MIXED) { node += 32; edge += 16; }
-    if (increment == MGCFD_INCREMENT_GATHER || (increment == MGCFD_INCREMENT_AUTO && precision == MGCFD_PRECISION_MIXED))
-      edge += 40 + 4;
+    if (mixed) { node += fused ? 64 : 32; edge += 16; }
+    if (gather) edge += (mixed ? 20 : 40) + 4;
     b += n * node + e * edge + nb * 96;
     b += n * 80 + e * 120 + nb * 64;                          // setup scratch (uploads, sort buffers)
   }
   return b;
 }
 
-void finish(mgcfd_server* S, Request* r) {
+// Host-work thread: copy the result out, free the solver, publish the record.
+void retire(mgcfd_server* S, Request* r) {
+  bool cached = false;
   if (r->solver) {
     if (r->out && r->status == MGCFD_OK) {
       int st = mgcfd_solver_fetch(r->solver, 0, MGCFD_Q_VARIABLES, r->out);
       if (st) r->status = st;
     }
-    mgcfd_solver_destroy(r->solver);
+    if (r->key != 0 && r->status == MGCFD_OK) {
+      std::lock_guard<std::mutex> lock(S->mu);
+      S->idle_cache.push_front({r->key, r->solver, r->estimate});
+      cached = true;
+    } else {
+      mgcfd_solver_destroy(r->solver);
+    }
     r->solver = nullptr;
   }
   r->t_finish = S->now();
@@ -112,116 +159,183 @@ void finish(mgcfd_server* S, Request* r) {
   res.rho_rms_last = r->rho_last;
   std::lock_guard<std::mutex> lock(S->mu);
   if (r->slot >= 0) S->slot_free[(size_t)r->slot] = 1;
-  S->used -= r->t_admit >= 0 ? r->estimate : 0;
+  if (!cached) S->used -= r->t_admit >= 0 ? r->estimate : 0;
   S->done.push_back(res);
   S->stats.completed++;
   if (r->status != MGCFD_OK) S->stats.failed++;
+  S->retiring_now--;
   S->cv.notify_all();
   delete r;
 }
 
-int enqueue_cycle(mgcfd_server* S, Request* r) {
-  int st = mgcfd_solver_run(r->solver, 1);
+// Enqueue the next chunk of V-cycles, then the status copy and its event.
+int enqueue_chunk(mgcfd_server* S, Request* r) {
+  const int n = std::min(kChunk, S->opt.max_cycles - r->enqueued);
+  int st = mgcfd_solver_run(r->solver, n);
   if (st) return st;
-  const cudaStream_t s = S->streams[(size_t)r->slot];
-  cudaError_t e = cudaMemcpyAsync(&S->pinned[r->slot], r->solver->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess) e = cudaEventRecord(S->events[(size_t)r->slot], s);
+  r->enqueued += n;
+  const size_t k = (size_t)r->slot * kDepth + (size_t)r->next_buf;
+  const cudaStream_t s = r->solver->stream;
+  cudaError_t e = cudaMemcpyAsync(&S->pinned[k], r->solver->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaEventRecord(S->events[k], s);
   if (e != cudaSuccess) return mgcfd::set_error(MGCFD_ERR_CUDA, std::string("server: ") + cudaGetErrorString(e));
-  r->inflight = true;
+  r->next_buf = (r->next_buf + 1) % kDepth;
+  r->inflight++;
   return MGCFD_OK;
 }
 
-void worker_main(mgcfd_server* S) {
+// Host-work thread: admission and retirement.
+void host_main(mgcfd_server* S) {
   cudaSetDevice(S->device);
   mgcfd_solver_options so;
   mgcfd_solver_default_options(&so);
   so.precision = S->opt.precision;
   so.increment = S->opt.increment;
+  so.accumulation = S->opt.accumulation;
   for (;;) {
-    // Admission.
-    for (;;) {
-      Request* r = nullptr;
-      {
-        std::unique_lock<std::mutex> lock(S->mu);
-        if (S->stop && S->pending.empty() && S->active.empty()) return;
-        if (S->pending.empty()) {
-          if (S->active.empty()) S->cv.wait_for(lock, std::chrono::milliseconds(2));
+    Request* r = nullptr;
+    bool admit = false;
+    mgcfd_solver* reuse = nullptr;        // an idle solver of this request's mesh
+    std::vector<mgcfd_solver*> victims;  // idle solvers evicted to make room
+    {
+      std::unique_lock<std::mutex> lock(S->mu);
+      for (;;) {
+        if (!S->retiring.empty()) {
+          r = S->retiring.front();
+          S->retiring.pop_front();
+          S->retiring_now++;
           break;
         }
-        Request* f = S->pending.front();
-        if (f->estimate > S->opt.hbm_budget_bytes) {  // can never fit
-          S->pending.pop_front();
-          f->status = MGCFD_ERR_BUDGET;
-          lock.unlock();
-          finish(S, f);
-          continue;
+        if (!S->pending.empty()) {
+          Request* f = S->pending.front();
+          if (f->estimate > S->opt.hbm_budget_bytes) {  // can never fit
+            S->pending.pop_front();
+            f->status = MGCFD_ERR_BUDGET;
+            S->retiring_now++;
+            r = f;
+            break;
+          }
+          int slot = -1;
+          for (size_t k = 0; k < S->slot_free.size(); k++)
+            if (S->slot_free[k]) { slot = (int)k; break; }
+          if (slot >= 0) {
+            auto hit = S->idle_cache.end();
+            if (f->key != 0)
+              for (auto it = S->idle_cache.begin(); it != S->idle_cache.end(); ++it)
+                if (it->key == f->key) { hit = it; break; }
+            bool fits = hit != S->idle_cache.end();
+            if (fits) {  // already charged to the budget
+              reuse = hit->solver;
+              f->estimate = hit->estimate;
+              S->idle_cache.erase(hit);
+              S->stats.cache_hits++;
+            } else {
+              // Evict least recently used idle solvers until the new mesh fits.
+              while (S->used + f->estimate > S->opt.hbm_budget_bytes && !S->idle_cache.empty()) {
+                victims.push_back(S->idle_cache.back().solver);
+                S->used -= S->idle_cache.back().estimate;
+                S->idle_cache.pop_back();
+              }
+              fits = S->used + f->estimate <= S->opt.hbm_budget_bytes;
+              if (fits) S->used += f->estimate;
+            }
+            if (fits) {
+              S->pending.pop_front();
+              S->slot_free[(size_t)slot] = 0;
+              S->stats.peak_bytes = std::max(S->stats.peak_bytes, S->used);
+              f->slot = slot;
+              f->t_admit = S->now();
+              S->admitting++;
+              r = f;
+              admit = true;
+              break;
+            }
+          }
         }
-        int slot = -1;
-        for (size_t k = 0; k < S->slot_free.size(); k++)
-          if (S->slot_free[k]) { slot = (int)k; break; }
-        if (slot < 0 || S->used + f->estimate > S->opt.hbm_budget_bytes) break;
-        S->pending.pop_front();
-        S->slot_free[(size_t)slot] = 0;
-        S->used += f->estimate;
-        S->stats.peak_bytes = std::max(S->stats.peak_bytes, S->used);
-        f->slot = slot;
-        f->t_admit = S->now();
-        S->active.push_back(f);
-        S->stats.peak_active = std::max<int64_t>(S->stats.peak_active, (int64_t)S->active.size());
-        r = f;
+        if (!victims.empty()) break;  // free them, then look again
+        if (S->stop && S->idle()) {
+          for (auto& c : S->idle_cache) mgcfd_solver_destroy(c.solver);
+          S->idle_cache.clear();
+          return;
+        }
+        S->cv.wait(lock);
       }
-      int st = mgcfd_solver_create((int32_t)r->levels.size(), r->levels.data(), r->mach, r->aoa, &so,
-                                   S->streams[(size_t)r->slot], &r->solver);
-      if (st == MGCFD_OK) st = enqueue_cycle(S, r);
-      if (st) {
-        r->status = st;
-        std::lock_guard<std::mutex> lock(S->mu);
-        S->active.erase(std::find(S->active.begin(), S->active.end(), r));
-      }
-      if (st) finish(S, r);
     }
-    // Progress.
-    std::vector<Request*> act;
+    for (mgcfd_solver* v : victims) mgcfd_solver_destroy(v);
+    if (!r) continue;
+    if (!admit) {
+      retire(S, r);
+      continue;
+    }
+    int st;
+    if (reuse) {
+      r->solver = reuse;
+      st = mgcfd::solver_retarget(reuse, r->mach, r->aoa);
+    } else {
+      st = mgcfd_solver_create((int32_t)r->levels.size(), r->levels.data(), r->mach, r->aoa, &so, nullptr, &r->solver);
+      if (st == MGCFD_OK) st = mgcfd::solver_set_stop_rule(r->solver, S->opt.max_cycles, S->opt.residual_drop);
+    }
+    for (int c = 0; st == MGCFD_OK && c < kDepth && r->enqueued < S->opt.max_cycles; c++) st = enqueue_chunk(S, r);
     {
       std::lock_guard<std::mutex> lock(S->mu);
+      S->admitting--;
+      if (st == MGCFD_OK) {
+        S->active.push_back(r);
+        S->stats.peak_active = std::max<int64_t>(S->stats.peak_active, (int64_t)S->active.size());
+        S->cv.notify_all();
+        continue;
+      }
+      S->retiring_now++;
+    }
+    if (r->solver) cudaStreamSynchronize(r->solver->stream);
+    r->status = st;
+    retire(S, r);
+  }
+}
+
+// Progress thread: completes chunks and enqueues the next ones.
+void progress_main(mgcfd_server* S) {
+  cudaSetDevice(S->device);
+  std::vector<Request*> act;
+  for (;;) {
+    {
+      std::unique_lock<std::mutex> lock(S->mu);
+      if (S->active.empty()) {
+        if (S->stop && S->idle()) return;
+        S->cv.wait_for(lock, std::chrono::milliseconds(2));
+        continue;
+      }
       act = S->active;
     }
     bool progressed = false;
     for (Request* r : act) {
-      if (!r->inflight) continue;
-      cudaError_t q = cudaEventQuery(S->events[(size_t)r->slot]);
+      const size_t k = (size_t)r->slot * kDepth + (size_t)r->oldest_buf;
+      const cudaError_t q = cudaEventQuery(S->events[k]);
       if (q == cudaErrorNotReady) continue;
       progressed = true;
-      r->inflight = false;
-      r->cycles++;
-      bool stop = false;
+      r->inflight--;
+      r->oldest_buf = (r->oldest_buf + 1) % kDepth;
       if (q != cudaSuccess) {
         r->status = mgcfd::set_error(MGCFD_ERR_CUDA, std::string("server: ") + cudaGetErrorString(q));
-        stop = true;
+        r->ending = true;
       } else {
-        const DevStatus& h = S->pinned[r->slot];
-        const double n0 = (double)r->levels[0].nnodes;
-        const double rho = std::sqrt(h.rho_acc / n0);
-        if (r->rho_first < 0) r->rho_first = rho;
-        r->rho_last = rho;
+        const DevStatus& h = S->pinned[k];
+        r->cycles = h.cycles_done;
+        if (h.cycles_done > 0) { r->rho_first = h.rho_first; r->rho_last = h.rho_last; }
         if (h.halt) {
-          r->status = h.neg_dt ? MGCFD_ERR_NEGATIVE_DT : MGCFD_ERR_BAD_VALUES;
-          stop = true;
-        } else if (r->cycles >= S->opt.max_cycles ||
-                   (S->opt.residual_drop > 0 && r->cycles > 1 && rho <= S->opt.residual_drop * r->rho_first)) {
-          stop = true;
+          if (!h.stopped && r->status == MGCFD_OK) r->status = h.neg_dt ? MGCFD_ERR_NEGATIVE_DT : MGCFD_ERR_BAD_VALUES;
+          r->ending = true;
         }
       }
-      if (!stop) {
-        int st = enqueue_cycle(S, r);
-        if (st) { r->status = st; stop = true; }
+      if (!r->ending && r->enqueued < S->opt.max_cycles) {
+        const int st = enqueue_chunk(S, r);
+        if (st) { r->status = st; r->ending = true; }
       }
-      if (stop) {
-        {
-          std::lock_guard<std::mutex> lock(S->mu);
-          S->active.erase(std::find(S->active.begin(), S->active.end(), r));
-        }
-        finish(S, r);
+      if (r->inflight == 0) {  // nothing left on the device for this request
+        std::lock_guard<std::mutex> lock(S->mu);
+        S->active.erase(std::find(S->active.begin(), S->active.end(), r));
+        S->retiring.push_back(r);
+        S->cv.notify_all();
       }
     }
     if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(20));
@@ -247,27 +361,25 @@ extern "C" int mgcfd_server_create(const mgcfd_server_options* opt, mgcfd_server
   std::unique_ptr<mgcfd_server> S(new (std::nothrow) mgcfd_server());
   if (!S) return mgcfd::set_error(MGCFD_ERR_NOMEM, "host allocation failed");
   if (opt) S->opt = *opt; else mgcfd_server_default_options(&S->opt);
-  if (S->opt.max_active < 1 || S->opt.max_active > 1024 || S->opt.max_cycles < 1 || S->opt.hbm_budget_bytes <= 0)
+  if (S->opt.max_active < 1 || S->opt.max_active > 1024 || S->opt.max_cycles < 1 || S->opt.hbm_budget_bytes <= 0 ||
+      (S->opt.precision != MGCFD_PRECISION_FP64 && S->opt.precision != MGCFD_PRECISION_MIXED))
     return mgcfd::set_error(MGCFD_ERR_INVALID, "mgcfd_server_create: bad options");
   CK(cudaGetDevice(&S->device));
   const int k = S->opt.max_active;
-  S->streams.resize((size_t)k);
-  S->events.resize((size_t)k);
+  S->events.resize((size_t)k * kDepth);
   S->slot_free.assign((size_t)k, 1);
-  for (int i = 0; i < k; i++) {
-    CK(cudaStreamCreateWithFlags(&S->streams[(size_t)i], cudaStreamNonBlocking));
-    CK(cudaEventCreateWithFlags(&S->events[(size_t)i], cudaEventDisableTiming));
-  }
-  CK(cudaMallocHost(reinterpret_cast<void**>(&S->pinned), sizeof(DevStatus) * (size_t)k));
+  for (auto& ev : S->events) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  CK(cudaMallocHost(reinterpret_cast<void**>(&S->pinned), sizeof(DevStatus) * (size_t)k * kDepth));
   S->t0 = Clock::now();
   mgcfd_server* raw = S.get();
-  S->worker = std::thread(worker_main, raw);
+  S->host_worker = std::thread(host_main, raw);
+  S->progress_worker = std::thread(progress_main, raw);
   *out = S.release();
   return MGCFD_OK;
 }
 
 extern "C" int mgcfd_server_submit(mgcfd_server* S, int32_t nlevels, const mgcfd_level_view* levels, double mach,
-                                   double aoa_deg, double* out_variables_l0, int64_t* id) {
+                                   double aoa_deg, int64_t mesh_key, double* out_variables_l0, int64_t* id) {
   if (!S || !levels || nlevels < 1 || nlevels > kMaxLevels)
     return mgcfd::set_error(MGCFD_ERR_INVALID, "mgcfd_server_submit: bad arguments");
   Request* r = new (std::nothrow) Request();
@@ -276,6 +388,7 @@ extern "C" int mgcfd_server_submit(mgcfd_server* S, int32_t nlevels, const mgcfd
   r->mach = mach;
   r->aoa = aoa_deg;
   r->out = out_variables_l0;
+  r->key = mesh_key;
   r->estimate = estimate_bytes(r->levels, S->opt.precision, S->opt.increment);
   std::lock_guard<std::mutex> lock(S->mu);
   r->id = S->next_id++;
@@ -308,7 +421,7 @@ extern "C" int mgcfd_server_drain(mgcfd_server* S, double timeout_s) {
   if (!S) return mgcfd::set_error(MGCFD_ERR_INVALID, "null server");
   std::unique_lock<std::mutex> lock(S->mu);
   const auto deadline = Clock::now() + std::chrono::duration<double>(timeout_s);
-  while (!(S->pending.empty() && S->active.empty())) {
+  while (!S->idle()) {
     if (S->cv.wait_until(lock, deadline) == std::cv_status::timeout && Clock::now() >= deadline)
       return mgcfd::set_error(MGCFD_ERR_TIMEOUT, "mgcfd_server_drain: requests still running");
   }
@@ -320,8 +433,9 @@ extern "C" int mgcfd_server_get_stats(mgcfd_server* S, mgcfd_server_stats* out) 
   std::lock_guard<std::mutex> lock(S->mu);
   *out = S->stats;
   out->used_bytes = S->used;
-  out->active = (int64_t)S->active.size();
+  out->active = (int64_t)S->active.size() + S->admitting;
   out->pending = (int64_t)S->pending.size();
+  out->cached_solvers = (int64_t)S->idle_cache.size();
   return MGCFD_OK;
 }
 
@@ -332,8 +446,8 @@ extern "C" void mgcfd_server_destroy(mgcfd_server* S) {
     S->stop = true;
     S->cv.notify_all();
   }
-  if (S->worker.joinable()) S->worker.join();
-  for (auto st : S->streams) cudaStreamDestroy(st);
+  if (S->host_worker.joinable()) S->host_worker.join();
+  if (S->progress_worker.joinable()) S->progress_worker.join();
   for (auto ev : S->events) cudaEventDestroy(ev);
   if (S->pinned) cudaFreeHost(S->pinned);
   delete S;

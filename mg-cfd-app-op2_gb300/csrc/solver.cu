@@ -9,7 +9,8 @@
 //   old, res, flux [N][5] f64; inv_vol, cbrt_vol, vol [N] f64
 //   e2n    [E]     int2 (a < b, sorted by a then b); w4 [E] double4
 //                       (-wx/2, -wy/2, -wz/2, -|w|*smoothing*0.5) or float4 (mixed)
-//   fe     [E][5]  f64  per-edge fluxes (gather increment strategy only)
+//   fe     [E][5]  f64  per-edge fluxes (gather increment strategy only;
+//                       f32 fe32 in mixed precision)
 //   bidx [N] int32 and bdata [NB][12] f64: boundary entries folded per node
 //   n2mg [N], dvec [N] double4: prolongation parent and |dx|,|dy|,|dz|,dist
 //   ch_off/ch_list: restriction children of each coarse node
@@ -47,10 +48,6 @@ namespace {
 
 constexpr int kNodeThreads = 128;
 
-
-
-
-
 // ---------------------------------------------------------------------------
 // Kernels.
 
@@ -73,24 +70,29 @@ struct NodePrimF {
   float rho, mx, my, mz, rhoE, p, s, rinv;
 };
 
-__device__ __forceinline__ void store_rec32(float* rec32, int64_t i, const NodePrim& p) {
-  float4* r = reinterpret_cast<float4*>(rec32 + 8 * i);
-  r[0] = make_float4((float)p.rho, (float)p.mx, (float)p.my, (float)p.mz);
-  r[1] = make_float4((float)p.rhoE, (float)p.p, (float)p.s, (float)p.rinv);
-}
-
-// Mixed precision: FP32 primitives straight from the FP64 state.
-__device__ __forceinline__ void store_rec32_from_var(float* rec32, int64_t i, double rho, double mx, double my,
-                                                     double mz, double rhoE) {
-  const float r = (float)rho, x = (float)mx, y = (float)my, z = (float)mz, e = (float)rhoE;
+// Mixed precision: FP32 primitives of an FP32 state.
+__device__ __forceinline__ NodePrimF prim32(float r, float x, float y, float z, float e) {
   const float rinv = 1.0f / r;
   const float ux = x * rinv, uy = y * rinv, uz = z * rinv;
   const float q2 = ux * ux + uy * uy + uz * uz;
   const float p = 0.4f * (e - 0.5f * r * q2);
-  const float s = sqrtf(q2) + sqrtf(1.4f * p * rinv);
+  const float sp = sqrtf(q2) + sqrtf(1.4f * p * rinv);
+  return NodePrimF{r, x, y, z, e, p, sp, rinv};
+}
+
+__device__ __forceinline__ void store_prim32(float* rec32, int64_t i, const NodePrimF& q) {
   float4* o = reinterpret_cast<float4*>(rec32 + 8 * i);
-  o[0] = make_float4(r, x, y, z);
-  o[1] = make_float4(e, p, s, rinv);
+  o[0] = make_float4(q.rho, q.mx, q.my, q.mz);
+  o[1] = make_float4(q.rhoE, q.p, q.s, q.rinv);
+}
+
+// FP32 primitives straight from the FP64 state; the narrowing runs on the
+// integer pipe (d2f_bits), so this issues no FP64 instruction.
+__device__ __forceinline__ NodePrimF store_rec32_from_var(float* rec32, int64_t i, double rho, double mx, double my,
+                                                          double mz, double rhoE) {
+  const NodePrimF q = prim32(d2f_bits(rho), d2f_bits(mx), d2f_bits(my), d2f_bits(mz), d2f_bits(rhoE));
+  store_prim32(rec32, i, q);
+  return q;
 }
 
 __device__ __forceinline__ NodePrimF load_rec32(const float* rec32, int64_t i) {
@@ -99,18 +101,23 @@ __device__ __forceinline__ NodePrimF load_rec32(const float* rec32, int64_t i) {
   return NodePrimF{x.x, x.y, x.z, x.w, y.x, y.y, y.z, y.w};
 }
 
+// The FP32 edge flux, spelled with explicit IEEE intrinsics (never contracted
+// or reordered by the compiler), so every kernel that inlines it -- the edge
+// kernel and the fused node-centric stage -- computes the same bits from the
+// same inputs.
 __device__ __forceinline__ void edge_flux_f32(const NodePrimF& a, const NodePrimF& b, float4 w, float f[5]) {
   // w = (-wx/2, -wy/2, -wz/2, wfac), as edge_flux in device_math.cuh.
-  const float mha = a.mx * w.x + a.my * w.y + a.mz * w.z;
-  const float mhb = b.mx * w.x + b.my * w.y + b.mz * w.z;
-  const float uha = mha * a.rinv, uhb = mhb * b.rinv;
-  const float fac = w.w * (a.s + b.s);
-  const float pp = a.p + b.p;
-  f[0] = fac * (a.rho - b.rho) + (mha + mhb);
-  f[1] = fac * (a.mx - b.mx) + (a.mx * uha + b.mx * uhb + pp * w.x);
-  f[2] = fac * (a.my - b.my) + (a.my * uha + b.my * uhb + pp * w.y);
-  f[3] = fac * (a.mz - b.mz) + (a.mz * uha + b.mz * uhb + pp * w.z);
-  f[4] = fac * (a.rhoE - b.rhoE) + ((a.rhoE + a.p) * uha + (b.rhoE + b.p) * uhb);
+  const float mha = __fmaf_rn(a.mz, w.z, __fmaf_rn(a.my, w.y, __fmul_rn(a.mx, w.x)));
+  const float mhb = __fmaf_rn(b.mz, w.z, __fmaf_rn(b.my, w.y, __fmul_rn(b.mx, w.x)));
+  const float uha = __fmul_rn(mha, a.rinv), uhb = __fmul_rn(mhb, b.rinv);
+  const float fac = __fmul_rn(w.w, __fadd_rn(a.s, b.s));
+  const float pp = __fadd_rn(a.p, b.p);
+  f[0] = __fmaf_rn(fac, __fsub_rn(a.rho, b.rho), __fadd_rn(mha, mhb));
+  f[1] = __fmaf_rn(fac, __fsub_rn(a.mx, b.mx), __fmaf_rn(pp, w.x, __fmaf_rn(b.mx, uhb, __fmul_rn(a.mx, uha))));
+  f[2] = __fmaf_rn(fac, __fsub_rn(a.my, b.my), __fmaf_rn(pp, w.y, __fmaf_rn(b.my, uhb, __fmul_rn(a.my, uha))));
+  f[3] = __fmaf_rn(fac, __fsub_rn(a.mz, b.mz), __fmaf_rn(pp, w.z, __fmaf_rn(b.mz, uhb, __fmul_rn(a.mz, uha))));
+  f[4] = __fmaf_rn(fac, __fsub_rn(a.rhoE, b.rhoE),
+                   __fmaf_rn(__fadd_rn(b.rhoE, b.p), uhb, __fmul_rn(__fadd_rn(a.rhoE, a.p), uha)));
 }
 
 // 1/vol and cbrt(vol) on the device for both setup paths, so the solver's
@@ -153,7 +160,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_step_begin(int32_t n, double* 
                                                              unsigned long long* __restrict__ dt_key,
                                                              const DevStatus* __restrict__ st,
                                                              const int32_t* __restrict__ mesh_id) {
-  __shared__ double smin[kNodeThreads / 32];
+  __shared__ unsigned long long smin[kNodeThreads / 32];
   __shared__ int s_halt;
   __shared__ unsigned long long s_key[SEG ? kNodeThreads : 1];
   if (threadIdx.x == 0) s_halt = st->halt;
@@ -161,33 +168,42 @@ __global__ void __launch_bounds__(kNodeThreads) k_step_begin(int32_t n, double* 
   __syncthreads();
   if (s_halt) return;  // block-uniform: the reduction below synchronises
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  double m = DBL_MAX;
+  // The minimum is taken over order-preserving integer keys of dt, so the
+  // reduction issues no FP64 compare; ~0 = no candidate.
+  unsigned long long key = ~0ull;
   if (i < n) {
     const double4_32a* r = reinterpret_cast<const double4_32a*>(rec + 8 * i);
     const double4_32a x = r[0];
     const double e = r[1].x;
-    const NodePrim p = node_prim(x.x, x.y, x.z, x.w, e);
-    store_rec(rec, i, p);
-    if (MIXED) store_rec32_from_var(rec32, i, x.x, x.y, x.z, x.w, e);
     double* o = old + 5 * i;
     o[0] = x.x; o[1] = x.y; o[2] = x.z; o[3] = x.w; o[4] = e;
-    const double dt = 0.5 * (cbrt_vol[i] / p.s);  // time_stepping_kernels.h:31
-    if (dt < m) m = dt;                            // NaN never wins, as in get_min_dt_kernel
+    double dt;
+    if (MIXED) {
+      // The spectral radius is edge-flux arithmetic (FP32); min_dt itself
+      // is exact in FP64 and the step factor and update stay FP64.
+      const NodePrimF q = store_rec32_from_var(rec32, i, x.x, x.y, x.z, x.w, e);
+      dt = f2d_bits(0.5f * (d2f_bits(cbrt_vol[i]) / q.s));  // time_stepping_kernels.h:31
+    } else {
+      const NodePrim p = node_prim(x.x, x.y, x.z, x.w, e);
+      store_rec(rec, i, p);
+      dt = 0.5 * (cbrt_vol[i] / p.s);  // time_stepping_kernels.h:31
+    }
+    key = dt_candidate_key(dt);
   }
   if (SEG) {
     const int32_t m0 = mesh_id[(int64_t)blockIdx.x * blockDim.x];
-    if (i < n && m < DBL_MAX) atomicMin(&s_key[mesh_id[i] - m0], dkey(m));
+    if (key != ~0ull) atomicMin(&s_key[mesh_id[i] - m0], key);
     __syncthreads();
     if (s_key[threadIdx.x] != ~0ull) atomicMin(dt_key + m0 + threadIdx.x, s_key[threadIdx.x]);
     return;
   }
-  m = warp_min(m);
-  if ((threadIdx.x & 31) == 0) smin[threadIdx.x >> 5] = m;
+  key = warp_min_u64(key);
+  if ((threadIdx.x & 31) == 0) smin[threadIdx.x >> 5] = key;
   __syncthreads();
   if (threadIdx.x < 32) {
-    m = threadIdx.x < kNodeThreads / 32 ? smin[threadIdx.x] : DBL_MAX;
-    m = warp_min(m);
-    if (threadIdx.x == 0 && m < DBL_MAX) atomicMin(dt_key, dkey(m));
+    key = threadIdx.x < kNodeThreads / 32 ? smin[threadIdx.x] : ~0ull;
+    key = warp_min_u64(key);
+    if (threadIdx.x == 0 && key != ~0ull) atomicMin(dt_key, key);
   }
 }
 
@@ -221,10 +237,13 @@ __global__ void k_flux_f64(int32_t ne, const int2* __restrict__ e2n, const doubl
   }
 }
 
-// Mixed precision edge flux: FP32 arithmetic, FP64 accumulation.
+// Mixed precision edge flux: FP32 arithmetic, FP64 accumulation.  The
+// gather strategy stores the FP32 fluxes (widened exactly, on the integer
+// pipe, where the node sums them in FP64); the atomic strategy widens them
+// here and adds them with FP64 atomics.
 template <bool GATHER>
 __global__ void k_flux_mixed(int32_t ne, const int2* __restrict__ e2n, const float4* __restrict__ w4f,
-                             const float* __restrict__ rec32, double* __restrict__ flux, double* __restrict__ fe,
+                             const float* __restrict__ rec32, double* __restrict__ flux, float* __restrict__ fe32,
                              const DevStatus* __restrict__ st) {
   if (st->halt) return;
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -236,16 +255,17 @@ __global__ void k_flux_mixed(int32_t ne, const int2* __restrict__ e2n, const flo
   float f[5];
   edge_flux_f32(a, b, w, f);
   if (GATHER) {
-    double* o = fe + 5 * e;
+    float* o = fe32 + 5 * e;
 #pragma unroll
-    for (int k = 0; k < 5; k++) o[k] = (double)f[k];
+    for (int k = 0; k < 5; k++) o[k] = f[k];
   } else {
     double* fa = flux + 5 * (int64_t)ab.x;
     double* fb = flux + 5 * (int64_t)ab.y;
 #pragma unroll
     for (int k = 0; k < 5; k++) {
-      atomicAdd(fa + k, (double)f[k]);
-      atomicAdd(fb + k, (double)-f[k]);
+      const double d = f2d_bits(f[k]);
+      atomicAdd(fa + k, d);
+      atomicAdd(fb + k, negate(d));
     }
   }
 }
@@ -286,6 +306,12 @@ struct UpdateArgs {
   const double* old;
   double* flux;
   const double* fe;
+  const float* fe32;
+  const float* rec32_in;   // fused: the stage's input primitives (rec32 is the output)
+  const int2* e2n;
+  const float4* w4f;
+  const int32_t* b_nbr;
+  const float4* b_w4f;
   const int32_t* a_off;
   const int32_t* b_off;
   const int32_t* b_list;
@@ -318,7 +344,7 @@ __device__ __forceinline__ void add_boundary(const NodePrim& p, const double* __
 // calc_rms_kernel and count_bad_vals in the last stage).  Plain solvers stop
 // everything on min_dt < 0 or NaN/Inf (the reference aborts); batched
 // solvers mark the failing mesh and leave the others running.
-template <bool GATHER, bool LAST, bool MIXED, bool SEG>
+template <bool GATHER, bool LAST, bool MIXED, bool SEG, bool PAIR = false, bool FUSED = false>
 __global__ void __launch_bounds__(kNodeThreads) k_update(UpdateArgs A) {
   __shared__ double srms[kNodeThreads / 32];
   __shared__ double srho[kNodeThreads / 32];
@@ -327,11 +353,23 @@ __global__ void __launch_bounds__(kNodeThreads) k_update(UpdateArgs A) {
   __shared__ double s_sum[SEG && LAST ? kNodeThreads : 1];
   __shared__ double s_rho[SEG && LAST ? kNodeThreads : 1];
   __shared__ int s_bad[SEG && LAST ? kNodeThreads : 1];
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  // The node's own data is loaded before the block-uniform halt and min_dt
+  // checks so that its latency overlaps them; nothing is written before.
+  double o[5] = {0.0, 0.0, 0.0, 0.0, 0.0}, Fa[5] = {0.0, 0.0, 0.0, 0.0, 0.0}, ivol = 0.0;
+  int32_t bi = -1;
+  if (!GATHER && i < A.n) {  // (the gather forms load them after their edge loop)
+#pragma unroll
+    for (int k = 0; k < 5; k++) o[k] = A.old[5 * i + k];
+    ivol = A.inv_vol[i];
+    bi = A.bidx[i];
+#pragma unroll
+    for (int k = 0; k < 5; k++) Fa[k] = A.flux[5 * i + k];
+  }
   if (threadIdx.x == 0) s_halt = A.st->halt;
   if (SEG && LAST) { s_sum[threadIdx.x] = 0.0; s_rho[threadIdx.x] = 0.0; s_bad[threadIdx.x] = 0; }
   __syncthreads();
   if (s_halt) return;  // block-uniform: the reduction below synchronises
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int32_t mid = 0;
   double min_dt;
   if (SEG) {
@@ -353,23 +391,71 @@ __global__ void __launch_bounds__(kNodeThreads) k_update(UpdateArgs A) {
   }
   if (active) {
     double F[5];
-    if (GATHER) {
+    if (FUSED) {
+      // Node-centric stage: the flux of each edge of this node, computed from
+      // the stage's input primitives exactly as k_flux_mixed computes it
+      // (end a first), summed in k_update's gather order.
+      const NodePrimF me = load_rec32(A.rec32_in, i);
+      float hi[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, lo[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int k = 0; k < 5; k++) F[k] = 0.0;
+      float f[5];
+      for (int32_t e = A.a_off[i]; e < A.a_off[i + 1]; e++) {
+        edge_flux_f32(me, load_rec32(A.rec32_in, A.e2n[e].y), A.w4f[e], f);
+#pragma unroll
+        for (int k = 0; k < 5; k++) {
+          if (PAIR) two_sum_acc(hi[k], lo[k], f[k]);
+          else F[k] += f2d_bits(f[k]);
+        }
+      }
+      for (int32_t j = A.b_off[i]; j < A.b_off[i + 1]; j++) {
+        edge_flux_f32(load_rec32(A.rec32_in, A.b_nbr[j]), me, A.b_w4f[j], f);
+#pragma unroll
+        for (int k = 0; k < 5; k++) {
+          if (PAIR) two_sum_acc(hi[k], lo[k], -f[k]);
+          else F[k] -= f2d_bits(f[k]);
+        }
+      }
+      if (PAIR) {
+#pragma unroll
+        for (int k = 0; k < 5; k++) F[k] = f2d_bits(hi[k]) + f2d_bits(lo[k]);
+      }
+    } else if (GATHER && MIXED && PAIR) {
+      // Unevaluated FP32 pairs (hi, lo) fed by error-free TwoSum steps;
+      // one FP64 add per variable at the end.
+      float hi[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, lo[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+      for (int32_t e = A.a_off[i]; e < A.a_off[i + 1]; e++)
+#pragma unroll
+        for (int k = 0; k < 5; k++) two_sum_acc(hi[k], lo[k], A.fe32[5 * (int64_t)e + k]);
+      for (int32_t j = A.b_off[i]; j < A.b_off[i + 1]; j++) {
+        const int64_t e = A.b_list[j];
+#pragma unroll
+        for (int k = 0; k < 5; k++) two_sum_acc(hi[k], lo[k], -A.fe32[5 * e + k]);
+      }
+#pragma unroll
+      for (int k = 0; k < 5; k++) F[k] = f2d_bits(hi[k]) + f2d_bits(lo[k]);
+    } else if (GATHER) {
 #pragma unroll
       for (int k = 0; k < 5; k++) F[k] = 0.0;
       for (int32_t e = A.a_off[i]; e < A.a_off[i + 1]; e++)
 #pragma unroll
-        for (int k = 0; k < 5; k++) F[k] += A.fe[5 * (int64_t)e + k];
+        for (int k = 0; k < 5; k++) F[k] += MIXED ? f2d_bits(A.fe32[5 * (int64_t)e + k]) : A.fe[5 * (int64_t)e + k];
       for (int32_t j = A.b_off[i]; j < A.b_off[i + 1]; j++) {
         const int64_t e = A.b_list[j];
 #pragma unroll
-        for (int k = 0; k < 5; k++) F[k] -= A.fe[5 * e + k];
+        for (int k = 0; k < 5; k++) F[k] -= MIXED ? f2d_bits(A.fe32[5 * e + k]) : A.fe[5 * e + k];
       }
     } else {
       double* fl = A.flux + 5 * i;
 #pragma unroll
-      for (int k = 0; k < 5; k++) { F[k] = fl[k]; fl[k] = 0.0; }
+      for (int k = 0; k < 5; k++) { F[k] = Fa[k]; fl[k] = 0.0; }
     }
-    const int32_t bi = A.bidx[i];
+    if (GATHER) {
+#pragma unroll
+      for (int k = 0; k < 5; k++) o[k] = A.old[5 * i + k];
+      ivol = A.inv_vol[i];
+      bi = A.bidx[i];
+    }
     if (bi >= 0) {
       NodePrim p;
       if (MIXED) {
@@ -381,8 +467,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_update(UpdateArgs A) {
       }
       add_boundary(p, A.bdata + 12 * (int64_t)bi, F);
     }
-    const double factor = (min_dt * A.inv_vol[i]) * A.inv_div;  // step_factor / (RK+1-rk)
-    const double* o = A.old + 5 * i;
+    const double factor = (min_dt * ivol) * A.inv_div;  // step_factor / (RK+1-rk)
     double v[5];
 #pragma unroll
     for (int k = 0; k < 5; k++) v[k] = o[k] + factor * F[k];
@@ -391,13 +476,19 @@ __global__ void __launch_bounds__(kNodeThreads) k_update(UpdateArgs A) {
       r[0] = make_double4_32a(v[0], v[1], v[2], v[3]);
       A.rec[8 * i + 4] = v[4];
       double* rs = A.res + 5 * i;
+      double d[5];
 #pragma unroll
       for (int k = 0; k < 5; k++) {
-        const double d = v[k] - o[k];
-        rs[k] = d;
-        r2 += d * d;
-        if (k == 0) rr = d * d;
-        if (isnan(v[k]) || isinf(v[k])) bad++;
+        d[k] = v[k] - o[k];
+        rs[k] = d[k];
+      }
+      if (A.level0) {  // calc_rms_kernel and count_bad_vals run on level 0 only
+#pragma unroll
+        for (int k = 0; k < 5; k++) {
+          r2 += d[k] * d[k];
+          bad += not_finite(v[k]) ? 1 : 0;
+        }
+        rr = d[0] * d[0];
       }
     } else if (MIXED) {
       double4_32a* r = reinterpret_cast<double4_32a*>(A.rec + 8 * i);
@@ -481,6 +572,47 @@ __global__ void k_prolong(int32_t nf, const int32_t* __restrict__ n2mg, const do
   for (int k = 0; k < 5; k++) r[k] -= dd[k] * (cres[5 * c + k] - fres[5 * i + k]);
 }
 
+// Far-field terms w.F_ff of every folded boundary row for a new freestream
+// (the same arithmetic as the setup's fold, so a retargeted solver holds the
+// bits a fresh one would).
+__global__ void k_bnd_ffw(int32_t nrows, double* __restrict__ bdata, mgcfd_freestream ff) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
+  double* row = bdata + 12 * r;
+  const double w0 = row[0], w1 = row[1], w2 = row[2];
+  const double* fv = ff.ff_variable;
+  const double* rows[4] = {ff.ff_flux_contribution_momentum_x, ff.ff_flux_contribution_momentum_y,
+                           ff.ff_flux_contribution_momentum_z, ff.ff_flux_contribution_density_energy};
+  row[6] = __dadd_rn(__dadd_rn(__dmul_rn(w0, fv[1]), __dmul_rn(w1, fv[2])), __dmul_rn(w2, fv[3]));
+  for (int q = 0; q < 4; q++)
+    row[7 + q] = __dadd_rn(__dadd_rn(__dmul_rn(w0, rows[q][0]), __dmul_rn(w1, rows[q][1])), __dmul_rn(w2, rows[q][2]));
+}
+
+// Fused increment: b-side copies of the edge data in b_list order.
+__global__ void k_bside(int32_t ne, const int32_t* __restrict__ b_list, const int2* __restrict__ e2n,
+                        const float4* __restrict__ w4f, int32_t* __restrict__ b_nbr, float4* __restrict__ b_w4f) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= ne) return;
+  const int32_t e = b_list[j];
+  b_nbr[j] = e2n[e].x;
+  b_w4f[j] = w4f[e];
+}
+
+// End of a V-cycle under a stop rule: count it, record the level-0 density
+// residual norm sqrt(sum(res_rho^2) / N0) and stop further work (not an
+// error) when the rule is met.  One thread.
+__global__ void k_cycle_end(DevStatus* st, double n0, int32_t max_cycles, double drop) {
+  if (st->halt) return;
+  const int c = ++st->cycles_done;
+  const double rho = sqrt(st->rho_acc / n0);
+  if (c == 1) st->rho_first = rho;
+  st->rho_last = rho;
+  if (c >= max_cycles || (drop > 0.0 && c > 1 && rho <= drop * st->rho_first)) {
+    st->stopped = 1;
+    st->halt = 1;
+  }
+}
+
 // Fetch helpers: scatter the renumbered rows [off, off + n) back to input
 // order (rows of one mesh, or of the whole level when off = 0).
 __global__ void k_unpermute(int32_t n, int32_t off, int32_t width, int32_t stride, const double* __restrict__ src,
@@ -526,6 +658,22 @@ const UpdateFn kUpdate[16] = {
     launch_update<1, 0, 0, 0>, launch_update<1, 0, 0, 1>, launch_update<1, 0, 1, 0>, launch_update<1, 0, 1, 1>,
     launch_update<1, 1, 0, 0>, launch_update<1, 1, 0, 1>, launch_update<1, 1, 1, 0>, launch_update<1, 1, 1, 1>};
 
+template <bool L, bool S>
+void launch_update_pair(int grid_n, cudaStream_t st, const UpdateArgs& A) {
+  k_update<true, L, true, S, true><<<grid_n, kNodeThreads, 0, st>>>(A);
+}
+const UpdateFn kUpdatePair[4] = {launch_update_pair<0, 0>, launch_update_pair<0, 1>, launch_update_pair<1, 0>,
+                                 launch_update_pair<1, 1>};
+
+template <bool L, bool S, bool P>
+void launch_update_fused(int grid_n, cudaStream_t st, const UpdateArgs& A) {
+  k_update<true, L, true, S, P, true><<<grid_n, kNodeThreads, 0, st>>>(A);
+}
+const UpdateFn kUpdateFused[8] = {launch_update_fused<0, 0, 0>, launch_update_fused<0, 0, 1>,
+                                  launch_update_fused<0, 1, 0>, launch_update_fused<0, 1, 1>,
+                                  launch_update_fused<1, 0, 0>, launch_update_fused<1, 0, 1>,
+                                  launch_update_fused<1, 1, 0>, launch_update_fused<1, 1, 1>};
+
 template <bool M, bool S>
 void launch_step_begin(const DevLevel& D, unsigned long long* key, const DevStatus* st, cudaStream_t stream) {
   k_step_begin<M, S><<<grid(D.n, kNodeThreads), kNodeThreads, 0, stream>>>(D.n, D.rec, D.rec32, D.old, D.cbrt_vol,
@@ -553,40 +701,61 @@ int enqueue_smooth(mgcfd_solver* s, int level) {
   kStepBegin[(mixed ? 2 : 0) | (seg ? 1 : 0)](D, key, s->st, s->stream);
   s->launches++;
   const int et = edge_threads(s);
+  const bool pair = mixed && s->opt.accumulation == MGCFD_ACCUM_PAIR32;
   for (int rk = 0; rk < kRK; rk++) {
-    if (D.ne > 0) {
-      std::pair<cudaEvent_t, cudaEvent_t> ev{nullptr, nullptr};
-      if (timing) {
-        if (!s->spare.empty()) { ev = s->spare.back(); s->spare.pop_back(); }
-        else {
-          CK(cudaEventCreate(&ev.first));
-          CK(cudaEventCreate(&ev.second));
-        }
-        CK(cudaEventRecord(ev.first, s->stream));
+    const bool last = rk == kRK - 1;
+    // Level-0 timing events wrap the flux sweep (the fused stage when the
+    // flux is computed inside the node kernel).
+    std::pair<cudaEvent_t, cudaEvent_t> ev{nullptr, nullptr};
+    const bool time_this = timing && D.ne > 0;
+    if (time_this) {
+      if (!s->spare.empty()) { ev = s->spare.back(); s->spare.pop_back(); }
+      else {
+        CK(cudaEventCreate(&ev.first));
+        CK(cudaEventCreate(&ev.second));
       }
+      CK(cudaEventRecord(ev.first, s->stream));
+    }
+    if (D.ne > 0 && !s->fused) {
       const int g = grid(D.ne, et);
       if (mixed) {
-        if (s->gather) k_flux_mixed<true><<<g, et, 0, s->stream>>>(D.ne, D.e2n, D.w4f, D.rec32, D.flux, D.fe, s->st);
-        else k_flux_mixed<false><<<g, et, 0, s->stream>>>(D.ne, D.e2n, D.w4f, D.rec32, D.flux, D.fe, s->st);
+        if (s->gather) k_flux_mixed<true><<<g, et, 0, s->stream>>>(D.ne, D.e2n, D.w4f, D.rec32, D.flux, D.fe32, s->st);
+        else k_flux_mixed<false><<<g, et, 0, s->stream>>>(D.ne, D.e2n, D.w4f, D.rec32, D.flux, D.fe32, s->st);
       } else {
         if (s->gather) k_flux_f64<true><<<g, et, 0, s->stream>>>(D.ne, D.e2n, D.w4, D.rec, D.flux, D.fe, s->st);
         else k_flux_f64<false><<<g, et, 0, s->stream>>>(D.ne, D.e2n, D.w4, D.rec, D.flux, D.fe, s->st);
       }
       s->launches++;
-      if (timing) {
+      if (time_this) {
         CK(cudaEventRecord(ev.second, s->stream));
         s->pending.push_back(ev);
       }
     }
     UpdateArgs A;
     A.n = D.n; A.level0 = level == 0; A.inv_div = 1.0 / (double)(kRK + 1 - rk);
-    A.rec = D.rec; A.rec32 = D.rec32; A.old = D.old; A.flux = D.flux; A.fe = D.fe;
+    A.rec = D.rec; A.rec32 = D.rec32; A.old = D.old; A.flux = D.flux; A.fe = D.fe; A.fe32 = D.fe32;
     A.a_off = D.a_off; A.b_off = D.b_off; A.b_list = D.b_list; A.inv_vol = D.inv_vol; A.bidx = D.bidx;
     A.bdata = D.bdata; A.res = D.res; A.dt_key = key; A.st = s->st;
     A.mesh_id = D.mesh_id; A.seg_neg = s->seg_neg; A.seg_bad = s->seg_bad; A.seg_rms = s->seg_rms;
     A.seg_rho = s->seg_rho;
-    const bool last = rk == kRK - 1;
-    kUpdate[(s->gather ? 8 : 0) | (last ? 4 : 0) | (mixed ? 2 : 0) | (seg ? 1 : 0)](grid(D.n, kNodeThreads), s->stream, A);
+    A.e2n = D.e2n; A.w4f = D.w4f; A.b_nbr = D.b_nbr; A.b_w4f = D.b_w4f;
+    if (s->fused) {
+      // Stage rk reads the primitives of stage rk and writes those of rk + 1
+      // into the other buffer: k_step_begin fills rec32 for stage 0.
+      A.rec32_in = (rk & 1) ? D.rec32b : D.rec32;
+      A.rec32 = (rk & 1) ? D.rec32 : D.rec32b;
+      kUpdateFused[(last ? 4 : 0) | (seg ? 2 : 0) | (pair ? 1 : 0)](grid(D.n, kNodeThreads), s->stream, A);
+      if (time_this) {
+        CK(cudaEventRecord(ev.second, s->stream));
+        s->pending.push_back(ev);
+      }
+    } else if (mixed && s->gather && pair) {
+      A.rec32_in = nullptr;
+      kUpdatePair[(last ? 2 : 0) | (seg ? 1 : 0)](grid(D.n, kNodeThreads), s->stream, A);
+    } else {
+      A.rec32_in = nullptr;
+      kUpdate[(s->gather ? 8 : 0) | (last ? 4 : 0) | (mixed ? 2 : 0) | (seg ? 1 : 0)](grid(D.n, kNodeThreads), s->stream, A);
+    }
     s->launches++;
     if (s->opt.measure_mem_bound && D.ne > 0) {
       k_stream<<<grid(D.ne, et), et, 0, s->stream>>>(D.ne, D.e2n, D.w4, D.rec, D.dummy, s->st);
@@ -601,13 +770,12 @@ int enqueue_smooth(mgcfd_solver* s, int level) {
 // One iteration of the reference's while loop (euler3d.cpp:458-640).
 int enqueue_iteration(mgcfd_solver* s) {
   const int levels = (int)s->L.size();
+  const int64_t cycle0 = s->cycle;
   int r = enqueue_smooth(s, s->level);
   if (r) return r;
   if (levels <= 1) {
     s->cycle++;
-    return MGCFD_OK;
-  }
-  if (s->up) {
+  } else if (s->up) {
     s->level++;
     DevLevel& F = s->L[(size_t)s->level - 1];
     DevLevel& Cl = s->L[(size_t)s->level];
@@ -624,6 +792,10 @@ int enqueue_iteration(mgcfd_solver* s) {
       s->up = true;
       s->cycle++;
     }
+  }
+  if (s->cycle != cycle0 && s->stop_max_cycles > 0) {  // a V-cycle just ended
+    k_cycle_end<<<1, 1, 0, s->stream>>>(s->st, (double)s->L[0].n, s->stop_max_cycles, s->stop_drop);
+    s->launches++;
   }
   CK(cudaGetLastError());
   return MGCFD_OK;
@@ -726,6 +898,22 @@ void free_solver(mgcfd_solver* s) {
 
 }  // namespace
 
+namespace {
+// Increment strategy: AUTO is FP64 atomics for FP64 and the fused
+// node-centric stage for mixed precision (the fastest of each, measured).
+int resolve_increment(mgcfd_solver* s) {
+  const int inc = s->opt.increment;
+  const bool mixed = s->opt.precision == MGCFD_PRECISION_MIXED;
+  if (inc < MGCFD_INCREMENT_AUTO || inc > MGCFD_INCREMENT_FUSED)
+    return set_error(MGCFD_ERR_INVALID, "unknown increment strategy");
+  if (inc == MGCFD_INCREMENT_FUSED && !mixed)
+    return set_error(MGCFD_ERR_INVALID, "the fused increment needs mixed precision");
+  s->fused = inc == MGCFD_INCREMENT_FUSED || (inc == MGCFD_INCREMENT_AUTO && mixed);
+  s->gather = s->fused || inc == MGCFD_INCREMENT_GATHER;
+  return MGCFD_OK;
+}
+}  // namespace
+
 extern "C" void mgcfd_solver_default_options(mgcfd_solver_options* o) {
   if (!o) return;
   std::memset(o, 0, sizeof(*o));
@@ -742,13 +930,15 @@ extern "C" int mgcfd_solver_create(int32_t nlevels, const mgcfd_level_view* leve
   if (nlevels < 1 || nlevels > kMaxLevels) return set_error(MGCFD_ERR_INVALID, "mgcfd_solver_create: 1..16 levels supported");
   std::unique_ptr<mgcfd_solver, void (*)(mgcfd_solver*)> s(new (std::nothrow) mgcfd_solver(), free_solver);
   if (!s) return set_error(MGCFD_ERR_NOMEM, "host allocation failed");
+  int r0;
   if (opt) s->opt = *opt; else mgcfd_solver_default_options(&s->opt);
   if (s->opt.precision != MGCFD_PRECISION_FP64 && s->opt.precision != MGCFD_PRECISION_MIXED)
     return set_error(MGCFD_ERR_INVALID, "unknown precision");
+  if (s->opt.accumulation != MGCFD_ACCUM_FP64 && s->opt.accumulation != MGCFD_ACCUM_PAIR32)
+    return set_error(MGCFD_ERR_INVALID, "unknown accumulation");
   if (s->opt.block_size < 0 || s->opt.block_size > 1024 || (s->opt.block_size % 32) != 0)
     return set_error(MGCFD_ERR_INVALID, "block_size must be 0 or a multiple of 32 up to 1024");
-  s->gather = s->opt.increment == MGCFD_INCREMENT_GATHER ||
-              (s->opt.increment == MGCFD_INCREMENT_AUTO && s->opt.precision == MGCFD_PRECISION_MIXED);
+  if ((r0 = resolve_increment(s.get()))) return r0;
   s->stream = static_cast<cudaStream_t>(stream);
   CK(cudaGetDevice(&s->device));
   if (!s->stream) {
@@ -815,10 +1005,14 @@ extern "C" int mgcfd_solver_create(int32_t nlevels, const mgcfd_level_view* leve
       if ((r = s->upload(&D.w4, p.w4.data(), (size_t)p.ne))) return r;
     }
     if (s->gather) {
-      if ((r = s->alloc(&D.fe, 5 * (size_t)p.ne)) || (r = s->upload(&D.a_off, p.a_off.data(), (size_t)p.n + 1)) ||
+      if ((r = s->upload(&D.a_off, p.a_off.data(), (size_t)p.n + 1)) ||
           (r = s->upload(&D.b_off, p.b_off.data(), (size_t)p.n + 1)) ||
           (r = s->upload(&D.b_list, p.b_list.data(), (size_t)p.ne)))
         return r;
+      if (s->fused) r = build_fused_tables(s.get(), D);
+      else if (mixed) r = s->alloc(&D.fe32, 5 * (size_t)p.ne);
+      else r = s->alloc(&D.fe, 5 * (size_t)p.ne);
+      if (r) return r;
     } else {
       if ((r = s->alloc(&D.flux, 5 * (size_t)p.n))) return r;
     }
@@ -848,15 +1042,17 @@ extern "C" int mgcfd_batch_create(int32_t nmeshes, int32_t nlevels, const mgcfd_
   if (nlevels < 1 || nlevels > kMaxLevels) return set_error(MGCFD_ERR_INVALID, "mgcfd_batch_create: 1..16 levels supported");
   std::unique_ptr<mgcfd_solver, void (*)(mgcfd_solver*)> s(new (std::nothrow) mgcfd_solver(), free_solver);
   if (!s) return set_error(MGCFD_ERR_NOMEM, "host allocation failed");
+  int r0;
   if (opt) s->opt = *opt; else mgcfd_solver_default_options(&s->opt);
   if (s->opt.precision != MGCFD_PRECISION_FP64 && s->opt.precision != MGCFD_PRECISION_MIXED)
     return set_error(MGCFD_ERR_INVALID, "unknown precision");
+  if (s->opt.accumulation != MGCFD_ACCUM_FP64 && s->opt.accumulation != MGCFD_ACCUM_PAIR32)
+    return set_error(MGCFD_ERR_INVALID, "unknown accumulation");
   if (s->opt.block_size < 0 || s->opt.block_size > 1024 || (s->opt.block_size % 32) != 0)
     return set_error(MGCFD_ERR_INVALID, "block_size must be 0 or a multiple of 32 up to 1024");
   if (s->opt.renumber == MGCFD_RENUMBER_RCM || s->opt.host_setup)
     return set_error(MGCFD_ERR_INVALID, "batched solvers are set up on the device (renumber none or spatial)");
-  s->gather = s->opt.increment == MGCFD_INCREMENT_GATHER ||
-              (s->opt.increment == MGCFD_INCREMENT_AUTO && s->opt.precision == MGCFD_PRECISION_MIXED);
+  if ((r0 = resolve_increment(s.get()))) return r0;
   s->stream = static_cast<cudaStream_t>(stream);
   CK(cudaGetDevice(&s->device));
   if (!s->stream) {
@@ -933,6 +1129,36 @@ extern "C" int mgcfd_solver_run(mgcfd_solver* s, int32_t ncycles) {
       if (r) return r;
     }
   }
+  return MGCFD_OK;
+}
+
+int mgcfd::build_fused_tables(mgcfd_solver* s, DevLevel& D) {
+  int r;
+  if ((r = s->alloc(&D.rec32b, 8 * (size_t)D.n)) || (r = s->alloc(&D.b_nbr, (size_t)D.ne)) ||
+      (r = s->alloc(&D.b_w4f, (size_t)D.ne)))
+    return r;
+  if (D.ne > 0)
+    k_bside<<<(unsigned)((D.ne + 255) / 256), 256, 0, s->stream>>>(D.ne, D.b_list, D.e2n, D.w4f, D.b_nbr, D.b_w4f);
+  CK(cudaGetLastError());
+  return MGCFD_OK;
+}
+
+int mgcfd::solver_retarget(mgcfd_solver* s, double mach, double aoa_deg) {
+  if (!s || s->nseg > 1) return set_error(MGCFD_ERR_INVALID, "retarget: plain solvers only");
+  int r = mgcfd_freestream_init(mach, aoa_deg, &s->ff);
+  if (r) return r;
+  for (auto& D : s->L)
+    if (D.nbrows > 0)
+      k_bnd_ffw<<<(unsigned)((D.nbrows + 127) / 128), 128, 0, s->stream>>>(D.nbrows, D.bdata, s->ff);
+  CK(cudaGetLastError());
+  return init_state(s);
+}
+
+int mgcfd::solver_set_stop_rule(mgcfd_solver* s, int32_t max_cycles, double residual_drop) {
+  if (!s || s->nseg > 1 || max_cycles < 1 || s->graph || s->cycle > 0)
+    return set_error(MGCFD_ERR_INVALID, "stop rule: plain solver before its first cycle only");
+  s->stop_max_cycles = max_cycles;
+  s->stop_drop = residual_drop;
   return MGCFD_OK;
 }
 

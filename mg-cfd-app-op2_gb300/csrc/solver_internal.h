@@ -27,9 +27,15 @@ struct DevStatus {
   int halt;                                // non-zero: stop all further work
   int neg_dt;                              // min_dt < 0 seen
   int bad_count;                           // NaN/Inf count at level 0
-  int pad;
+  int stopped;                             // the stop rule ended the solve (not an error)
   double rms_acc;                          // sum of residual^2, last level-0 step
   double rho_acc;                          // its density part
+  // Stop rule (solvers run by the server): V-cycles completed and the
+  // level-0 density residual norm of the first and the latest of them.
+  int cycles_done;
+  int pad;
+  double rho_first;
+  double rho_last;
 };
 
 struct DevLevel {
@@ -38,6 +44,7 @@ struct DevLevel {
   int32_t nfine = 0;   // fine nodes (length of ch_list) when this level has a finer one
   double* rec = nullptr;
   float* rec32 = nullptr;
+  float* rec32b = nullptr;  // second FP32 primitive buffer (fused stages ping-pong)
   double* old = nullptr;
   double* flux = nullptr;
   double* res = nullptr;
@@ -48,10 +55,13 @@ struct DevLevel {
   int2* e2n = nullptr;
   double4_32a* w4 = nullptr;
   float4* w4f = nullptr;
-  double* fe = nullptr;
+  double* fe = nullptr;     // [E][5] per-edge fluxes, FP64 gather
+  float* fe32 = nullptr;    // [E][5] per-edge fluxes, mixed-precision gather
   int32_t* a_off = nullptr;
   int32_t* b_off = nullptr;
   int32_t* b_list = nullptr;
+  int32_t* b_nbr = nullptr;   // fused: end a of each edge in b_list order
+  float4* b_w4f = nullptr;    // fused: w4f of each edge in b_list order
   int32_t* bidx = nullptr;
   double* bdata = nullptr;
   int32_t* n2mg = nullptr;
@@ -91,13 +101,19 @@ struct mgcfd_solver {
   int64_t steps = 0;
   int64_t launches = 0;
   int64_t launches_per_cycle = 0;
-  bool gather = false;
+  bool gather = false;  // node-side CSR tables exist (GATHER or FUSED)
+  bool fused = false;   // FUSED: flux and update in one node-centric kernel
   cudaGraphExec_t graph = nullptr;
   // Kernel timing.
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending, spare;
   double flux_ms = 0.0;
   int64_t flux_sweeps = 0;
   int status = MGCFD_OK;
+  // Stop rule evaluated on the device at the end of every V-cycle (0 = off):
+  // stop after stop_max_cycles cycles, or once the level-0 density residual
+  // norm is at most stop_drop times that of the first cycle.
+  int32_t stop_max_cycles = 0;
+  double stop_drop = 0.0;
 
   template <class T>
   int alloc(T** p, size_t count) {
@@ -131,4 +147,17 @@ struct MeshInput {
 // meshes (concatenated per level, each renumbered on its own), device_setup.cu.
 // For one mesh the results equal prepare_mesh() in setup.cpp.
 int device_prepare(mgcfd_solver* s, const std::vector<MeshInput>& meshes);
+
+// FUSED increment: the second FP32 primitive buffer and the b-side copies
+// (b_nbr, b_w4f) of a level whose e2n, w4f and b_list are in place.
+int build_fused_tables(mgcfd_solver* s, DevLevel& D);
+
+// Re-initialises a plain solver for a new freestream (Mach, angle of
+// attack): far-field boundary terms, state and counters, as a fresh solver
+// on the same mesh would have them.  Stream-ordered.
+int solver_retarget(mgcfd_solver* s, double mach, double aoa_deg);
+
+// Installs the device-side stop rule on a plain solver before its first run
+// (the V-cycle graph is captured with it).
+int solver_set_stop_rule(mgcfd_solver* s, int32_t max_cycles, double residual_drop);
 }  // namespace mgcfd

@@ -33,7 +33,8 @@ class LevelView(C.Structure):
 class SolverOptions(C.Structure):
     _fields_ = [("precision", C.c_int32), ("increment", C.c_int32), ("renumber", C.c_int32),
                 ("use_graph", C.c_int32), ("measure_mem_bound", C.c_int32), ("block_size", C.c_int32),
-                ("time_kernels", C.c_int32), ("host_setup", C.c_int32), ("reserved", C.c_int32 * 8)]
+                ("time_kernels", C.c_int32), ("host_setup", C.c_int32), ("accumulation", C.c_int32),
+                ("reserved", C.c_int32 * 7)]
 
 
 class SolverStats(C.Structure):
@@ -45,7 +46,7 @@ class SolverStats(C.Structure):
 class ServerOptions(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_int64), ("max_active", C.c_int32), ("precision", C.c_int32),
                 ("increment", C.c_int32), ("max_cycles", C.c_int32), ("residual_drop", C.c_double),
-                ("reserved", C.c_int32 * 8)]
+                ("accumulation", C.c_int32), ("reserved", C.c_int32 * 7)]
 
 
 class RequestResult(C.Structure):
@@ -57,7 +58,8 @@ class RequestResult(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("failed", C.c_int64), ("active", C.c_int64),
                 ("pending", C.c_int64), ("used_bytes", C.c_int64), ("peak_bytes", C.c_int64),
-                ("peak_active", C.c_int64), ("reserved", C.c_int64 * 4)]
+                ("peak_active", C.c_int64), ("cache_hits", C.c_int64), ("cached_solvers", C.c_int64),
+                ("reserved", C.c_int64 * 2)]
 
 
 OK = 0
@@ -125,8 +127,8 @@ SIGNATURES = {
     "mgcfd_solver_mesh_status": (C.c_int, [_vp, _i32, _pp(C.c_double), _pp(C.c_double)]),
     "mgcfd_server_default_options": (None, [_pp(ServerOptions)]),
     "mgcfd_server_create": (C.c_int, [_pp(ServerOptions), _pp(_vp)]),
-    "mgcfd_server_submit": (C.c_int, [_vp, _i32, _pp(LevelView), C.c_double, C.c_double, c_double_p,
-                                      _pp(C.c_int64)]),
+    "mgcfd_server_submit": (C.c_int, [_vp, _i32, _pp(LevelView), C.c_double, C.c_double, C.c_int64,
+                                      c_double_p, _pp(C.c_int64)]),
     "mgcfd_server_poll": (C.c_int, [_vp, _pp(RequestResult), _i32, _pp(_i32)]),
     "mgcfd_server_drain": (C.c_int, [_vp, C.c_double]),
     "mgcfd_server_get_stats": (C.c_int, [_vp, _pp(ServerStats)]),

@@ -9,7 +9,7 @@ import time
 from .solver import Batch, Solver
 
 _CACHE: dict = {}
-CANDIDATES = [("atomic", 128), ("atomic", 256), ("gather", 128), ("gather", 256)]
+CANDIDATES = [("atomic", 128), ("atomic", 256), ("gather", 128), ("gather", 256), ("fused", 0)]
 
 
 def _key(total_nodes: int, precision: str):
@@ -27,6 +27,8 @@ def tune(make, total_nodes: int, precision: str = "fp64", cycles: int = 2, candi
         return _CACHE[key]
     timings = {}
     for inc, bs in candidates:
+        if inc == "fused" and precision != "mixed":
+            continue  # the fused node-centric stage exists for mixed precision only
         s = make(increment=inc, block_size=bs, precision=precision)
         s.run(1)  # warm-up, graph capture
         if s.synchronize() != 0:

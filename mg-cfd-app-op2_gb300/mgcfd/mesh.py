@@ -63,9 +63,14 @@ def renumber_nodes(method: str, coords: np.ndarray, edge_to_nodes: np.ndarray | 
 class HostMesh:
     """Owner of a native mgcfd_host_mesh; level arrays are zero-copy views."""
 
+    _next_serial = 1
+
     def __init__(self, handle):
         self._h = handle
         self._lib = _lib.load()
+        # Process-unique identity, used as the server's resident-mesh key.
+        self.serial = HostMesh._next_serial
+        HostMesh._next_serial += 1
 
     @classmethod
     def generate(cls, n: int, nlevels: int, seed: int) -> "HostMesh":

@@ -7,7 +7,7 @@ import numpy as np
 
 from . import _lib
 from .mesh import HostMesh, level_views_from_arrays
-from .solver import INCREMENT, PRECISION
+from .solver import ACCUMULATION, INCREMENT, PRECISION
 
 
 def estimate_bytes(mesh, precision: str = "fp64", increment: str = "auto") -> int:
@@ -25,7 +25,8 @@ class Server:
     """Continuous-batching solve server on one GPU."""
 
     def __init__(self, hbm_budget_gb: float = 150.0, max_active: int = 16, precision: str = "fp64",
-                 increment: str = "auto", max_cycles: int = 50, residual_drop: float = 1e-6):
+                 increment: str = "auto", max_cycles: int = 50, residual_drop: float = 1e-6,
+                 accumulation: str = "fp64"):
         self._lib = _lib.load()
         o = _lib.ServerOptions()
         self._lib.mgcfd_server_default_options(C.byref(o))
@@ -35,17 +36,24 @@ class Server:
         o.increment = INCREMENT[increment]
         o.max_cycles = max_cycles
         o.residual_drop = residual_drop
+        o.accumulation = ACCUMULATION[accumulation]
         h = C.c_void_p()
         _lib.check(self._lib.mgcfd_server_create(C.byref(o), C.byref(h)))
         self._h = h
         self._keep = {}  # request id -> (levels, views, output) kept alive until completion
 
-    def submit(self, mesh, mach: float, aoa_deg: float, want_result: bool = False) -> int:
+    def submit(self, mesh, mach: float, aoa_deg: float, want_result: bool = False, mesh_key: int | None = None,
+               resident: bool = True) -> int:
+        """Queue a solve.  A HostMesh is kept resident on the device between
+        requests (keyed by the HostMesh object) unless resident=False; a list
+        of Level arrays is resident only under an explicit mesh_key."""
         levels = mesh.levels() if isinstance(mesh, HostMesh) else mesh
+        if mesh_key is None:
+            mesh_key = mesh.serial if (resident and isinstance(mesh, HostMesh)) else 0
         views = level_views_from_arrays(levels)
         out = np.empty((levels[0].nnodes, 5)) if want_result else None
         rid = C.c_int64()
-        _lib.check(self._lib.mgcfd_server_submit(self._h, len(levels), views, mach, aoa_deg,
+        _lib.check(self._lib.mgcfd_server_submit(self._h, len(levels), views, mach, aoa_deg, int(mesh_key),
                                                  out.ctypes.data_as(_lib.c_double_p) if out is not None else None,
                                                  C.byref(rid)))
         self._keep[rid.value] = (mesh, levels, views, out)

@@ -9,13 +9,14 @@ from . import _lib
 from .mesh import HostMesh, level_views_from_arrays
 
 PRECISION = {"fp64": 0, "mixed": 1}
-INCREMENT = {"auto": 0, "atomic": 1, "gather": 2}
+INCREMENT = {"auto": 0, "atomic": 1, "gather": 2, "fused": 3}
 RENUMBER = {"none": 0, "spatial": 1, "rcm": 2}
+ACCUMULATION = {"fp64": 0, "pair32": 1}
 Q_VARIABLES, Q_FLUXES, Q_STEP_FACTORS, Q_VOLUMES, Q_RESIDUALS, Q_OLD_VARIABLES = range(6)
 
 
 def options(precision="fp64", increment="auto", renumber="spatial", use_graph=True, measure_mem_bound=False,
-            block_size=0, time_kernels=False, host_setup=False) -> _lib.SolverOptions:
+            block_size=0, time_kernels=False, host_setup=False, accumulation="fp64") -> _lib.SolverOptions:
     o = _lib.SolverOptions()
     _lib.load().mgcfd_solver_default_options(C.byref(o))
     o.precision = PRECISION[precision]
@@ -26,6 +27,7 @@ def options(precision="fp64", increment="auto", renumber="spatial", use_graph=Tr
     o.block_size = int(block_size)
     o.time_kernels = int(time_kernels)
     o.host_setup = int(host_setup)
+    o.accumulation = ACCUMULATION[accumulation]
     return o
 
 

@@ -60,8 +60,9 @@ def test_failing_mesh_is_isolated(meshes):
         assert state_error(b.fetch_mesh(m, 0), ref.get(0, O.Q_VARIABLES)) <= STATE_TOL
 
 
-def test_mixed_precision_batch(meshes):
-    b = mgcfd.Batch(meshes, MACH, AOA, precision="mixed", increment="gather")
+@pytest.mark.parametrize("increment,accumulation", [("gather", "fp64"), ("fused", "fp64"), ("fused", "pair32")])
+def test_mixed_precision_batch(meshes, increment, accumulation):
+    b = mgcfd.Batch(meshes, MACH, AOA, precision="mixed", increment=increment, accumulation=accumulation)
     b.run(3)
     assert b.synchronize() == 0
     for m, mesh in enumerate(meshes):
@@ -69,6 +70,12 @@ def test_mixed_precision_batch(meshes):
         assert ref.run(MACH[m], AOA[m], 3)[0] == 0
         mx, l2 = per_variable_errors(b.fetch_mesh(m, 0), ref.get(0, O.Q_VARIABLES))
         assert mx.max() <= MIXED_TOL and l2.max() <= MIXED_TOL
+        if increment == "fused":  # deterministic: equal to the mesh solved alone
+            s = mgcfd.Solver(mesh, MACH[m], AOA[m], precision="mixed", increment="fused", accumulation=accumulation)
+            s.run(3)
+            assert s.synchronize() == 0
+            np.testing.assert_array_equal(b.fetch_mesh(m, 0), s.fetch(0))
+            s.close()
 
 
 def test_residual_norms_match_oracle(meshes):

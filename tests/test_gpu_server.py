@@ -111,3 +111,57 @@ def test_failing_request_does_not_disturb_others(meshes):
     ref = O.OracleRun(meshes[0].levels())
     assert ref.run(CASES[0][3], CASES[0][4], 3)[0] == 0
     assert state_error(res[good][1], ref.get(0, O.Q_VARIABLES)) <= STATE_TOL
+
+
+def test_device_stop_rule_ends_the_solve_at_the_right_cycle(meshes):
+    """residual_drop = 10 is met as soon as it is tested (second cycle): the
+    server stops there although it has enqueued more cycles, and the result
+    is that of a plain 2-cycle solve, bit for bit (gather increment)."""
+    srv = mgcfd.Server(max_active=2, increment="gather", max_cycles=50, residual_drop=10.0)
+    out = run_requests(srv, meshes, [2])
+    srv.close()
+    res, var = out[2]
+    assert res["status"] == 0 and res["cycles"] == 2
+    assert res["rho_rms_first"] > 0 and res["rho_rms_last"] > 0
+    s = mgcfd.Solver(meshes[2], CASES[2][3], CASES[2][4], increment="gather")
+    s.run(2)
+    assert s.synchronize() == 0
+    np.testing.assert_array_equal(var, s.fetch(0))
+    s.close()
+
+
+def test_resident_mesh_reused_across_freestreams(meshes):
+    """Requests on the same HostMesh reuse its device tables (cache hits),
+    and each result equals a fresh solver's for that request's freestream."""
+    flows = [(0.5, 1.0), (0.8, 4.0), (0.35, 0.0)]
+    srv = mgcfd.Server(max_active=1, increment="gather", max_cycles=3)
+    got = {}
+    for mach, aoa in flows:
+        rid = srv.submit(meshes[1], mach, aoa, want_result=True)
+        srv.drain(300)
+        for res, var in srv.poll():
+            assert res["id"] == rid and res["status"] == 0
+            got[(mach, aoa)] = var
+    st = srv.stats()
+    srv.close()
+    assert st["cache_hits"] == 2 and st["cached_solvers"] == 1
+    for mach, aoa in flows:
+        s = mgcfd.Solver(meshes[1], mach, aoa, increment="gather")
+        s.run(3)
+        assert s.synchronize() == 0
+        np.testing.assert_array_equal(got[(mach, aoa)], s.fetch(0))
+        s.close()
+
+
+def test_idle_meshes_are_evicted_for_new_ones(meshes):
+    a, b = meshes[0], meshes[2]
+    budget = max(server.estimate_bytes(a), server.estimate_bytes(b)) * 1.5  # one resident mesh at a time
+    srv = mgcfd.Server(hbm_budget_gb=budget / 2 ** 30, max_active=2, max_cycles=2)
+    for mesh in (a, b, a):
+        srv.submit(mesh, 0.5, 1.0)
+        srv.drain(300)
+    res = [r for r, _ in srv.poll()]
+    st = srv.stats()
+    srv.close()
+    assert [r["status"] for r in res] == [0, 0, 0]
+    assert st["cache_hits"] == 0 and st["cached_solvers"] == 1 and st["used_bytes"] <= budget

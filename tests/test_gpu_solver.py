@@ -80,6 +80,52 @@ def test_mixed_precision_error_bound():
         assert delta_error(x, r, x0) <= 1e-4   # FP32 flux: the change itself is right to ~1e-6
 
 
+def test_mixed_precision_pair_accumulation():
+    """MGCFD_ACCUM_PAIR32: node sums in compensated FP32 pairs; same bar
+    against the oracle, and within 1e-8 of the FP64-accumulated mixed run."""
+    mesh = mgcfd.HostMesh.generate(24, 3, 78)
+    levels = mesh.levels()
+    mach, aoa, cycles = 0.7, 2.0, 4
+    ref = _oracle(levels, mach, aoa, cycles)
+    runs = {}
+    for acc in ("fp64", "pair32"):
+        s = mgcfd.Solver(mesh, mach, aoa, precision="mixed", increment="gather", accumulation=acc)
+        s.run(cycles)
+        assert s.synchronize() == 0
+        runs[acc] = [s.fetch(l) for l in range(3)]
+        s.close()
+    for l in range(3):
+        mx, l2 = per_variable_errors(runs["pair32"][l], ref.get(l, O.Q_VARIABLES))
+        assert mx.max() <= MIXED_TOL and l2.max() <= MIXED_TOL, (mx, l2)
+        mx, _ = per_variable_errors(runs["pair32"][l], runs["fp64"][l])
+        assert mx.max() <= 1e-8, mx
+
+
+@pytest.mark.parametrize("accumulation", ["fp64", "pair32"])
+@pytest.mark.parametrize("n,nl,cycles,host_setup", [(12, 3, 3, False), (17, 2, 2, True), (48, 3, 2, False)])
+def test_fused_stage_equals_gather_bitwise(n, nl, cycles, host_setup, accumulation):
+    """The fused node-centric stage computes each edge's FP32 flux at both
+    ends from the same inputs and sums in the gather order: the gather
+    strategy's results bit for bit, on every level."""
+    mesh = mgcfd.HostMesh.generate(n, nl, 100 + n)
+    out = {}
+    for inc in ("gather", "fused"):
+        s = mgcfd.Solver(mesh, 0.75, 2.5, precision="mixed", increment=inc, accumulation=accumulation,
+                         host_setup=host_setup)
+        s.run(cycles)
+        assert s.synchronize() == 0
+        out[inc] = [s.fetch(l) for l in range(nl)] + [s.fetch(0, mgcfd.Q_RESIDUALS)]
+        s.close()
+    for a, b in zip(out["gather"], out["fused"]):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_fused_needs_mixed_precision():
+    mesh = mgcfd.HostMesh.generate(6, 1, 1)
+    with pytest.raises(mgcfd._lib.MgcfdError):
+        mgcfd.Solver(mesh, 0.5, 0.0, precision="fp64", increment="fused")
+
+
 def test_run_in_pieces_equals_one_run():
     mesh = mgcfd.HostMesh.generate(12, 3, 5)
     a = mgcfd.Solver(mesh, 0.5, 3.0, increment="gather")
