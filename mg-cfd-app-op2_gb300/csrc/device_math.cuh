@@ -119,46 +119,56 @@ __device__ __forceinline__ void farfield_flux(const NodePrim& b, double wx, doub
 //             overflow rounds to infinity, NaNs keep the top payload bits and
 //             become quiet; results in the binary32 subnormal range are
 //             rounded with the same rule from the full 53-bit significand.
-__device__ __forceinline__ double f2d_bits(float f) {
+// The 64-bit register is packed and unpacked with PTX moves, which the
+// compiler cannot fold back into a floating-point conversion.
+__device__ __forceinline__ double pack_words(uint32_t hi, uint32_t lo) {
+  double d;
+  asm("mov.b64 %0, {%1, %2};" : "=d"(d) : "r"(lo), "r"(hi));
+  return d;
+}
+
+__device__ __forceinline__ void unpack_words(double d, uint32_t& hi, uint32_t& lo) {
+  asm("mov.b64 {%0, %1}, %2;" : "=r"(lo), "=r"(hi) : "d"(d));
+}
+
+// Zero, subnormal, infinity and NaN inputs: a separate, rarely taken call, so
+// the common path issues only its own integer instructions.  A subnormal is
+// first scaled by 2^24 in FP32 (exact) and its exponent corrected after.
+static __device__ __noinline__ double f2d_bits_special(float f) {
   const uint32_t u = __float_as_uint(f);
   const uint32_t sign = u & 0x80000000u;
   const uint32_t a = u & 0x7fffffffu;
-  uint32_t hi, lo;
-  if (a - 0x00800000u < 0x7f000000u) {  // normal: exponent field 1..254
-    hi = sign | ((a >> 3) + (896u << 20));
-    lo = u << 29;
-  } else if (a >= 0x7f800000u) {         // infinity or NaN
-    hi = sign | 0x7ff00000u | ((a & 0x7fffffu) >> 3);
-    lo = u << 29;
-  } else if (a == 0u) {
-    hi = sign;
-    lo = 0u;
-  } else {                               // subnormal: a = m * 2^-149, m < 2^23
-    const int s = __clz(a) - 8;          // a << s has bit 23 set
-    const uint32_t m = (a << s) & 0x7fffffu;
-    hi = sign | ((uint32_t)(897 - s) << 20) | (m >> 3);
-    lo = m << 29;
-  }
-  return __hiloint2double((int)hi, (int)lo);
+  if (a == 0u) return pack_words(sign, 0u);
+  if (a >= 0x7f800000u) return pack_words(sign | 0x7ff00000u | ((a & 0x7fffffu) >> 3), u << 29);
+  const uint32_t g = __float_as_uint(__fmul_rn(__uint_as_float(a), 16777216.0f));  // normal now
+  return pack_words(sign | (((g >> 3) + (896u << 20)) - (24u << 20)), g << 29);
+}
+
+__device__ __forceinline__ double f2d_bits(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t a = u & 0x7fffffffu;
+  if (a - 0x00800000u >= 0x7f000000u) return f2d_bits_special(f);  // not a normal number
+  return pack_words((u & 0x80000000u) | ((a >> 3) + (896u << 20)), u << 29);
 }
 
 __device__ __forceinline__ float d2f_bits(double d) {
-  const unsigned long long u = (unsigned long long)__double_as_longlong(d);
-  const uint32_t sign = (uint32_t)(u >> 32) & 0x80000000u;
-  const int de = (int)((u >> 52) & 0x7ff);
-  const unsigned long long m = u & 0xfffffffffffffull;
+  uint32_t hi, lo;
+  unpack_words(d, hi, lo);
+  const uint32_t sign = hi & 0x80000000u;
+  const int de = (int)((hi >> 20) & 0x7ffu);
+  const uint32_t mhi = hi & 0xfffffu;    // top 20 of the 52 significand bits
   uint32_t r;
   if (de > 896 && de < 1151) {           // binary32 normal range before rounding
-    const uint32_t rest = (uint32_t)(m & 0x1fffffffu);
-    r = ((uint32_t)(de - 896) << 23) | (uint32_t)(m >> 29);
+    const uint32_t rest = lo & 0x1fffffffu;
+    r = ((uint32_t)(de - 896) << 23) | (mhi << 3) | (lo >> 29);
     r += (rest > 0x10000000u || (rest == 0x10000000u && (r & 1u))) ? 1u : 0u;  // carries into the exponent
   } else if (de == 2047) {               // infinity or NaN
-    r = 0x7f800000u | (m ? (0x400000u | (uint32_t)(m >> 29)) : 0u);
+    r = 0x7f800000u | ((mhi | lo) ? (0x400000u | (mhi << 3) | (lo >> 29)) : 0u);
   } else if (de >= 1151) {               // beyond binary32: infinity
     r = 0x7f800000u;
   } else {                               // subnormal or zero in binary32
     const int k = 926 - de;              // value / 2^-149 = full >> k, k >= 30
-    const unsigned long long full = (de ? (1ull << 52) : 0ull) | m;
+    const unsigned long long full = ((unsigned long long)(de ? (mhi | 0x100000u) : mhi) << 32) | lo;
     if (k >= 64) {
       r = 0u;
     } else {

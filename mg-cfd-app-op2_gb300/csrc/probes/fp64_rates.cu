@@ -64,6 +64,71 @@ __global__ void k_unary(double* out, int iters) {
   for (int k = 0; k < 8; k++) s += x[k];
   out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
+// Widening and accumulating FP32 values into FP64, as the mixed-precision
+// node sums do: op 0 = acc += 1.0 (the FP64 add alone), 1 = acc += (double)x
+// (hardware cvt), 2 = acc += f2d_bits(x) (integer pipe).  The FP32 chain that
+// makes x runs on the FP32 pipe in all three.
+template <int OP>
+__global__ void k_widen(double* out, int iters) {
+  float x[8];
+  double acc[8];
+  for (int k = 0; k < 8; k++) { x[k] = 1.0f + 1e-3f * (threadIdx.x + k); acc[k] = 0.0; }
+  for (int i = 0; i < iters; i++)
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      x[k] = fmaf(x[k], 1.0001f, 1e-3f);
+      if (OP == 0) acc[k] += 1.0;
+      if (OP == 1) acc[k] += (double)x[k];
+      if (OP == 2) acc[k] += mgcfd::f2d_bits(x[k]);
+    }
+  double s = 0;
+  for (int k = 0; k < 8; k++) s += acc[k] + x[k];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+// Widening forms for the node-sum probe (finite normal inputs only).
+__device__ __forceinline__ double widen_hilo(float f) {  // __hiloint2double packing
+  const uint32_t u = __float_as_uint(f), a = u & 0x7fffffffu;
+  return __hiloint2double((int)((u & 0x80000000u) | ((a >> 3) + (896u << 20))), (int)(u << 29));
+}
+__device__ __forceinline__ double widen_i64(float f) {  // one 64-bit integer expression
+  const unsigned long long u = __float_as_uint(f);
+  const unsigned long long b = ((u & 0x80000000ull) << 32) | (((u & 0x7fffffffull) << 29) + (896ull << 52));
+  return __longlong_as_double((long long)b);
+}
+__device__ __forceinline__ double widen_asm(float f) {  // asm packing, no special cases
+  const uint32_t u = __float_as_uint(f), a = u & 0x7fffffffu;
+  return mgcfd::pack_words((u & 0x80000000u) | ((a >> 3) + (896u << 20)), u << 29);
+}
+
+// The node-sum pattern of the mixed-precision update: each thread widens 30
+// FP32 values read from memory (6 edges x 5 variables) and adds them into 5
+// FP64 sums.  op 0 = hardware cvt, 1 = f2d_bits, 2 = FP32 sums widened once.
+// The array (256 K threads x 30 floats) stays in L2, so the arithmetic shows.
+template <int OP>
+__global__ void k_node_sums(int n, const float* __restrict__ fe, double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double F[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  float G[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  const float* p = fe + 30 * (int64_t)i;
+  for (int e = 0; e < 6; e++)
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+      const float x = p[5 * e + k];
+      if (OP == 0) F[k] += (double)x;
+      if (OP == 1) F[k] += mgcfd::f2d_bits(x);
+      if (OP == 2) G[k] += x;
+      if (OP == 3) F[k] += widen_hilo(x);
+      if (OP == 4) F[k] += widen_i64(x);
+      if (OP == 5) F[k] += widen_asm(x);
+    }
+  double s = 0;
+#pragma unroll
+  for (int k = 0; k < 5; k++) s += OP == 2 ? mgcfd::f2d_bits(G[k]) : F[k];
+  out[i] = s;
+}
+
 __global__ void k_red(double* arr, uint32_t n, int per_thread) {
   uint32_t h = (blockIdx.x * blockDim.x + threadIdx.x) * 2654435761u;
   for (int i = 0; i < per_thread; i++) {
@@ -107,6 +172,20 @@ int main() {
   const float t_rsqrt = timed([&] { k_unary<2><<<kBlocks, kThreads>>>(od, iu); });
   const float t_cvt = timed([&] { k_unary<3><<<kBlocks, kThreads>>>(od, iu); });
   const float t_cvti = timed([&] { k_unary<4><<<kBlocks, kThreads>>>(od, iu); });
+  const float t_w0 = timed([&] { k_widen<0><<<kBlocks, kThreads>>>(od, iu); });
+  const float t_w1 = timed([&] { k_widen<1><<<kBlocks, kThreads>>>(od, iu); });
+  const float t_w2 = timed([&] { k_widen<2><<<kBlocks, kThreads>>>(od, iu); });
+  const int nsum = 256 * 1024;
+  float* fe;
+  CK(cudaMalloc(&fe, sizeof(float) * 30 * (size_t)nsum));
+  CK(cudaMemset(fe, 0x3f, sizeof(float) * 30 * (size_t)nsum));  // every float 0x3f3f3f3f = 0.747: normal
+  auto sums = [&](auto kernel) {
+    return timed([&] {
+      for (int r = 0; r < 20; r++) kernel<<<(nsum + 255) / 256, 256>>>(nsum, fe, od);
+    });
+  };
+  const float t_s0 = sums(k_node_sums<0>), t_s1 = sums(k_node_sums<1>), t_s2 = sums(k_node_sums<2>);
+  const float t_s3 = sums(k_node_sums<3>), t_s4 = sums(k_node_sums<4>), t_s5 = sums(k_node_sums<5>);
   CK(cudaGetLastError());
   const uint32_t an = 64u << 20;  // 512 MB of doubles: atomics go to HBM
   double* arr;
@@ -128,12 +207,17 @@ int main() {
   printf("{\"device\": \"%s\", \"sms\": %d, \"dfma_g_per_s\": %.1f, \"fp64_tflops\": %.3f, \"fp32_tflops\": %.2f, "
          "\"rcp_g_per_s\": %.1f, \"rcp_dfma_eq\": %.2f, \"sqrt_g_per_s\": %.1f, \"sqrt_dfma_eq\": %.2f, "
          "\"rsqrt_g_per_s\": %.1f, \"rsqrt_dfma_eq\": %.2f, \"cvt_d2f2d_dfma_eq\": %.2f, "
-         "\"intpipe_d2f2d_dfma_eq\": %.2f, \"red_f64_hbm_g_per_s\": %.1f, \"d2d_copy_gb_per_s\": %.1f}\n",
+         "\"intpipe_d2f2d_dfma_eq\": %.2f, \"widen_add_dfma_eq\": {\"add_only\": %.2f, \"hw_cvt\": %.2f, "
+         "\"f2d_bits\": %.2f}, \"node_sums_us\": {\"hw_cvt\": %.1f, \"f2d_bits\": %.1f, \"fp32_then_once\": %.1f, \"hilo\": %.1f, "
+         "\"i64\": %.1f, \"asm_normal_only\": %.1f}, "
+         "\"red_f64_hbm_g_per_s\": %.1f, \"d2d_copy_gb_per_s\": %.1f}\n",
          p.name, p.multiProcessorCount, dfma_per_s / 1e9, 2 * dfma_per_s / 1e12,
          2 * 8.0 * ops / (t_ffma * 1e-3) / 1e12, uops / (t_rcp * 1e-3) / 1e9, eq(t_rcp, uops),
          uops / (t_sqrt * 1e-3) / 1e9, eq(t_sqrt, uops), uops / (t_rsqrt * 1e-3) / 1e9, eq(t_rsqrt, uops),
-         eq(t_cvt, uops), eq(t_cvti, uops), (double)per * kN / (t_red * 1e-3) / 1e9,
+         eq(t_cvt, uops), eq(t_cvti, uops), eq(t_w0, uops), eq(t_w1, uops), eq(t_w2, uops),
+         1e3 * t_s0 / 20, 1e3 * t_s1 / 20, 1e3 * t_s2 / 20, 1e3 * t_s3 / 20, 1e3 * t_s4 / 20, 1e3 * t_s5 / 20,
+         (double)per * kN / (t_red * 1e-3) / 1e9,
          2.0 * big * 8 / (t_copy * 1e-3) / 1e9);
-  cudaFree(od); cudaFree(of); cudaFree(arr); cudaFree(src); cudaFree(dst);
+  cudaFree(od); cudaFree(of); cudaFree(arr); cudaFree(src); cudaFree(dst); cudaFree(fe);
   return 0;
 }
