@@ -201,6 +201,15 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
   lo += e;
 }
 
+// Order-preserving map from float to uint32 and back.
+__device__ __forceinline__ unsigned int fkey(float v) {
+  const unsigned int u = __float_as_uint(v);
+  return (u >> 31) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float fkey_inv(unsigned int k) {
+  return __uint_as_float((k >> 31) ? (k & 0x7fffffffu) : ~k);
+}
+
 // Key of a dt value for the min_dt reduction, or ~0 when the value takes no
 // part: get_min_dt_kernel (time_stepping_kernels.h:34-41) keeps its DBL_MAX
 // start unless dt < it, so NaN, +inf and DBL_MAX itself never win.  Integer

@@ -5,7 +5,7 @@
 //                 [-I interval] [-n] [-c config] [--output-variables]
 //                 [--output-fluxes] [--output-step-factors]
 //                 [--mach M] [--aoa DEG] [--precision fp64|mixed]
-//                 [--increment atomic|gather]
+//                 [--increment auto|atomic|gather|fused] [--accumulation fp64|pair32]
 //
 // Differences from the reference, all forced by running on one GPU:
 //   * -m/-r (partitioner) and -p (PAPI) are accepted and ignored;
@@ -35,7 +35,7 @@ struct Config {
   int cycles = 25;           // config.h:150
   int flow_interval = 0;
   double mach = 1.2, aoa = 0.0;
-  int precision = MGCFD_PRECISION_FP64, increment = MGCFD_INCREMENT_AUTO;
+  int precision = MGCFD_PRECISION_FP64, increment = MGCFD_INCREMENT_AUTO, accumulation = MGCFD_ACCUM_FP64;
 };
 
 std::string trim(const std::string& s) {
@@ -96,7 +96,8 @@ void usage() {
                "-v, --validate-result            check final state against pre-calculated solution\n"
                "-I, --output-flow-interval=INT   cycles between writes of the level-0 flow\n"
                "--output-variables | --output-fluxes | --output-step-factors\n"
-               "--mach=FLOAT (1.2)  --aoa=DEGREES (0.0)  --precision=fp64|mixed  --increment=atomic|gather\n"
+               "--mach=FLOAT (1.2)  --aoa=DEGREES (0.0)  --precision=fp64|mixed\n"
+               "--increment=auto|atomic|gather|fused  --accumulation=fp64|pair32\n"
                "-m, -r, -p are accepted for compatibility and ignored (one GPU, no PAPI).\n");
 }
 
@@ -124,6 +125,7 @@ bool parse(int argc, char** argv, Config& c) {
       {"aoa", required_argument, nullptr, 1002},
       {"precision", required_argument, nullptr, 1003},
       {"increment", required_argument, nullptr, 1004},
+      {"accumulation", required_argument, nullptr, 1005},
       {nullptr, 0, nullptr, 0}};
   int o;
   while ((o = getopt_long(argc, argv, "hc:li:d:p:o:g:m:r:vbnI:", opts, nullptr)) != -1) {
@@ -144,8 +146,13 @@ bool parse(int argc, char** argv, Config& c) {
       case 1002: c.aoa = std::atof(optarg); break;
       case 1003: c.precision = std::strcmp(optarg, "mixed") == 0 ? MGCFD_PRECISION_MIXED : MGCFD_PRECISION_FP64; break;
       case 1004:
-        c.increment = std::strcmp(optarg, "gather") == 0 ? MGCFD_INCREMENT_GATHER
-                      : std::strcmp(optarg, "atomic") == 0 ? MGCFD_INCREMENT_ATOMIC : MGCFD_INCREMENT_AUTO;
+        c.increment = std::strcmp(optarg, "gather") == 0   ? MGCFD_INCREMENT_GATHER
+                      : std::strcmp(optarg, "atomic") == 0 ? MGCFD_INCREMENT_ATOMIC
+                      : std::strcmp(optarg, "fused") == 0  ? MGCFD_INCREMENT_FUSED
+                                                           : MGCFD_INCREMENT_AUTO;
+        break;
+      case 1005:
+        c.accumulation = std::strcmp(optarg, "pair32") == 0 ? MGCFD_ACCUM_PAIR32 : MGCFD_ACCUM_FP64;
         break;
       case 0: break;
       default: std::printf("Unknown command line parameter '%c'\n", o);
@@ -206,6 +213,7 @@ int main(int argc, char** argv) {
   mgcfd_solver_default_options(&opt);
   opt.precision = c.precision;
   opt.increment = c.increment;
+  opt.accumulation = c.accumulation;
   opt.renumber = c.renumber ? MGCFD_RENUMBER_RCM : MGCFD_RENUMBER_SPATIAL;
   opt.measure_mem_bound = c.mem_bound ? 1 : 0;
   mgcfd_solver* s = nullptr;

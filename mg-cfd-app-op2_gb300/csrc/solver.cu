@@ -161,6 +161,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_step_begin(int32_t n, double* 
                                                              const DevStatus* __restrict__ st,
                                                              const int32_t* __restrict__ mesh_id) {
   __shared__ unsigned long long smin[kNodeThreads / 32];
+  __shared__ unsigned int sest[kNodeThreads / 32];
   __shared__ int s_halt;
   __shared__ unsigned long long s_key[SEG ? kNodeThreads : 1];
   if (threadIdx.x == 0) s_halt = st->halt;
@@ -171,24 +172,46 @@ __global__ void __launch_bounds__(kNodeThreads) k_step_begin(int32_t n, double* 
   // The minimum is taken over order-preserving integer keys of dt, so the
   // reduction issues no FP64 compare; ~0 = no candidate.
   unsigned long long key = ~0ull;
+  double cv = 0.0, sp = 1.0;  // FP64: cbrt(vol) and |u| + c of this node
+  float est = 0.0f;
   if (i < n) {
     const double4_32a* r = reinterpret_cast<const double4_32a*>(rec + 8 * i);
     const double4_32a x = r[0];
     const double e = r[1].x;
     double* o = old + 5 * i;
     o[0] = x.x; o[1] = x.y; o[2] = x.z; o[3] = x.w; o[4] = e;
-    double dt;
     if (MIXED) {
       // The spectral radius is edge-flux arithmetic (FP32); min_dt itself
       // is exact in FP64 and the step factor and update stay FP64.
       const NodePrimF q = store_rec32_from_var(rec32, i, x.x, x.y, x.z, x.w, e);
-      dt = f2d_bits(0.5f * (d2f_bits(cbrt_vol[i]) / q.s));  // time_stepping_kernels.h:31
+      key = dt_candidate_key(f2d_bits(0.5f * (d2f_bits(cbrt_vol[i]) / q.s)));  // time_stepping_kernels.h:31
     } else {
       const NodePrim p = node_prim(x.x, x.y, x.z, x.w, e);
       store_rec(rec, i, p);
-      dt = 0.5 * (cbrt_vol[i] / p.s);  // time_stepping_kernels.h:31
+      cv = cbrt_vol[i];
+      sp = p.s;
+      if (SEG) key = dt_candidate_key(0.5 * (cv / sp));  // time_stepping_kernels.h:31
+      else est = 0.5f * __fdividef(d2f_bits(cv), d2f_bits(sp));
     }
-    key = dt_candidate_key(dt);
+  }
+  if (!MIXED && !SEG) {
+    // Only the minimum of dt is needed.  An FP32 estimate (relative error
+    // below 4e-7: two narrowings and __fdividef's 2 ulp) picks the nodes
+    // that can hold the minimum -- those within 4e-6 of the block's smallest
+    // estimate -- and only they divide in FP64.  Estimates that are not
+    // finite normal numbers always take the exact path.
+    const uint32_t eb = __float_as_uint(est) & 0x7fffffffu;
+    const bool normal = i < n && eb - 0x00800000u < 0x7f000000u;
+    unsigned int ek = normal ? fkey(est) : 0xffffffffu;
+    ek = __reduce_min_sync(0xffffffffu, ek);
+    if ((threadIdx.x & 31) == 0) sest[threadIdx.x >> 5] = ek;
+    __syncthreads();
+    unsigned int bk = sest[0];
+#pragma unroll
+    for (int w = 1; w < kNodeThreads / 32; w++) bk = min(bk, sest[w]);
+    const float m32 = bk == 0xffffffffu ? INFINITY : fkey_inv(bk);
+    if (i < n && (!normal || est <= m32 + fabsf(m32) * 4e-6f))
+      key = dt_candidate_key(0.5 * (cv / sp));  // time_stepping_kernels.h:31
   }
   if (SEG) {
     const int32_t m0 = mesh_id[(int64_t)blockIdx.x * blockDim.x];
@@ -346,9 +369,9 @@ __device__ __forceinline__ void add_boundary(const NodePrim& p, const double* __
 // solvers mark the failing mesh and leave the others running.
 template <bool GATHER, bool LAST, bool MIXED, bool SEG, bool PAIR = false, bool FUSED = false>
 __global__ void __launch_bounds__(kNodeThreads) k_update(UpdateArgs A) {
-  __shared__ double srms[kNodeThreads / 32];
-  __shared__ double srho[kNodeThreads / 32];
-  __shared__ int sbad[kNodeThreads / 32];
+  __shared__ double srms[LAST ? kNodeThreads : 1];
+  __shared__ double srho[LAST ? kNodeThreads : 1];
+  __shared__ int sbad[LAST ? kNodeThreads : 1];
   __shared__ int s_halt;
   __shared__ double s_sum[SEG && LAST ? kNodeThreads : 1];
   __shared__ double s_rho[SEG && LAST ? kNodeThreads : 1];
@@ -516,18 +539,23 @@ __global__ void __launch_bounds__(kNodeThreads) k_update(UpdateArgs A) {
     if (s_bad[t]) atomicAdd(A.seg_bad + m0 + t, s_bad[t]);
     return;
   }
-  r2 = warp_sum(r2);
-  rr = warp_sum(rr);
-  bad = warp_sum_int(bad);
-  if ((threadIdx.x & 31) == 0) { srms[threadIdx.x >> 5] = r2; srho[threadIdx.x >> 5] = rr; sbad[threadIdx.x >> 5] = bad; }
+  // Block sums through shared memory, halving the active threads each step
+  // down to one warp: every FP64 add is a useful one (a shuffle tree in each
+  // warp would issue five per thread).
+  const int t = threadIdx.x;
+  srms[t] = r2;
+  srho[t] = rr;
+  sbad[t] = bad;
   __syncthreads();
-  if (threadIdx.x < 32) {
-    r2 = threadIdx.x < kNodeThreads / 32 ? srms[threadIdx.x] : 0.0;
-    rr = threadIdx.x < kNodeThreads / 32 ? srho[threadIdx.x] : 0.0;
-    bad = threadIdx.x < kNodeThreads / 32 ? sbad[threadIdx.x] : 0;
-    r2 = warp_sum(r2);
-    rr = warp_sum(rr);
-    bad = warp_sum_int(bad);
+#pragma unroll
+  for (int w = kNodeThreads / 2; w >= 32; w >>= 1) {
+    if (t < w) { srms[t] += srms[t + w]; srho[t] += srho[t + w]; sbad[t] += sbad[t + w]; }
+    __syncthreads();
+  }
+  if (t < 32) {
+    r2 = warp_sum(srms[t]);
+    rr = warp_sum(srho[t]);
+    bad = warp_sum_int(sbad[t]);
     if (threadIdx.x == 0) {
       atomicAdd(&A.st->rms_acc, r2);
       atomicAdd(&A.st->rho_acc, rr);

@@ -88,3 +88,24 @@ def test_legacy_mode_and_mem_bound_flag(tmp_path):
         outs.append(mgcfd.h5_read(f"{pre}variables.L0.cycles=2.h5", "p_variables_result_L0"))
     for o in outs[1:]:
         assert state_error(o, outs[0]) <= STATE_TOL
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("extra", [["--precision", "mixed"], ["--precision", "mixed", "--accumulation", "pair32"],
+                                   ["--precision", "mixed", "--increment", "gather"]])
+def test_mixed_precision_flags(tmp_path, extra):
+    """--precision mixed (with the increment and accumulation choices) stays
+    within the mixed-precision bar of the FP64 run's solution files."""
+    from parity import MIXED_TOL, per_variable_errors
+    mesh = mgcfd.HostMesh.generate(10, 2, 33)
+    mesh.write(str(tmp_path), "m_")
+    base = ["-i", "input.dat", "-d", tmp_path, "-g", 3, "--mach", 0.6, "--aoa", 2.0, "--output-variables"]
+    assert cli(*base, "-o", f"{tmp_path}/f.").returncode == 0
+    r = cli(*base, "-o", f"{tmp_path}/m.", *extra)
+    assert r.returncode == 0, r.stdout + r.stderr
+    for l in range(2):
+        a = mgcfd.h5_read(tmp_path / f"f.variables.L{l}.cycles=3.h5", f"p_variables_result_L{l}")
+        b = mgcfd.h5_read(tmp_path / f"m.variables.L{l}.cycles=3.h5", f"p_variables_result_L{l}")
+        mx, l2 = per_variable_errors(b, a)
+        assert mx.max() <= MIXED_TOL and l2.max() <= MIXED_TOL
+        assert not np.array_equal(a, b)  # the flag took effect
