@@ -5,12 +5,16 @@
 //   rec    [N][8]  f64  rho, rho*u, rho*v, rho*w, rho*E, p, |u|+c, 1/rho
 //                       (the conserved state plus the primitives the edge
 //                       kernel needs; 64 B rows read with two 256-bit loads)
-//   rec32  [N][8]  f32  the same in FP32 (mixed precision only)
+//   rec32  [N][8]  f32  the same in FP32 (mixed precision only; the fused
+//                       strategy alternates it with rec32b between stages)
 //   old, res, flux [N][5] f64; inv_vol, cbrt_vol, vol [N] f64
 //   e2n    [E]     int2 (a < b, sorted by a then b); w4 [E] double4
 //                       (-wx/2, -wy/2, -wz/2, -|w|*smoothing*0.5) or float4 (mixed)
 //   fe     [E][5]  f64  per-edge fluxes (gather increment strategy only;
 //                       f32 fe32 in mixed precision)
+//   a_off/b_off/b_list  CSR of each node's edges as end a and as end b
+//                       (gather and fused); b_nbr/b_w4f: the b-side edge data
+//                       in b_list order (fused)
 //   bidx [N] int32 and bdata [NB][12] f64: boundary entries folded per node
 //   n2mg [N], dvec [N] double4: prolongation parent and |dx|,|dy|,|dz|,dist
 //   ch_off/ch_list: restriction children of each coarse node
@@ -23,8 +27,11 @@
 //         k_update nodes  gathered flux + boundary flux, time step, flux = 0,
 //                         primitives for the next stage; in the last stage
 //                         residual, and at level 0 the rms and NaN/Inf count }
+//   (fused strategy, mixed precision: no k_flux; k_update computes each of
+//   its node's edge fluxes itself from the stage's input primitives)
 // then k_restrict (coarse nodes, children mean, mg.h:29-64) or k_prolong
-// (fine nodes, mg.h:66-88).
+// (fine nodes, mg.h:66-88), and under a stop rule k_cycle_end after each
+// V-cycle.
 //
 // Failure handling: min_dt < 0 and NaN/Inf at level 0 set a sticky device
 // status word; every later kernel sees it and returns, so the run stops at the
