@@ -106,6 +106,9 @@ int mgcfd_host_mesh_load(const char* input_file, const char* input_dir, int lega
  * ("*.renumbered", "areas", "edge_weights.recalculated"; euler3d.cpp:247-309). */
 int mgcfd_host_mesh_write(const mgcfd_host_mesh* mesh, const char* dir, const char* prefix,
                           int32_t legacy_datasets);
+/* A host mesh holding copies of the caller's level arrays (any mesh, not only
+ * a synthetic lattice), e.g. to write it in the reference's layout. */
+int mgcfd_host_mesh_from_views(int32_t nlevels, const mgcfd_level_view* levels, mgcfd_host_mesh** out);
 int mgcfd_host_mesh_num_levels(const mgcfd_host_mesh* mesh);
 /* Views stay valid until the mesh is destroyed. */
 int mgcfd_host_mesh_level(const mgcfd_host_mesh* mesh, int level, mgcfd_level_view* out);

@@ -100,6 +100,44 @@ extern "C" int mgcfd_host_mesh_generate(int n, int nlevels, uint64_t seed, mgcfd
   return MGCFD_OK;
 }
 
+extern "C" int mgcfd_host_mesh_from_views(int32_t nlevels, const mgcfd_level_view* levels, mgcfd_host_mesh** out) {
+  if (!out || !levels || nlevels < 1) return set_error(MGCFD_ERR_INVALID, "mgcfd_host_mesh_from_views: bad arguments");
+  *out = nullptr;
+  for (int l = 0; l < nlevels; l++) {
+    const mgcfd_level_view& v = levels[l];
+    if (v.nnodes < 1 || v.nedges < 0 || v.nbnd < 0 || !v.coords || (v.nedges && (!v.edge_to_nodes || !v.edge_weights)) ||
+        (v.nbnd && (!v.bnd_to_node || !v.bnd_group || !v.bnd_weights)) || (l + 1 < nlevels && !v.node_to_mg))
+      return set_error(MGCFD_ERR_INVALID, "mgcfd_host_mesh_from_views: level " + std::to_string(l) + " is incomplete");
+  }
+  try {
+    std::unique_ptr<mgcfd_host_mesh> m(new mgcfd_host_mesh());
+    m->mesh.levels.resize((size_t)nlevels);
+    for (int l = 0; l < nlevels; l++) {
+      const mgcfd_level_view& v = levels[l];
+      mgcfd::HostLevel& L = m->mesh.levels[(size_t)l];
+      const size_t n = (size_t)v.nnodes, ne = (size_t)v.nedges, nb = (size_t)v.nbnd;
+      L.n_axis = v.n_axis;
+      L.nnodes = v.nnodes; L.nedges = v.nedges; L.nbnd = v.nbnd;
+      L.coords.assign(v.coords, v.coords + 3 * n);
+      if (ne) {
+        L.edge_to_nodes.assign(v.edge_to_nodes, v.edge_to_nodes + 2 * ne);
+        L.edge_weights.assign(v.edge_weights, v.edge_weights + 3 * ne);
+      }
+      if (nb) {
+        L.bnd_to_node.assign(v.bnd_to_node, v.bnd_to_node + nb);
+        L.bnd_group.assign(v.bnd_group, v.bnd_group + nb);
+        L.bnd_weights.assign(v.bnd_weights, v.bnd_weights + 3 * nb);
+      }
+      if (l + 1 < nlevels) L.node_to_mg.assign(v.node_to_mg, v.node_to_mg + n);
+      if (v.volumes) L.volumes.assign(v.volumes, v.volumes + n);
+    }
+    *out = m.release();
+  } catch (const std::bad_alloc&) {
+    return set_error(MGCFD_ERR_NOMEM, "host allocation failed");
+  }
+  return MGCFD_OK;
+}
+
 namespace {
 
 std::string trim(const std::string& s) {

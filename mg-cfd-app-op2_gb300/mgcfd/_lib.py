@@ -81,6 +81,7 @@ SIGNATURES = {
     "mgcfd_host_mesh_num_levels": (C.c_int, [_vp]),
     "mgcfd_host_mesh_level": (C.c_int, [_vp, C.c_int, _pp(LevelView)]),
     "mgcfd_host_mesh_destroy": (None, [_vp]),
+    "mgcfd_host_mesh_from_views": (C.c_int, [_i32, _pp(LevelView), _pp(_vp)]),
     "mgcfd_renumber_nodes": (C.c_int, [C.c_int, _i32, c_double_p, _i32, c_int32_p, c_int32_p]),
     "mgcfd_host_mesh_renumber": (C.c_int, [_vp, C.c_int, C.POINTER(_vp)]),
     "mgcfd_h5_dataset_shape": (C.c_int, [C.c_char_p, C.c_char_p, _pp(C.c_int64), _pp(C.c_int)]),

@@ -87,6 +87,15 @@ class HostMesh:
                                             C.byref(h)))
         return cls(h)
 
+    @classmethod
+    def from_levels(cls, levels) -> "HostMesh":
+        """A host mesh copied from a list of Level arrays (mgcfd_host_mesh_from_views)."""
+        lib = _lib.load()
+        views = level_views_from_arrays(levels)
+        h = C.c_void_p()
+        _lib.check(lib.mgcfd_host_mesh_from_views(len(levels), views, C.byref(h)))
+        return cls(h)
+
     def write(self, directory: str, prefix: str = "mesh_", legacy_datasets: bool = False) -> None:
         _lib.check(self._lib.mgcfd_host_mesh_write(self._h, str(directory).encode(), prefix.encode(),
                                                    int(legacy_datasets)))
