@@ -263,7 +263,8 @@ typedef struct mgcfd_solver_options {
   int32_t renumber;          /* MGCFD_RENUMBER_*                                    */
   int32_t use_graph;         /* capture one V-cycle as a CUDA graph and replay it  */
   int32_t measure_mem_bound; /* also run unstructured_stream each RK stage (-b)   */
-  int32_t block_size;        /* threads per block of the edge kernels; 0 = default */
+  int32_t block_size;        /* threads per block of the edge kernels (a multiple
+                                of 32 up to 1024); 0 = default (128)               */
   int32_t time_kernels;      /* record CUDA events around level-0 flux sweeps      */
   int32_t host_setup;        /* build the mesh tables on the host instead of the GPU
                                 (always on for MGCFD_RENUMBER_RCM); same results      */
