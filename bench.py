@@ -350,7 +350,7 @@ def run_batch(args):
         b = mgcfd.Batch(meshes, machs, aoas, **o)
         b.run(cycles)
         assert b.synchronize() == 0
-        outs = [b.fetch_mesh(m, 0) for m in range(nm)]
+        outs = b.fetch_meshes(0)
         b.close()
         return outs
 

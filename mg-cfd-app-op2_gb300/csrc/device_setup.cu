@@ -35,23 +35,86 @@ int bits_for(int64_t n) {  // number of bits needed to hold values 0..n
 }
 
 // Temporary device memory for the setup, freed (stream-ordered) at the end.
+// Setup scratch: a bump allocator over stream-ordered chunks of at least
+// 64 MiB, so that the many small temporaries of a setup cost a handful of
+// allocation calls.  Everything is released when the setup ends.
 struct Temp {
+  static constexpr size_t kChunk = 64ull << 20;
   cudaStream_t stream;
-  std::vector<void*> ptrs;
+  std::vector<void*> chunks;
+  char* cur = nullptr;
+  size_t left = 0;
   explicit Temp(cudaStream_t s) : stream(s) {}
   ~Temp() {
-    for (void* p : ptrs) cudaFreeAsync(p, stream);
+    for (void* p : chunks) cudaFreeAsync(p, stream);
   }
   template <class X>
   int get(X** p, size_t count) {
     *p = nullptr;
     if (count == 0) count = 1;
-    cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(p), count * sizeof(X), stream);
-    if (e != cudaSuccess) {
-      cudaGetLastError();
-      return set_error(MGCFD_ERR_NOMEM, std::string("setup scratch allocation failed: ") + cudaGetErrorString(e));
+    const size_t bytes = (count * sizeof(X) + 255) & ~size_t(255);
+    if (bytes > left) {
+      const size_t size = bytes > kChunk ? bytes : kChunk;
+      void* c = nullptr;
+      cudaError_t e = cudaMallocAsync(&c, size, stream);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(MGCFD_ERR_NOMEM, std::string("setup scratch allocation failed: ") + cudaGetErrorString(e));
+      }
+      chunks.push_back(c);
+      cur = static_cast<char*>(c);
+      left = size;
     }
-    ptrs.push_back(*p);
+    *p = reinterpret_cast<X*>(cur);
+    cur += bytes;
+    left -= bytes;
+    return MGCFD_OK;
+  }
+};
+
+// Independent per-mesh setup work of a batch runs on up to kLanes streams,
+// so that the many small kernels of small meshes overlap; the level-wide
+// arrays are allocated on the solver's stream, which forks to the lanes and
+// joins them again.  One mesh: the solver's stream alone.
+struct Lanes {
+  static constexpr int kLanes = 8;
+  cudaStream_t main;
+  std::vector<cudaStream_t> streams;
+  std::vector<std::unique_ptr<Temp>> temps;
+  std::vector<cudaEvent_t> events;  // events[0]: fork point on main; events[1 + k]: lane k done
+  explicit Lanes(cudaStream_t m) : main(m) {}
+  ~Lanes() {
+    temps.clear();  // frees enqueued on the lanes
+    for (size_t k = 0; k < streams.size(); k++)
+      if (streams[k] != main) cudaStreamDestroy(streams[k]);
+    for (cudaEvent_t e : events) cudaEventDestroy(e);
+  }
+  int init(int nseg) {
+    const int k = nseg > 1 ? std::min(nseg, kLanes) : 1;
+    for (int i = 0; i < k; i++) {
+      cudaStream_t sm = main;
+      if (k > 1) CK(cudaStreamCreateWithFlags(&sm, cudaStreamNonBlocking));
+      streams.push_back(sm);
+      temps.emplace_back(new Temp(sm));
+    }
+    events.resize((size_t)k + 1);
+    for (auto& e : events) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    return MGCFD_OK;
+  }
+  cudaStream_t stream(int m) const { return streams[(size_t)m % streams.size()]; }
+  Temp& temp(int m) { return *temps[(size_t)m % temps.size()]; }
+  int fork() {
+    if (streams.size() < 2) return MGCFD_OK;
+    CK(cudaEventRecord(events[0], main));
+    for (cudaStream_t sm : streams) CK(cudaStreamWaitEvent(sm, events[0], 0));
+    return MGCFD_OK;
+  }
+  int join() {
+    if (streams.size() < 2) return MGCFD_OK;
+    for (size_t k = 0; k < streams.size(); k++) {
+      CK(cudaEventRecord(events[1 + k], streams[k]));
+      CK(cudaStreamWaitEvent(main, events[1 + k], 0));
+    }
     return MGCFD_OK;
   }
 };
@@ -259,7 +322,8 @@ __global__ void k_bnd_keys(int32_t nb, int32_t nn, const int32_t* __restrict__ b
 // Folded boundary rows (flux.h:14-39 is linear in the weight), entries in order.
 __global__ void k_bnd_fold(int32_t nn, const int32_t* __restrict__ off, const int32_t* __restrict__ entries,
                            const int32_t* __restrict__ grp, const double* __restrict__ bwt,
-                           const int32_t* __restrict__ row_of, int32_t row_off, mgcfd_freestream ff,
+                           const int32_t* __restrict__ row_of, const int32_t* __restrict__ row_base,
+                           mgcfd_freestream ff,
                            int32_t* __restrict__ bidx,
                            double* __restrict__ bdata) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -272,7 +336,7 @@ __global__ void k_bnd_fold(int32_t nn, const int32_t* __restrict__ off, const in
     double* dst = grp[k] <= 2 ? wwall : wff;
     for (int c = 0; c < 3; c++) dst[c] = __dadd_rn(dst[c], __dmul_rn(bwt[3 * (int64_t)k + c], 1e-7));
   }
-  const int32_t r = row_of[i] + row_off;
+  const int32_t r = row_of[i] + *row_base;
   bidx[i] = r;
   double* row = bdata + 12 * (int64_t)r;
   for (int c = 0; c < 3; c++) { row[c] = wff[c]; row[3 + c] = wwall[c]; }
@@ -284,6 +348,18 @@ __global__ void k_bnd_fold(int32_t nn, const int32_t* __restrict__ off, const in
     row[7 + q] = __dadd_rn(__dadd_rn(__dmul_rn(wff[0], rows[q][0]), __dmul_rn(wff[1], rows[q][1])),
                            __dmul_rn(wff[2], rows[q][2]));
   row[11] = 0.0;
+}
+
+__global__ void k_copy1(const int32_t* __restrict__ src, int32_t* __restrict__ dst) { *dst = *src; }
+
+// base[0] = 0, base[m + 1] = base[m] + count[m] for a handful of meshes.
+__global__ void k_exclusive_scan_small(int32_t n, const int32_t* __restrict__ count, int32_t* __restrict__ base) {
+  int32_t acc = 0;
+  base[0] = 0;
+  for (int32_t m = 0; m < n; m++) {
+    acc += count[m];
+    base[m + 1] = acc;
+  }
 }
 
 __global__ void k_nonempty(int32_t nn, const int32_t* __restrict__ off, int32_t* __restrict__ flag) {
@@ -352,6 +428,11 @@ struct LevelTmp {
   int32_t* inv = nullptr;   // local input id -> local new id
   double* xyz = nullptr;
   int32_t* n2mg_in = nullptr;
+  // the level's input arrays on the device
+  int32_t *e2n_in = nullptr, *b2n_in = nullptr, *grp_in = nullptr;
+  double *ewt_in = nullptr, *bwt_in = nullptr, *vol_in = nullptr;
+  // boundary fold inputs, kept for the fold pass after the lanes join
+  int32_t *b_off = nullptr, *b_entries = nullptr, *b_row = nullptr;
 };
 
 __global__ void k_offset_copy(int32_t n, const int32_t* __restrict__ src, int32_t add, int32_t* __restrict__ dst) {
@@ -369,6 +450,8 @@ __global__ void k_fill(int32_t n, int32_t value, int32_t* __restrict__ dst) {
 int device_prepare(mgcfd_solver* s, const std::vector<MeshInput>& meshes) {
   cudaStream_t st = s->stream;
   Temp tmp(st);
+  Lanes lanes(st);
+  if (int r0 = lanes.init((int)meshes.size())) return r0;
   unsigned* err = nullptr;
   int r = tmp.get(&err, 1);
   if (r) return r;
@@ -404,36 +487,53 @@ int device_prepare(mgcfd_solver* s, const std::vector<MeshInput>& meshes) {
                       (r = s->alloc(&D.b_list, (size_t)NE))))
       return r;
     if (nseg > 1 && (r = s->alloc(&D.mesh_id, (size_t)N))) return r;
-    int32_t row_off = 0;
+    // Folded boundary rows of mesh m start at row_base[m]; the offsets stay on
+    // the device, so the meshes' setup work is queued without host round trips.
+    int32_t *row_base, *rows_tot;
+    if ((r = tmp.get(&row_base, (size_t)nseg + 1)) || (r = tmp.get(&rows_tot, (size_t)nseg))) return r;
+    if ((r = lanes.fork())) return r;
+
+    // Upload every mesh's input arrays first: a copy from pageable host
+    // memory may wait for the stream, so the copies go ahead of the kernels.
+    for (int m = 0; m < nseg; m++) {
+      const cudaStream_t st = lanes.stream(m);
+      Temp& tmp = lanes.temp(m);
+      const mgcfd_level_view& v = meshes[(size_t)m].levels[l];
+      LevelTmp& T_ = lt[(size_t)m][(size_t)l];
+      const int32_t n = v.nnodes, ne = v.nedges, nb = v.nbnd;
+      if ((r = tmp.get(&T_.xyz, 3 * (size_t)n)) || (r = tmp.get(&T_.e2n_in, 2 * (size_t)ne)) ||
+          (r = tmp.get(&T_.ewt_in, 3 * (size_t)ne)) || (r = tmp.get(&T_.b2n_in, (size_t)nb)) ||
+          (r = tmp.get(&T_.grp_in, (size_t)nb)) || (r = tmp.get(&T_.bwt_in, 3 * (size_t)nb)) ||
+          (r = tmp.get(&T_.vol_in, (size_t)n)))
+        return r;
+      CK(cudaMemcpyAsync(T_.xyz, v.coords, 24 * (size_t)n, cudaMemcpyHostToDevice, st));
+      if (ne) {
+        CK(cudaMemcpyAsync(T_.e2n_in, v.edge_to_nodes, 8 * (size_t)ne, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(T_.ewt_in, v.edge_weights, 24 * (size_t)ne, cudaMemcpyHostToDevice, st));
+      }
+      if (nb) {
+        CK(cudaMemcpyAsync(T_.b2n_in, v.bnd_to_node, 4 * (size_t)nb, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(T_.grp_in, v.bnd_group, 4 * (size_t)nb, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(T_.bwt_in, v.bnd_weights, 24 * (size_t)nb, cudaMemcpyHostToDevice, st));
+      }
+      if (v.volumes) CK(cudaMemcpyAsync(T_.vol_in, v.volumes, 8 * (size_t)n, cudaMemcpyHostToDevice, st));
+      if (v.node_to_mg) {
+        if ((r = tmp.get(&T_.n2mg_in, (size_t)n))) return r;
+        CK(cudaMemcpyAsync(T_.n2mg_in, v.node_to_mg, 4 * (size_t)n, cudaMemcpyHostToDevice, st));
+      }
+    }
 
     for (int m = 0; m < nseg; m++) {
+      const cudaStream_t st = lanes.stream(m);
+      Temp& tmp = lanes.temp(m);
       const mgcfd_level_view& v = meshes[(size_t)m].levels[l];
       const mgcfd_freestream& ff = meshes[(size_t)m].ff;
       const double sc = ff.smoothing_coefficient;
       LevelTmp& T_ = lt[(size_t)m][(size_t)l];
       const int32_t n = v.nnodes, ne = v.nedges, nb = v.nbnd;
       const int32_t noff = s->seg_noff[(size_t)l][(size_t)m], eoff = seg_eoff[(size_t)l][(size_t)m];
-      // Upload the input arrays.
-      int32_t *e2n_in, *b2n_in, *grp_in;
-      double *ewt_in, *bwt_in;
-      if ((r = tmp.get(&T_.xyz, 3 * (size_t)n)) || (r = tmp.get(&e2n_in, 2 * (size_t)ne)) ||
-          (r = tmp.get(&ewt_in, 3 * (size_t)ne)) || (r = tmp.get(&b2n_in, (size_t)nb)) ||
-          (r = tmp.get(&grp_in, (size_t)nb)) || (r = tmp.get(&bwt_in, 3 * (size_t)nb)))
-        return r;
-      CK(cudaMemcpyAsync(T_.xyz, v.coords, 24 * (size_t)n, cudaMemcpyHostToDevice, st));
-      if (ne) {
-        CK(cudaMemcpyAsync(e2n_in, v.edge_to_nodes, 8 * (size_t)ne, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(ewt_in, v.edge_weights, 24 * (size_t)ne, cudaMemcpyHostToDevice, st));
-      }
-      if (nb) {
-        CK(cudaMemcpyAsync(b2n_in, v.bnd_to_node, 4 * (size_t)nb, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(grp_in, v.bnd_group, 4 * (size_t)nb, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(bwt_in, v.bnd_weights, 24 * (size_t)nb, cudaMemcpyHostToDevice, st));
-      }
-      if (v.node_to_mg) {
-        if ((r = tmp.get(&T_.n2mg_in, (size_t)n))) return r;
-        CK(cudaMemcpyAsync(T_.n2mg_in, v.node_to_mg, 4 * (size_t)n, cudaMemcpyHostToDevice, st));
-      }
+      const int32_t *e2n_in = T_.e2n_in, *b2n_in = T_.b2n_in, *grp_in = T_.grp_in;
+      const double *ewt_in = T_.ewt_in, *bwt_in = T_.bwt_in;
       if (nseg > 1) k_fill<<<nblk(n), T, 0, st>>>(n, m, D.mesh_id + noff);
 
       // Node order (local to the mesh).
@@ -456,13 +556,11 @@ int device_prepare(mgcfd_solver* s, const std::vector<MeshInput>& meshes) {
       k_offset_copy<<<nblk(n), T, 0, st>>>(n, T_.perm, noff, D.perm + noff);
 
       // Geometry and volumes.
-      double *tv, *wd, *vol_in;
-      if ((r = tmp.get(&tv, (size_t)ne)) || (r = tmp.get(&wd, 3 * (size_t)ne)) || (r = tmp.get(&vol_in, (size_t)n)))
-        return r;
+      double *tv, *wd;
+      double* vol_in = T_.vol_in;
+      if ((r = tmp.get(&tv, (size_t)ne)) || (r = tmp.get(&wd, 3 * (size_t)ne))) return r;
       if (ne) k_edge_geometry<<<nblk(ne), T, 0, st>>>(ne, n, e2n_in, T_.xyz, ewt_in, v.volumes != nullptr, tv, wd, err);
-      if (v.volumes) {
-        CK(cudaMemcpyAsync(vol_in, v.volumes, 8 * (size_t)n, cudaMemcpyHostToDevice, st));
-      } else {
+      if (!v.volumes) {
         int32_t *ikey, *ival, *ikey2, *ival2, *cnt, *off;
         if ((r = tmp.get(&ikey, 2 * (size_t)ne)) || (r = tmp.get(&ival, 2 * (size_t)ne)) ||
             (r = tmp.get(&ikey2, 2 * (size_t)ne)) || (r = tmp.get(&ival2, 2 * (size_t)ne)) ||
@@ -527,14 +625,25 @@ int device_prepare(mgcfd_solver* s, const std::vector<MeshInput>& meshes) {
         CK(cudaMemsetAsync(flag, 0, sizeof(int32_t) * ((size_t)n + 1), st));
         k_nonempty<<<nblk(n), T, 0, st>>>(n, off, flag);
         if ((r = offsets(tmp, flag, row, n, st))) return r;
-        k_bnd_fold<<<nblk(n), T, 0, st>>>(n, off, val2, grp_in, bwt_in, row, row_off, ff, D.bidx + noff, D.bdata);
-        int32_t rows = 0;
-        CK(cudaMemcpyAsync(&rows, row + n, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        row_off += rows;
+        k_copy1<<<1, 1, 0, st>>>(row + n, rows_tot + m);
+        T_.b_off = off;
+        T_.b_entries = val2;
+        T_.b_row = row;
       }
     }
-    D.nbrows = row_off;
+    // Row offsets of every mesh's folded boundary rows, then the fold.
+    if ((r = lanes.join())) return r;
+    k_exclusive_scan_small<<<1, 1, 0, st>>>(nseg, rows_tot, row_base);
+    if ((r = lanes.fork())) return r;
+    for (int m = 0; m < nseg; m++) {
+      const LevelTmp& T_ = lt[(size_t)m][(size_t)l];
+      const int32_t n = meshes[(size_t)m].levels[l].nnodes, noff = s->seg_noff[(size_t)l][(size_t)m];
+      k_bnd_fold<<<nblk(n), T, 0, lanes.stream(m)>>>(n, T_.b_off, T_.b_entries, T_.grp_in, T_.bwt_in, T_.b_row,
+                                                   row_base + m, meshes[(size_t)m].ff, D.bidx + noff, D.bdata);
+    }
+    if ((r = lanes.join())) return r;
+    CK(cudaMemcpyAsync(&D.nbrows, row_base + nseg, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
     if (s->gather) {
       k_fill<<<1, 1, 0, st>>>(1, NE, D.a_off + N);
       k_fill<<<1, 1, 0, st>>>(1, NE, D.b_off + N);
@@ -570,7 +679,10 @@ int device_prepare(mgcfd_solver* s, const std::vector<MeshInput>& meshes) {
         (r = s->alloc(&Cl.ch_off, (size_t)Cl.n + 1)) || (r = s->alloc(&Cl.ch_list, (size_t)F.n)))
       return r;
     Cl.nfine = F.n;
+    if ((r = lanes.fork())) return r;
     for (int m = 0; m < nseg; m++) {
+      const cudaStream_t st = lanes.stream(m);
+      Temp& tmp = lanes.temp(m);
       const int32_t nf = meshes[(size_t)m].levels[l].nnodes, nc = meshes[(size_t)m].levels[l + 1].nnodes;
       const int32_t noff_f = s->seg_noff[(size_t)l][(size_t)m], noff_c = s->seg_noff[(size_t)l + 1][(size_t)m];
       int32_t *key, *val, *key2, *cnt, *off, *list;
@@ -587,6 +699,7 @@ int device_prepare(mgcfd_solver* s, const std::vector<MeshInput>& meshes) {
       k_offset_copy<<<nblk(nf), T, 0, st>>>(nf, list, noff_f, Cl.ch_list + noff_f);
       k_offset_copy<<<nblk(nc), T, 0, st>>>(nc, off, noff_f, Cl.ch_off + noff_c);
     }
+    if ((r = lanes.join())) return r;
     k_fill<<<1, 1, 0, st>>>(1, F.n, Cl.ch_off + Cl.n);
   }
   CK(cudaGetLastError());

@@ -140,6 +140,13 @@ class Batch(Solver):
                                                      out.ctypes.data_as(_lib.c_double_p)))
         return out
 
+    def fetch_meshes(self, level: int, quantity: int = Q_VARIABLES):
+        """Every mesh's rows of one level with a single device-to-host copy:
+        a list of arrays (views into one buffer), in mesh order."""
+        whole = self.fetch(level, quantity)
+        bounds = np.cumsum([0] + [nn[level] for nn in self._mesh_nn])
+        return [whole[bounds[m]:bounds[m + 1]] for m in range(len(self._mesh_nn))]
+
     def mesh_status(self, mesh: int):
         """(status, rms_l0, density_rms_l0) of one mesh after synchronising."""
         rms, rho = C.c_double(), C.c_double()

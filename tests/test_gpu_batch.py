@@ -42,6 +42,8 @@ def test_batch_equals_individual_solves(meshes, increment):
     # the concatenated fetch is the meshes' rows in order
     whole = b.fetch(0)
     np.testing.assert_array_equal(whole[: meshes[0].level(0).nnodes], b.fetch_mesh(0, 0))
+    for m, rows in enumerate(b.fetch_meshes(1)):
+        np.testing.assert_array_equal(rows, b.fetch_mesh(m, 1))
 
 
 def test_failing_mesh_is_isolated(meshes):
