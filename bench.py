@@ -511,7 +511,7 @@ def run_rates(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
@@ -526,7 +526,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mode", default="plain", choices=["plain", "batch", "serve", "rates"])
     ap.add_argument("--batch-meshes", type=int, default=64)
-    ap.add_argument("--serve-requests", type=int, default=200)
+    ap.add_argument("--serve-requests", type=int, default=240)
     ap.add_argument("--serve-pool", type=int, default=24)
     ap.add_argument("--serve-rate-multiples", type=float, nargs="+", default=[0.5, 0.9, 2.0])
     ap.add_argument("--serve-slots", type=int, default=16)
