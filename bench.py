@@ -368,21 +368,27 @@ def run_batch(args):
             "unit": "solves/s", "higher_is_better": True, "n_gpus": 1, "data": "synthetic: seeded lattices",
             "config": {"workload": f"{nm} meshes, {total_nodes} level-0 nodes in total, sizes {sizes.min()}^3.."
                                    f"{sizes.max()}^3"}}
+    def timed(fn, **o):  # median wall time of `repeats` runs, and the last run's results
+        ts = []
+        for _ in range(repeats):
+            t0 = time.perf_counter()
+            outs = fn(**o)
+            ts.append(time.perf_counter() - t0)
+        return statistics.median(ts), outs
+
+    repeats = 3
     t0 = time.perf_counter()
     solve_sequential(precision="fp64")  # warm-up pass (pool, graphs, clocks)
     line["warmup_s"] = round(time.perf_counter() - t0, 3)
-    t0 = time.perf_counter()
-    seq = solve_sequential(precision="fp64")
-    t_seq = time.perf_counter() - t0
+    line["timing"] = f"median wall time of {repeats} runs, each from host meshes to level-0 results on the host"
+    t_seq, seq = timed(solve_sequential, precision="fp64")
     results = {"sequential_fp64": nm / t_seq}
     for prec in ("fp64", "mixed"):
         t0 = time.perf_counter()
         best, timings = autotune.tune_batch(meshes, machs, aoas, precision=prec)
         t_tune = time.perf_counter() - t0
         solve_batch(**best)
-        t0 = time.perf_counter()
-        outs = solve_batch(**best)
-        dt = time.perf_counter() - t0
+        dt, outs = timed(solve_batch, **best)
         results[f"batched_{prec}"] = nm / dt
         err = max(float(np.max(np.abs(a - b) / np.maximum(np.abs(b).max(axis=0), 1e-300))) for a, b in zip(outs, seq))
         line[f"batched_{prec}_tuning"] = {"chosen": best, "ms_per_cycle": {f"{k[0]}/{k[1]}": round(v, 3)
@@ -391,9 +397,8 @@ def run_batch(args):
         if prec == "mixed":  # the same batch with compensated FP32-pair node sums
             pair = dict(best, accumulation="pair32")
             solve_batch(**pair)
-            t0 = time.perf_counter()
-            outs = solve_batch(**pair)
-            results["batched_mixed_pair32"] = nm / (time.perf_counter() - t0)
+            dt, outs = timed(solve_batch, **pair)
+            results["batched_mixed_pair32"] = nm / dt
             line["batched_mixed_pair32_max_rel_err_vs_fp64_sequential"] = max(
                 float(np.max(np.abs(a - b) / np.maximum(np.abs(b).max(axis=0), 1e-300))) for a, b in zip(outs, seq))
     line["value"] = round(results["batched_fp64"], 3)

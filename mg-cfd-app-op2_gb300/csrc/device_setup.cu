@@ -10,11 +10,24 @@
 //   * edges oriented a < b and stably sorted by (a, b); CSR tables by counting
 //     and prefix sums;
 //   * boundary entries folded per node in entry order; multigrid tables.
+//
+// A batch of meshes is prepared as one: per level, the meshes' arrays are
+// concatenated (mesh m's nodes, edges and boundary entries start at its
+// segment offsets) and every kernel and sort runs once over the whole level.
+// Maps stay mesh-local in the input and become global by adding the mesh's
+// node offset; a kernel finds an element's mesh by binary search over the
+// offsets.  Sorting by global node ids equals sorting each mesh by its local
+// ids, because meshes occupy consecutive id ranges; the one per-mesh sort key,
+// the Morton code, is sorted first and then stably by mesh.  The tables of
+// mesh m are therefore those of mesh m prepared alone, shifted by its offsets.
+//
 // Every kernel that reads an input map checks the entry against the target
-// set size first; an out-of-range entry is recorded and skipped, and setup
-// fails with MGCFD_ERR_INVALID after the last kernel.
+// set size of its mesh first; an out-of-range entry is recorded and replaced
+// by an in-range one, and setup fails with MGCFD_ERR_INVALID after the last
+// kernel.
 #include <cub/cub.cuh>
 
+#include <climits>
 #include <cmath>
 #include <cstring>
 
@@ -34,9 +47,8 @@ int bits_for(int64_t n) {  // number of bits needed to hold values 0..n
   return b;
 }
 
-// Temporary device memory for the setup, freed (stream-ordered) at the end.
 // Setup scratch: a bump allocator over stream-ordered chunks of at least
-// 64 MiB, so that the many small temporaries of a setup cost a handful of
+// 64 MiB, so that the many temporaries of a setup cost a handful of
 // allocation calls.  Everything is released when the setup ends.
 struct Temp {
   static constexpr size_t kChunk = 64ull << 20;
@@ -72,52 +84,29 @@ struct Temp {
   }
 };
 
-// Independent per-mesh setup work of a batch runs on up to kLanes streams,
-// so that the many small kernels of small meshes overlap; the level-wide
-// arrays are allocated on the solver's stream, which forks to the lanes and
-// joins them again.  One mesh: the solver's stream alone.
-struct Lanes {
-  static constexpr int kLanes = 8;
-  cudaStream_t main;
-  std::vector<cudaStream_t> streams;
-  std::vector<std::unique_ptr<Temp>> temps;
-  std::vector<cudaEvent_t> events;  // events[0]: fork point on main; events[1 + k]: lane k done
-  explicit Lanes(cudaStream_t m) : main(m) {}
-  ~Lanes() {
-    temps.clear();  // frees enqueued on the lanes
-    for (size_t k = 0; k < streams.size(); k++)
-      if (streams[k] != main) cudaStreamDestroy(streams[k]);
-    for (cudaEvent_t e : events) cudaEventDestroy(e);
-  }
-  int init(int nseg) {
-    const int k = nseg > 1 ? std::min(nseg, kLanes) : 1;
-    for (int i = 0; i < k; i++) {
-      cudaStream_t sm = main;
-      if (k > 1) CK(cudaStreamCreateWithFlags(&sm, cudaStreamNonBlocking));
-      streams.push_back(sm);
-      temps.emplace_back(new Temp(sm));
-    }
-    events.resize((size_t)k + 1);
-    for (auto& e : events) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    return MGCFD_OK;
-  }
-  cudaStream_t stream(int m) const { return streams[(size_t)m % streams.size()]; }
-  Temp& temp(int m) { return *temps[(size_t)m % temps.size()]; }
-  int fork() {
-    if (streams.size() < 2) return MGCFD_OK;
-    CK(cudaEventRecord(events[0], main));
-    for (cudaStream_t sm : streams) CK(cudaStreamWaitEvent(sm, events[0], 0));
-    return MGCFD_OK;
-  }
-  int join() {
-    if (streams.size() < 2) return MGCFD_OK;
-    for (size_t k = 0; k < streams.size(); k++) {
-      CK(cudaEventRecord(events[1 + k], streams[k]));
-      CK(cudaStreamWaitEvent(main, events[1 + k], 0));
-    }
-    return MGCFD_OK;
-  }
+// Segment table of one level: offsets of each mesh's nodes, edges and
+// boundary entries ([nseg + 1] each), per-mesh flags and free streams.
+constexpr int32_t kHasVolumes = 1;  // the mesh came with volumes (legacy datasets)
+struct Seg {
+  int32_t nseg;
+  const int32_t* noff;
+  const int32_t* eoff;
+  const int32_t* boff;
+  const int32_t* flags;
+  const mgcfd_freestream* ff;
 };
+
+// The segment of global index i: the largest m with off[m] <= i.  Segments
+// may be empty (edges, boundary entries); i is below off[nseg].
+__device__ __forceinline__ int32_t seg_of(const int32_t* __restrict__ off, int32_t nseg, int64_t i) {
+  int32_t lo = 0, hi = nseg - 1;
+  while (lo < hi) {
+    const int32_t mid = (lo + hi + 1) >> 1;
+    if (off[mid] <= i) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
 
 __device__ __forceinline__ bool ok_index(int32_t i, int32_t n, unsigned* err) {
   if ((uint32_t)i < (uint32_t)n) return true;
@@ -125,23 +114,37 @@ __device__ __forceinline__ bool ok_index(int32_t i, int32_t n, unsigned* err) {
   return false;
 }
 
+// out[i] = segment of (idx ? idx[i] : i).
+__global__ void k_seg_of(int32_t n, const int32_t* __restrict__ off, int32_t nseg, const int32_t* __restrict__ idx,
+                         int32_t* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = seg_of(off, nseg, idx ? idx[i] : i);
+}
+
 // ---- node order -------------------------------------------------------------
 
-__global__ void k_bbox(int32_t n, const double* __restrict__ xyz, unsigned long long* __restrict__ box) {
-  __shared__ unsigned long long lo[3], hi[3];
-  if (threadIdx.x < 3) { lo[threadIdx.x] = ~0ull; hi[threadIdx.x] = 0ull; }
-  __syncthreads();
+// Per-mesh bounding boxes as ordered keys: lo[3m + d], hi[3m + d].  A warp
+// whose nodes share one mesh reduces first and updates once.
+__global__ void k_bbox(int32_t n, const double* __restrict__ xyz, Seg g, unsigned long long* __restrict__ lo,
+                       unsigned long long* __restrict__ hi) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n)
-    for (int d = 0; d < 3; d++) {
-      const unsigned long long k = dkey(xyz[3 * i + d]);
-      atomicMin(&lo[d], k);
-      atomicMax(&hi[d], k);
+  const bool in = i < n;
+  const int32_t m = in ? seg_of(g.noff, g.nseg, i) : -1;
+  const int32_t m0 = __shfl_sync(0xffffffffu, m, 0);
+  const bool uniform = __all_sync(0xffffffffu, m == m0 || m < 0);
+  for (int d = 0; d < 3; d++) {
+    const unsigned long long k = in ? dkey(xyz[3 * i + d]) : 0ull;
+    if (uniform) {
+      const unsigned long long kmin = warp_min_u64(in ? k : ~0ull);
+      const unsigned long long kmax = ~warp_min_u64(in ? ~k : ~0ull);
+      if ((threadIdx.x & 31) == 0 && m0 >= 0) {
+        atomicMin(&lo[3 * m0 + d], kmin);
+        atomicMax(&hi[3 * m0 + d], kmax);
+      }
+    } else if (in) {
+      atomicMin(&lo[3 * m + d], k);
+      atomicMax(&hi[3 * m + d], k);
     }
-  __syncthreads();
-  if (threadIdx.x < 3) {
-    atomicMin(&box[threadIdx.x], lo[threadIdx.x]);
-    atomicMax(&box[3 + threadIdx.x], hi[threadIdx.x]);
   }
 }
 
@@ -155,17 +158,20 @@ __device__ __forceinline__ uint64_t spread3(uint64_t x) {
   return x;
 }
 
-// Same quantisation as spatial_order() in setup.cpp.
-__global__ void k_morton(int32_t n, const double* __restrict__ xyz, const unsigned long long* __restrict__ box,
-                         unsigned long long* __restrict__ key, int32_t* __restrict__ val) {
+// Same quantisation as spatial_order() in setup.cpp, against the node's own
+// mesh's box.
+__global__ void k_morton(int32_t n, const double* __restrict__ xyz, Seg g, const unsigned long long* __restrict__ lo,
+                         const unsigned long long* __restrict__ hi, unsigned long long* __restrict__ key,
+                         int32_t* __restrict__ val) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  const int32_t m = seg_of(g.noff, g.nseg, i);
   uint64_t q[3];
   for (int d = 0; d < 3; d++) {
-    const double lo = dkey_inv(box[d]), hi = dkey_inv(box[3 + d]);
-    const double span = __dsub_rn(hi, lo);
-    const double scale = (hi > lo && isfinite(span)) ? __ddiv_rn(2097151.0, span) : 0.0;
-    double t = __dmul_rn(__dsub_rn(xyz[3 * i + d], lo), scale);
+    const double a = dkey_inv(lo[3 * m + d]), b = dkey_inv(hi[3 * m + d]);
+    const double span = __dsub_rn(b, a);
+    const double scale = (b > a && isfinite(span)) ? __ddiv_rn(2097151.0, span) : 0.0;
+    double t = __dmul_rn(__dsub_rn(xyz[3 * i + d], a), scale);
     if (!(t > 0.0)) t = 0.0;
     if (t > 2097151.0) t = 2097151.0;
     q[d] = (uint64_t)t;
@@ -190,20 +196,27 @@ __device__ __forceinline__ double sq3(double a, double b, double c) {
   return __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), __dmul_rn(c, c));
 }
 
-__global__ void k_edge_geometry(int32_t ne, int32_t nn, const int32_t* __restrict__ e2n,
-                                const double* __restrict__ xyz, const double* __restrict__ ewt_in, int legacy,
+// Per edge: global input end nodes (-1 where the entry is out of range),
+// volume contribution tv and damped weights w.
+__global__ void k_edge_geometry(int32_t ne, Seg g, const int32_t* __restrict__ e2n, const double* __restrict__ xyz,
+                                const double* __restrict__ ewt_in, int32_t* __restrict__ ge2n,
                                 double* __restrict__ tv, double* __restrict__ w, unsigned* __restrict__ err) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= ne) return;
-  const int32_t a = e2n[2 * e], b = e2n[2 * e + 1];
+  const int32_t m = seg_of(g.eoff, g.nseg, e);
+  const int32_t base = g.noff[m], nn = g.noff[m + 1] - base;
+  const int32_t la = e2n[2 * e], lb = e2n[2 * e + 1];
+  const bool va = ok_index(la, nn, err), vb = ok_index(lb, nn, err);
+  const int32_t a = va ? base + la : -1, b = vb ? base + lb : -1;
+  ge2n[2 * e] = a;
+  ge2n[2 * e + 1] = b;
   const double* wi = ewt_in + 3 * e;
-  if (legacy) {  // weights used as read (euler3d.cpp:416-431 skipped)
+  if (g.flags[m] & kHasVolumes) {  // weights used as read (euler3d.cpp:416-431 skipped)
+    tv[e] = 0.0;
     for (int i = 0; i < 3; i++) w[3 * e + i] = __dmul_rn(wi[i], 1e-7);
-    ok_index(a, nn, err);
-    ok_index(b, nn, err);
     return;
   }
-  if (!ok_index(a, nn, err) || !ok_index(b, nn, err)) {
+  if (!va || !vb) {
     tv[e] = 0.0;
     for (int i = 0; i < 3; i++) w[3 * e + i] = 0.0;
     return;
@@ -218,23 +231,25 @@ __global__ void k_edge_geometry(int32_t ne, int32_t nn, const int32_t* __restric
 
 // Incidence pairs (node, edge) in edge order; a stable sort by node keeps
 // each node's edges in increasing id.
-__global__ void k_incidence(int32_t ne, int32_t nn, const int32_t* __restrict__ e2n, int32_t* __restrict__ key,
+__global__ void k_incidence(int32_t ne, int32_t nn, const int32_t* __restrict__ ge2n, int32_t* __restrict__ key,
                             int32_t* __restrict__ val, int32_t* __restrict__ cnt) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= ne) return;
   for (int k = 0; k < 2; k++) {
-    int32_t v = e2n[2 * e + k];
-    if ((uint32_t)v >= (uint32_t)nn) v = nn;  // sentinel: sorts last, never summed
+    int32_t v = ge2n[2 * e + k];
+    if (v < 0) v = nn;  // sentinel: sorts last, never summed
     key[2 * e + k] = v;
     val[2 * e + k] = (int32_t)e;
     if (v < nn) atomicAdd(cnt + v, 1);
   }
 }
 
-__global__ void k_volumes(int32_t nn, const int32_t* __restrict__ off, const int32_t* __restrict__ edges,
+// Volumes of the meshes that came without them, at input node ids.
+__global__ void k_volumes(int32_t nn, Seg g, const int32_t* __restrict__ off, const int32_t* __restrict__ edges,
                           const double* __restrict__ tv, double* __restrict__ vol) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nn) return;
+  if (g.flags[seg_of(g.noff, g.nseg, i)] & kHasVolumes) return;
   double v = 0.0;  // zero_1d_array_kernel, then OP_INC in edge order
   for (int32_t j = off[i]; j < off[i + 1]; j++) v = __dadd_rn(v, tv[edges[j]]);
   vol[i] = v;
@@ -253,14 +268,14 @@ __global__ void k_node_constants(int32_t nn, const int32_t* __restrict__ perm, c
 
 // ---- edges -------------------------------------------------------------------
 
-__global__ void k_edge_keys(int32_t ne, int32_t nn, const int32_t* __restrict__ e2n, const int32_t* __restrict__ inv,
+__global__ void k_edge_keys(int32_t ne, const int32_t* __restrict__ ge2n, const int32_t* __restrict__ inv,
                             unsigned long long* __restrict__ key, int32_t* __restrict__ val,
                             unsigned char* __restrict__ flip) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= ne) return;
-  int32_t a = e2n[2 * e], b = e2n[2 * e + 1];
-  a = (uint32_t)a < (uint32_t)nn ? inv[a] : 0;  // out-of-range maps were recorded by k_edge_geometry
-  b = (uint32_t)b < (uint32_t)nn ? inv[b] : 0;
+  int32_t a = ge2n[2 * e], b = ge2n[2 * e + 1];
+  a = a >= 0 ? inv[a] : 0;  // out-of-range maps were recorded by k_edge_geometry
+  b = b >= 0 ? inv[b] : 0;
   const bool f = a > b;
   const uint32_t lo = f ? b : a, hi = f ? a : b;
   key[e] = ((unsigned long long)lo << 32) | hi;
@@ -268,15 +283,16 @@ __global__ void k_edge_keys(int32_t ne, int32_t nn, const int32_t* __restrict__ 
   flip[e] = f;
 }
 
-__global__ void k_edge_finalize(int32_t ne, int32_t node_off, const unsigned long long* __restrict__ key,
+__global__ void k_edge_finalize(int32_t ne, Seg g, const unsigned long long* __restrict__ key,
                                 const int32_t* __restrict__ order, const double* __restrict__ w,
-                                const unsigned char* __restrict__ flip, double sc, int2* __restrict__ e2n,
+                                const unsigned char* __restrict__ flip, int2* __restrict__ e2n,
                                 double* __restrict__ w4, int32_t* __restrict__ acnt, int32_t* __restrict__ bcnt) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= ne) return;
   const int64_t e = order[k];
+  const double sc = g.ff[seg_of(g.eoff, g.nseg, e)].smoothing_coefficient;
   const int32_t a = (int32_t)(key[k] >> 32), b = (int32_t)(key[k] & 0xffffffffu);
-  e2n[k] = make_int2(a + node_off, b + node_off);
+  e2n[k] = make_int2(a, b);
   double x = w[3 * e], y = w[3 * e + 1], z = w[3 * e + 2];
   if (flip[e]) { x = -x; y = -y; z = -z; }
   const double mag = __dsqrt_rn(sq3(x, y, z));
@@ -288,11 +304,11 @@ __global__ void k_edge_finalize(int32_t ne, int32_t node_off, const unsigned lon
   atomicAdd(bcnt + b, 1);
 }
 
-__global__ void k_b_pairs(int32_t ne, const int2* __restrict__ e2n, int32_t node_off, int32_t* __restrict__ key,
+__global__ void k_b_pairs(int32_t ne, const int2* __restrict__ e2n, int32_t* __restrict__ key,
                           int32_t* __restrict__ val) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= ne) return;
-  key[k] = e2n[k].y - node_off;
+  key[k] = e2n[k].y;
   val[k] = (int32_t)k;
 }
 
@@ -303,16 +319,19 @@ __global__ void k_to_float(int64_t n, const double* __restrict__ x, float* __res
 
 // ---- boundary -----------------------------------------------------------------
 
-__global__ void k_bnd_keys(int32_t nb, int32_t nn, const int32_t* __restrict__ b2n, const int32_t* __restrict__ grp,
-                           const int32_t* __restrict__ inv, int32_t* __restrict__ key, int32_t* __restrict__ val,
-                           int32_t* __restrict__ cnt, unsigned* __restrict__ err) {
+__global__ void k_bnd_keys(int32_t nb, int32_t nn, Seg g, const int32_t* __restrict__ b2n,
+                           const int32_t* __restrict__ grp, const int32_t* __restrict__ inv,
+                           int32_t* __restrict__ key, int32_t* __restrict__ val, int32_t* __restrict__ cnt,
+                           unsigned* __restrict__ err) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= nb) return;
+  const int32_t m = seg_of(g.boff, g.nseg, k);
+  const int32_t base = g.noff[m];
   const int32_t n = b2n[k];
-  const int g = grp[k];
+  const int gr = grp[k];
   int32_t node = nn;  // sentinel: ignored entry
-  if (ok_index(n, nn, err) && g <= 7) {
-    node = inv[n];
+  if (ok_index(n, g.noff[m + 1] - base, err) && gr <= 7) {
+    node = inv[base + n];
     atomicAdd(cnt + node, 1);
   }
   key[k] = node;
@@ -320,11 +339,9 @@ __global__ void k_bnd_keys(int32_t nb, int32_t nn, const int32_t* __restrict__ b
 }
 
 // Folded boundary rows (flux.h:14-39 is linear in the weight), entries in order.
-__global__ void k_bnd_fold(int32_t nn, const int32_t* __restrict__ off, const int32_t* __restrict__ entries,
+__global__ void k_bnd_fold(int32_t nn, Seg g, const int32_t* __restrict__ off, const int32_t* __restrict__ entries,
                            const int32_t* __restrict__ grp, const double* __restrict__ bwt,
-                           const int32_t* __restrict__ row_of, const int32_t* __restrict__ row_base,
-                           mgcfd_freestream ff,
-                           int32_t* __restrict__ bidx,
+                           const int32_t* __restrict__ row_of, int32_t* __restrict__ bidx,
                            double* __restrict__ bdata) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nn) return;
@@ -336,10 +353,11 @@ __global__ void k_bnd_fold(int32_t nn, const int32_t* __restrict__ off, const in
     double* dst = grp[k] <= 2 ? wwall : wff;
     for (int c = 0; c < 3; c++) dst[c] = __dadd_rn(dst[c], __dmul_rn(bwt[3 * (int64_t)k + c], 1e-7));
   }
-  const int32_t r = row_of[i] + *row_base;
+  const int32_t r = row_of[i];
   bidx[i] = r;
   double* row = bdata + 12 * (int64_t)r;
   for (int c = 0; c < 3; c++) { row[c] = wff[c]; row[3 + c] = wwall[c]; }
+  const mgcfd_freestream& ff = g.ff[seg_of(g.noff, g.nseg, i)];
   const double* fv = ff.ff_variable;
   const double* rows[4] = {ff.ff_flux_contribution_momentum_x, ff.ff_flux_contribution_momentum_y,
                            ff.ff_flux_contribution_momentum_z, ff.ff_flux_contribution_density_energy};
@@ -350,17 +368,7 @@ __global__ void k_bnd_fold(int32_t nn, const int32_t* __restrict__ off, const in
   row[11] = 0.0;
 }
 
-__global__ void k_copy1(const int32_t* __restrict__ src, int32_t* __restrict__ dst) { *dst = *src; }
-
-// base[0] = 0, base[m + 1] = base[m] + count[m] for a handful of meshes.
-__global__ void k_exclusive_scan_small(int32_t n, const int32_t* __restrict__ count, int32_t* __restrict__ base) {
-  int32_t acc = 0;
-  base[0] = 0;
-  for (int32_t m = 0; m < n; m++) {
-    acc += count[m];
-    base[m + 1] = acc;
-  }
-}
+__global__ void k_copy1(const int32_t* __restrict__ src, unsigned* __restrict__ dst) { *dst = (unsigned)*src; }
 
 __global__ void k_nonempty(int32_t nn, const int32_t* __restrict__ off, int32_t* __restrict__ flag) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -369,24 +377,30 @@ __global__ void k_nonempty(int32_t nn, const int32_t* __restrict__ off, int32_t*
 
 // ---- multigrid ----------------------------------------------------------------
 
-__global__ void k_mg(int32_t nf, int32_t nc, int32_t coarse_off, const int32_t* __restrict__ perm_f,
-                     const int32_t* __restrict__ n2mg_in,
+// Fine node f (new global id) of mesh m: its coarse node (new global id),
+// the distance vector to it (mg.h:76) and a (coarse, fine) pair for the
+// child lists.
+__global__ void k_mg(int32_t nf, int32_t nseg, const int32_t* __restrict__ noff_f, const int32_t* __restrict__ noff_c,
+                     const int32_t* __restrict__ perm_f, const int32_t* __restrict__ n2mg_in,
                      const int32_t* __restrict__ inv_c, const double* __restrict__ xf, const double* __restrict__ xc,
                      int32_t* __restrict__ n2mg, double* __restrict__ dvec, int32_t* __restrict__ key,
                      int32_t* __restrict__ val, int32_t* __restrict__ cnt, unsigned* __restrict__ err) {
   const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nf) return;
+  const int32_t m = seg_of(noff_f, nseg, f);
+  const int32_t cbase = noff_c[m];
   const int32_t fin = perm_f[f];
   const int32_t cin = n2mg_in[fin];
-  int32_t c = 0;
+  int32_t c = cbase;
   double dx = 0.0, dy = 0.0, dz = 0.0;
-  if (ok_index(cin, nc, err)) {
-    c = inv_c[cin];
-    dx = fabs(__dsub_rn(xf[3 * (int64_t)fin], xc[3 * (int64_t)cin]));
-    dy = fabs(__dsub_rn(xf[3 * (int64_t)fin + 1], xc[3 * (int64_t)cin + 1]));
-    dz = fabs(__dsub_rn(xf[3 * (int64_t)fin + 2], xc[3 * (int64_t)cin + 2]));
+  if (ok_index(cin, noff_c[m + 1] - cbase, err)) {
+    const int64_t cg = (int64_t)cbase + cin;
+    c = inv_c[cg];
+    dx = fabs(__dsub_rn(xf[3 * (int64_t)fin], xc[3 * cg]));
+    dy = fabs(__dsub_rn(xf[3 * (int64_t)fin + 1], xc[3 * cg + 1]));
+    dz = fabs(__dsub_rn(xf[3 * (int64_t)fin + 2], xc[3 * cg + 2]));
   }
-  n2mg[f] = c + coarse_off;
+  n2mg[f] = c;
   dvec[4 * f + 0] = dx;
   dvec[4 * f + 1] = dy;
   dvec[4 * f + 2] = dz;
@@ -422,59 +436,102 @@ int offsets(Temp& tmp, int32_t* cnt, int32_t* off, int64_t n, cudaStream_t s) {
   return MGCFD_OK;
 }
 
-// Per mesh and level: the arrays kept until the multigrid tables are built.
-struct LevelTmp {
-  int32_t* perm = nullptr;  // local new id -> local input id
-  int32_t* inv = nullptr;   // local input id -> local new id
-  double* xyz = nullptr;
-  int32_t* n2mg_in = nullptr;
-  // the level's input arrays on the device
-  int32_t *e2n_in = nullptr, *b2n_in = nullptr, *grp_in = nullptr;
-  double *ewt_in = nullptr, *bwt_in = nullptr, *vol_in = nullptr;
-  // boundary fold inputs, kept for the fold pass after the lanes join
-  int32_t *b_off = nullptr, *b_entries = nullptr, *b_row = nullptr;
+// One level's input arrays on the device, the meshes concatenated.
+struct LevelIn {
+  double *xyz = nullptr, *ewt = nullptr, *bwt = nullptr, *vol = nullptr;
+  int32_t *e2n = nullptr, *b2n = nullptr, *grp = nullptr, *n2mg = nullptr;
+  int32_t* inv = nullptr;  // input node id -> new node id (global)
 };
-
-__global__ void k_offset_copy(int32_t n, const int32_t* __restrict__ src, int32_t add, int32_t* __restrict__ dst) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) dst[i] = src[i] + add;
-}
-
-__global__ void k_fill(int32_t n, int32_t value, int32_t* __restrict__ dst) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) dst[i] = value;
-}
 
 }  // namespace
 
 int device_prepare(mgcfd_solver* s, const std::vector<MeshInput>& meshes) {
   cudaStream_t st = s->stream;
   Temp tmp(st);
-  Lanes lanes(st);
-  if (int r0 = lanes.init((int)meshes.size())) return r0;
-  unsigned* err = nullptr;
-  int r = tmp.get(&err, 1);
-  if (r) return r;
-  CK(cudaMemsetAsync(err, 0, sizeof(unsigned), st));
   const bool mixed = s->opt.precision == MGCFD_PRECISION_MIXED;
   const int nseg = (int)meshes.size();
   const int nlevels = (int)s->L.size();
-  std::vector<std::vector<LevelTmp>> lt((size_t)nseg, std::vector<LevelTmp>((size_t)nlevels));
+  int r;
+
+  // Segment tables, checked to fit the 32-bit ids (incidence pairs: 2 per edge).
+  const size_t per = 4 * (size_t)nseg + 3;  // noff | eoff | boff | flags
+  std::vector<int32_t> meta(per * (size_t)nlevels, 0);
   s->seg_noff.assign((size_t)nlevels, std::vector<int32_t>((size_t)nseg + 1, 0));
-  std::vector<std::vector<int32_t>> seg_eoff((size_t)nlevels, std::vector<int32_t>((size_t)nseg + 1, 0));
-  for (int l = 0; l < nlevels; l++)
+  bool any_computed_volumes = false;
+  for (int l = 0; l < nlevels; l++) {
+    int32_t* M = meta.data() + per * (size_t)l;
+    int64_t n = 0, ne = 0, nb = 0;
     for (int m = 0; m < nseg; m++) {
       const mgcfd_level_view& v = meshes[(size_t)m].levels[l];
-      s->seg_noff[(size_t)l][(size_t)m + 1] = s->seg_noff[(size_t)l][(size_t)m] + v.nnodes;
-      seg_eoff[(size_t)l][(size_t)m + 1] = seg_eoff[(size_t)l][(size_t)m] + v.nedges;
+      n += v.nnodes; ne += v.nedges; nb += v.nbnd;
+      if (n >= INT32_MAX || 2 * ne >= INT32_MAX || nb >= INT32_MAX)
+        return set_error(MGCFD_ERR_INVALID, "level " + std::to_string(l) + ": more than 2^31 nodes, "
+                                            "2^30 edges or 2^31 boundary entries in one solver");
+      M[m + 1] = (int32_t)n;
+      M[nseg + 1 + m + 1] = (int32_t)ne;
+      M[2 * (nseg + 1) + m + 1] = (int32_t)nb;
+      M[3 * (nseg + 1) + m] = v.volumes ? kHasVolumes : 0;
+      any_computed_volumes |= !v.volumes;
+      s->seg_noff[(size_t)l][(size_t)m + 1] = (int32_t)n;
     }
+  }
+  std::vector<mgcfd_freestream> ffs((size_t)nseg);
+  for (int m = 0; m < nseg; m++) ffs[(size_t)m] = meshes[(size_t)m].ff;
+  int32_t* dmeta;
+  mgcfd_freestream* dff;
+  unsigned* fin;  // fin[0]: out-of-range map entries; fin[1 + l]: folded boundary rows of level l
+  if ((r = tmp.get(&dmeta, meta.size())) || (r = tmp.get(&dff, (size_t)nseg)) ||
+      (r = tmp.get(&fin, 1 + (size_t)nlevels)))
+    return r;
+  unsigned* err = fin;
+  CK(cudaMemcpyAsync(dmeta, meta.data(), 4 * meta.size(), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(dff, ffs.data(), sizeof(mgcfd_freestream) * (size_t)nseg, cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(fin, 0, sizeof(unsigned) * (1 + (size_t)nlevels), st));
+  auto seg = [&](int l) {
+    const int32_t* M = dmeta + per * (size_t)l;
+    return Seg{nseg, M, M + (nseg + 1), M + 2 * (nseg + 1), M + 3 * (nseg + 1), dff};
+  };
+  auto total = [&](int l, int which) { return meta[per * (size_t)l + (size_t)which * (nseg + 1) + (size_t)nseg]; };
+
+  // Upload every level's inputs before the first kernel: a copy from pageable
+  // host memory may wait for the work queued ahead of it on the stream.
+  std::vector<LevelIn> in((size_t)nlevels);
+  for (int l = 0; l < nlevels; l++) {
+    LevelIn& I = in[(size_t)l];
+    const int32_t N = total(l, 0), NE = total(l, 1), NB = total(l, 2);
+    if ((r = tmp.get(&I.xyz, 3 * (size_t)N)) || (r = tmp.get(&I.e2n, 2 * (size_t)NE)) ||
+        (r = tmp.get(&I.ewt, 3 * (size_t)NE)) || (r = tmp.get(&I.b2n, (size_t)NB)) ||
+        (r = tmp.get(&I.grp, (size_t)NB)) || (r = tmp.get(&I.bwt, 3 * (size_t)NB)) ||
+        (r = tmp.get(&I.vol, (size_t)N)) || (r = tmp.get(&I.inv, (size_t)N)) ||
+        (l + 1 < nlevels && (r = tmp.get(&I.n2mg, (size_t)N))))
+      return r;
+    for (int m = 0; m < nseg; m++) {
+      const mgcfd_level_view& v = meshes[(size_t)m].levels[l];
+      const int64_t noff = s->seg_noff[(size_t)l][(size_t)m];
+      const int64_t eoff = meta[per * (size_t)l + (size_t)(nseg + 1) + (size_t)m];
+      const int64_t boff = meta[per * (size_t)l + 2 * (size_t)(nseg + 1) + (size_t)m];
+      CK(cudaMemcpyAsync(I.xyz + 3 * noff, v.coords, 24 * (size_t)v.nnodes, cudaMemcpyHostToDevice, st));
+      if (v.nedges) {
+        CK(cudaMemcpyAsync(I.e2n + 2 * eoff, v.edge_to_nodes, 8 * (size_t)v.nedges, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(I.ewt + 3 * eoff, v.edge_weights, 24 * (size_t)v.nedges, cudaMemcpyHostToDevice, st));
+      }
+      if (v.nbnd) {
+        CK(cudaMemcpyAsync(I.b2n + boff, v.bnd_to_node, 4 * (size_t)v.nbnd, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(I.grp + boff, v.bnd_group, 4 * (size_t)v.nbnd, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(I.bwt + 3 * boff, v.bnd_weights, 24 * (size_t)v.nbnd, cudaMemcpyHostToDevice, st));
+      }
+      if (v.volumes) CK(cudaMemcpyAsync(I.vol + noff, v.volumes, 8 * (size_t)v.nnodes, cudaMemcpyHostToDevice, st));
+      if (I.n2mg)
+        CK(cudaMemcpyAsync(I.n2mg + noff, v.node_to_mg, 4 * (size_t)v.nnodes, cudaMemcpyHostToDevice, st));
+    }
+  }
 
   for (int l = 0; l < nlevels; l++) {
     DevLevel& D = s->L[(size_t)l];
-    const int32_t N = s->seg_noff[(size_t)l][(size_t)nseg], NE = seg_eoff[(size_t)l][(size_t)nseg];
-    int64_t NB = 0;
-    for (int m = 0; m < nseg; m++) NB += meshes[(size_t)m].levels[l].nbnd;
-    D.n = N; D.ne = NE; D.nb = (int32_t)NB;
+    LevelIn& I = in[(size_t)l];
+    const Seg g = seg(l);
+    const int32_t N = total(l, 0), NE = total(l, 1), NB = total(l, 2);
+    D.n = N; D.ne = NE; D.nb = NB;
     if ((r = s->alloc(&D.perm, (size_t)N)) || (r = s->alloc(&D.vol, (size_t)N)) ||
         (r = s->alloc(&D.inv_vol, (size_t)N)) || (r = s->alloc(&D.cbrt_vol, (size_t)N)) ||
         (r = s->alloc(&D.e2n, (size_t)NE)) || (r = s->alloc(&D.bidx, (size_t)N)) ||
@@ -486,167 +543,104 @@ int device_prepare(mgcfd_solver* s, const std::vector<MeshInput>& meshes) {
     if (s->gather && ((r = s->alloc(&D.a_off, (size_t)N + 1)) || (r = s->alloc(&D.b_off, (size_t)N + 1)) ||
                       (r = s->alloc(&D.b_list, (size_t)NE))))
       return r;
-    if (nseg > 1 && (r = s->alloc(&D.mesh_id, (size_t)N))) return r;
-    // Folded boundary rows of mesh m start at row_base[m]; the offsets stay on
-    // the device, so the meshes' setup work is queued without host round trips.
-    int32_t *row_base, *rows_tot;
-    if ((r = tmp.get(&row_base, (size_t)nseg + 1)) || (r = tmp.get(&rows_tot, (size_t)nseg))) return r;
-    if ((r = lanes.fork())) return r;
+    if (nseg > 1) {
+      if ((r = s->alloc(&D.mesh_id, (size_t)N))) return r;
+      k_seg_of<<<nblk(N), T, 0, st>>>(N, g.noff, nseg, nullptr, D.mesh_id);
+    }
 
-    // Upload every mesh's input arrays first: a copy from pageable host
-    // memory may wait for the stream, so the copies go ahead of the kernels.
-    for (int m = 0; m < nseg; m++) {
-      const cudaStream_t st = lanes.stream(m);
-      Temp& tmp = lanes.temp(m);
-      const mgcfd_level_view& v = meshes[(size_t)m].levels[l];
-      LevelTmp& T_ = lt[(size_t)m][(size_t)l];
-      const int32_t n = v.nnodes, ne = v.nedges, nb = v.nbnd;
-      if ((r = tmp.get(&T_.xyz, 3 * (size_t)n)) || (r = tmp.get(&T_.e2n_in, 2 * (size_t)ne)) ||
-          (r = tmp.get(&T_.ewt_in, 3 * (size_t)ne)) || (r = tmp.get(&T_.b2n_in, (size_t)nb)) ||
-          (r = tmp.get(&T_.grp_in, (size_t)nb)) || (r = tmp.get(&T_.bwt_in, 3 * (size_t)nb)) ||
-          (r = tmp.get(&T_.vol_in, (size_t)n)))
+    // Node order: Morton codes within each mesh, then stably by mesh.
+    if (s->opt.renumber == MGCFD_RENUMBER_SPATIAL) {
+      unsigned long long *lo, *hi, *key, *key2;
+      int32_t *val, *val2;
+      if ((r = tmp.get(&lo, 3 * (size_t)nseg)) || (r = tmp.get(&hi, 3 * (size_t)nseg)) ||
+          (r = tmp.get(&key, (size_t)N)) || (r = tmp.get(&key2, (size_t)N)) || (r = tmp.get(&val, (size_t)N)) ||
+          (r = tmp.get(&val2, (size_t)N)))
         return r;
-      CK(cudaMemcpyAsync(T_.xyz, v.coords, 24 * (size_t)n, cudaMemcpyHostToDevice, st));
-      if (ne) {
-        CK(cudaMemcpyAsync(T_.e2n_in, v.edge_to_nodes, 8 * (size_t)ne, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(T_.ewt_in, v.edge_weights, 24 * (size_t)ne, cudaMemcpyHostToDevice, st));
-      }
-      if (nb) {
-        CK(cudaMemcpyAsync(T_.b2n_in, v.bnd_to_node, 4 * (size_t)nb, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(T_.grp_in, v.bnd_group, 4 * (size_t)nb, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(T_.bwt_in, v.bnd_weights, 24 * (size_t)nb, cudaMemcpyHostToDevice, st));
-      }
-      if (v.volumes) CK(cudaMemcpyAsync(T_.vol_in, v.volumes, 8 * (size_t)n, cudaMemcpyHostToDevice, st));
-      if (v.node_to_mg) {
-        if ((r = tmp.get(&T_.n2mg_in, (size_t)n))) return r;
-        CK(cudaMemcpyAsync(T_.n2mg_in, v.node_to_mg, 4 * (size_t)n, cudaMemcpyHostToDevice, st));
-      }
-    }
-
-    for (int m = 0; m < nseg; m++) {
-      const cudaStream_t st = lanes.stream(m);
-      Temp& tmp = lanes.temp(m);
-      const mgcfd_level_view& v = meshes[(size_t)m].levels[l];
-      const mgcfd_freestream& ff = meshes[(size_t)m].ff;
-      const double sc = ff.smoothing_coefficient;
-      LevelTmp& T_ = lt[(size_t)m][(size_t)l];
-      const int32_t n = v.nnodes, ne = v.nedges, nb = v.nbnd;
-      const int32_t noff = s->seg_noff[(size_t)l][(size_t)m], eoff = seg_eoff[(size_t)l][(size_t)m];
-      const int32_t *e2n_in = T_.e2n_in, *b2n_in = T_.b2n_in, *grp_in = T_.grp_in;
-      const double *ewt_in = T_.ewt_in, *bwt_in = T_.bwt_in;
-      if (nseg > 1) k_fill<<<nblk(n), T, 0, st>>>(n, m, D.mesh_id + noff);
-
-      // Node order (local to the mesh).
-      if ((r = tmp.get(&T_.perm, (size_t)n)) || (r = tmp.get(&T_.inv, (size_t)n))) return r;
-      if (s->opt.renumber == MGCFD_RENUMBER_SPATIAL) {
-        unsigned long long *box, *key, *key2;
-        int32_t* val;
-        if ((r = tmp.get(&box, 6)) || (r = tmp.get(&key, (size_t)n)) || (r = tmp.get(&key2, (size_t)n)) ||
-            (r = tmp.get(&val, (size_t)n)))
-          return r;
-        CK(cudaMemsetAsync(box, 0xff, 3 * sizeof(unsigned long long), st));
-        CK(cudaMemsetAsync(box + 3, 0, 3 * sizeof(unsigned long long), st));
-        k_bbox<<<nblk(n), T, 0, st>>>(n, T_.xyz, box);
-        k_morton<<<nblk(n), T, 0, st>>>(n, T_.xyz, box, key, val);
-        if ((r = sort_pairs(tmp, key, key2, val, T_.perm, n, 63, st))) return r;
+      CK(cudaMemsetAsync(lo, 0xff, 24 * (size_t)nseg, st));
+      CK(cudaMemsetAsync(hi, 0, 24 * (size_t)nseg, st));
+      k_bbox<<<nblk(N), T, 0, st>>>(N, I.xyz, g, lo, hi);
+      k_morton<<<nblk(N), T, 0, st>>>(N, I.xyz, g, lo, hi, key, val);
+      if (nseg == 1) {
+        if ((r = sort_pairs(tmp, key, key2, val, D.perm, N, 63, st))) return r;
       } else {
-        k_iota<<<nblk(n), T, 0, st>>>(n, T_.perm);
+        int32_t *mkey, *mkey2;
+        if ((r = tmp.get(&mkey, (size_t)N)) || (r = tmp.get(&mkey2, (size_t)N))) return r;
+        if ((r = sort_pairs(tmp, key, key2, val, val2, N, 63, st))) return r;
+        k_seg_of<<<nblk(N), T, 0, st>>>(N, g.noff, nseg, val2, mkey);
+        if ((r = sort_pairs(tmp, mkey, mkey2, val2, D.perm, N, bits_for(nseg - 1), st))) return r;
       }
-      k_inverse<<<nblk(n), T, 0, st>>>(n, T_.perm, T_.inv);
-      k_offset_copy<<<nblk(n), T, 0, st>>>(n, T_.perm, noff, D.perm + noff);
+    } else {
+      k_iota<<<nblk(N), T, 0, st>>>(N, D.perm);
+    }
+    k_inverse<<<nblk(N), T, 0, st>>>(N, D.perm, I.inv);
 
-      // Geometry and volumes.
-      double *tv, *wd;
-      double* vol_in = T_.vol_in;
-      if ((r = tmp.get(&tv, (size_t)ne)) || (r = tmp.get(&wd, 3 * (size_t)ne))) return r;
-      if (ne) k_edge_geometry<<<nblk(ne), T, 0, st>>>(ne, n, e2n_in, T_.xyz, ewt_in, v.volumes != nullptr, tv, wd, err);
-      if (!v.volumes) {
-        int32_t *ikey, *ival, *ikey2, *ival2, *cnt, *off;
-        if ((r = tmp.get(&ikey, 2 * (size_t)ne)) || (r = tmp.get(&ival, 2 * (size_t)ne)) ||
-            (r = tmp.get(&ikey2, 2 * (size_t)ne)) || (r = tmp.get(&ival2, 2 * (size_t)ne)) ||
-            (r = tmp.get(&cnt, (size_t)n + 1)) || (r = tmp.get(&off, (size_t)n + 1)))
-          return r;
-        CK(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * ((size_t)n + 1), st));
-        if (ne) k_incidence<<<nblk(ne), T, 0, st>>>(ne, n, e2n_in, ikey, ival, cnt);
-        if ((r = sort_pairs(tmp, ikey, ikey2, ival, ival2, 2 * (int64_t)ne, bits_for(n), st))) return r;
-        if ((r = offsets(tmp, cnt, off, n, st))) return r;
-        k_volumes<<<nblk(n), T, 0, st>>>(n, off, ival2, tv, vol_in);
+    // Geometry and volumes.
+    double *tv, *wd;
+    int32_t* ge2n;
+    if ((r = tmp.get(&tv, (size_t)NE)) || (r = tmp.get(&wd, 3 * (size_t)NE)) || (r = tmp.get(&ge2n, 2 * (size_t)NE)))
+      return r;
+    if (NE) k_edge_geometry<<<nblk(NE), T, 0, st>>>(NE, g, I.e2n, I.xyz, I.ewt, ge2n, tv, wd, err);
+    if (any_computed_volumes) {
+      int32_t *ikey, *ival, *ikey2, *ival2, *cnt, *off;
+      if ((r = tmp.get(&ikey, 2 * (size_t)NE)) || (r = tmp.get(&ival, 2 * (size_t)NE)) ||
+          (r = tmp.get(&ikey2, 2 * (size_t)NE)) || (r = tmp.get(&ival2, 2 * (size_t)NE)) ||
+          (r = tmp.get(&cnt, (size_t)N + 1)) || (r = tmp.get(&off, (size_t)N + 1)))
+        return r;
+      CK(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * ((size_t)N + 1), st));
+      if (NE) k_incidence<<<nblk(NE), T, 0, st>>>(NE, N, ge2n, ikey, ival, cnt);
+      if ((r = sort_pairs(tmp, ikey, ikey2, ival, ival2, 2 * (int64_t)NE, bits_for(N), st))) return r;
+      if ((r = offsets(tmp, cnt, off, N, st))) return r;
+      k_volumes<<<nblk(N), T, 0, st>>>(N, g, off, ival2, tv, I.vol);
+    }
+    k_node_constants<<<nblk(N), T, 0, st>>>(N, D.perm, I.vol, D.vol, D.inv_vol, D.cbrt_vol);
+
+    // Edges: orientation, order, weights, CSR.
+    {
+      unsigned long long *key, *key2;
+      int32_t *val, *order, *acnt, *bcnt;
+      unsigned char* flip;
+      if ((r = tmp.get(&key, (size_t)NE)) || (r = tmp.get(&key2, (size_t)NE)) || (r = tmp.get(&val, (size_t)NE)) ||
+          (r = tmp.get(&order, (size_t)NE)) || (r = tmp.get(&flip, (size_t)NE)) ||
+          (r = tmp.get(&acnt, (size_t)N + 1)) || (r = tmp.get(&bcnt, (size_t)N + 1)))
+        return r;
+      CK(cudaMemsetAsync(acnt, 0, sizeof(int32_t) * ((size_t)N + 1), st));
+      CK(cudaMemsetAsync(bcnt, 0, sizeof(int32_t) * ((size_t)N + 1), st));
+      if (NE) {
+        k_edge_keys<<<nblk(NE), T, 0, st>>>(NE, ge2n, I.inv, key, val, flip);
+        if ((r = sort_pairs(tmp, key, key2, val, order, NE, 32 + bits_for(N), st))) return r;
+        k_edge_finalize<<<nblk(NE), T, 0, st>>>(NE, g, key2, order, wd, flip, D.e2n, w4all, acnt, bcnt);
       }
-      k_node_constants<<<nblk(n), T, 0, st>>>(n, T_.perm, vol_in, D.vol + noff, D.inv_vol + noff, D.cbrt_vol + noff);
-
-      // Edges: orientation, order, weights, CSR.
-      {
-        unsigned long long *key, *key2;
-        int32_t *val, *order, *acnt, *bcnt;
-        unsigned char* flip;
-        if ((r = tmp.get(&key, (size_t)ne)) || (r = tmp.get(&key2, (size_t)ne)) || (r = tmp.get(&val, (size_t)ne)) ||
-            (r = tmp.get(&order, (size_t)ne)) || (r = tmp.get(&flip, (size_t)ne)) ||
-            (r = tmp.get(&acnt, (size_t)n + 1)) || (r = tmp.get(&bcnt, (size_t)n + 1)))
+      if (s->gather) {
+        int32_t *bkey, *bval, *bkey2;
+        if ((r = tmp.get(&bkey, (size_t)NE)) || (r = tmp.get(&bval, (size_t)NE)) || (r = tmp.get(&bkey2, (size_t)NE)))
           return r;
-        CK(cudaMemsetAsync(acnt, 0, sizeof(int32_t) * ((size_t)n + 1), st));
-        CK(cudaMemsetAsync(bcnt, 0, sizeof(int32_t) * ((size_t)n + 1), st));
-        if (ne) {
-          k_edge_keys<<<nblk(ne), T, 0, st>>>(ne, n, e2n_in, T_.inv, key, val, flip);
-          if ((r = sort_pairs(tmp, key, key2, val, order, ne, 32 + bits_for(n), st))) return r;
-          k_edge_finalize<<<nblk(ne), T, 0, st>>>(ne, noff, key2, order, wd, flip, sc, D.e2n + eoff,
-                                                  w4all + 4 * (size_t)eoff, acnt, bcnt);
+        if ((r = offsets(tmp, acnt, D.a_off, N, st)) || (r = offsets(tmp, bcnt, D.b_off, N, st))) return r;
+        if (NE) {
+          k_b_pairs<<<nblk(NE), T, 0, st>>>(NE, D.e2n, bkey, bval);
+          if ((r = sort_pairs(tmp, bkey, bkey2, bval, D.b_list, NE, bits_for(N), st))) return r;
         }
-        if (s->gather) {
-          int32_t *aoff, *boff, *bkey, *bval, *bkey2, *blist;
-          if ((r = tmp.get(&aoff, (size_t)n + 1)) || (r = tmp.get(&boff, (size_t)n + 1)) ||
-              (r = tmp.get(&bkey, (size_t)ne)) || (r = tmp.get(&bval, (size_t)ne)) ||
-              (r = tmp.get(&bkey2, (size_t)ne)) || (r = tmp.get(&blist, (size_t)ne)))
-            return r;
-          if ((r = offsets(tmp, acnt, aoff, n, st)) || (r = offsets(tmp, bcnt, boff, n, st))) return r;
-          k_offset_copy<<<nblk(n), T, 0, st>>>(n, aoff, eoff, D.a_off + noff);
-          k_offset_copy<<<nblk(n), T, 0, st>>>(n, boff, eoff, D.b_off + noff);
-          if (ne) {
-            k_b_pairs<<<nblk(ne), T, 0, st>>>(ne, D.e2n + eoff, noff, bkey, bval);
-            if ((r = sort_pairs(tmp, bkey, bkey2, bval, blist, ne, bits_for(n), st))) return r;
-            k_offset_copy<<<nblk(ne), T, 0, st>>>(ne, blist, eoff, D.b_list + eoff);
-          }
-        }
-      }
-
-      // Boundary entries folded per node.
-      {
-        int32_t *key, *val, *key2, *val2, *cnt, *off, *flag, *row;
-        if ((r = tmp.get(&key, (size_t)nb)) || (r = tmp.get(&val, (size_t)nb)) || (r = tmp.get(&key2, (size_t)nb)) ||
-            (r = tmp.get(&val2, (size_t)nb)) || (r = tmp.get(&cnt, (size_t)n + 1)) ||
-            (r = tmp.get(&off, (size_t)n + 1)) || (r = tmp.get(&flag, (size_t)n + 1)) ||
-            (r = tmp.get(&row, (size_t)n + 1)))
-          return r;
-        CK(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * ((size_t)n + 1), st));
-        if (nb) {
-          k_bnd_keys<<<nblk(nb), T, 0, st>>>(nb, n, b2n_in, grp_in, T_.inv, key, val, cnt, err);
-          if ((r = sort_pairs(tmp, key, key2, val, val2, nb, bits_for(n), st))) return r;
-        }
-        if ((r = offsets(tmp, cnt, off, n, st))) return r;
-        CK(cudaMemsetAsync(flag, 0, sizeof(int32_t) * ((size_t)n + 1), st));
-        k_nonempty<<<nblk(n), T, 0, st>>>(n, off, flag);
-        if ((r = offsets(tmp, flag, row, n, st))) return r;
-        k_copy1<<<1, 1, 0, st>>>(row + n, rows_tot + m);
-        T_.b_off = off;
-        T_.b_entries = val2;
-        T_.b_row = row;
       }
     }
-    // Row offsets of every mesh's folded boundary rows, then the fold.
-    if ((r = lanes.join())) return r;
-    k_exclusive_scan_small<<<1, 1, 0, st>>>(nseg, rows_tot, row_base);
-    if ((r = lanes.fork())) return r;
-    for (int m = 0; m < nseg; m++) {
-      const LevelTmp& T_ = lt[(size_t)m][(size_t)l];
-      const int32_t n = meshes[(size_t)m].levels[l].nnodes, noff = s->seg_noff[(size_t)l][(size_t)m];
-      k_bnd_fold<<<nblk(n), T, 0, lanes.stream(m)>>>(n, T_.b_off, T_.b_entries, T_.grp_in, T_.bwt_in, T_.b_row,
-                                                   row_base + m, meshes[(size_t)m].ff, D.bidx + noff, D.bdata);
-    }
-    if ((r = lanes.join())) return r;
-    CK(cudaMemcpyAsync(&D.nbrows, row_base + nseg, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    if (s->gather) {
-      k_fill<<<1, 1, 0, st>>>(1, NE, D.a_off + N);
-      k_fill<<<1, 1, 0, st>>>(1, NE, D.b_off + N);
+
+    // Boundary entries folded per node.
+    {
+      int32_t *key, *val, *key2, *val2, *cnt, *off, *flag, *row;
+      if ((r = tmp.get(&key, (size_t)NB)) || (r = tmp.get(&val, (size_t)NB)) || (r = tmp.get(&key2, (size_t)NB)) ||
+          (r = tmp.get(&val2, (size_t)NB)) || (r = tmp.get(&cnt, (size_t)N + 1)) ||
+          (r = tmp.get(&off, (size_t)N + 1)) || (r = tmp.get(&flag, (size_t)N + 1)) ||
+          (r = tmp.get(&row, (size_t)N + 1)))
+        return r;
+      CK(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * ((size_t)N + 1), st));
+      if (NB) {
+        k_bnd_keys<<<nblk(NB), T, 0, st>>>(NB, N, g, I.b2n, I.grp, I.inv, key, val, cnt, err);
+        if ((r = sort_pairs(tmp, key, key2, val, val2, NB, bits_for(N), st))) return r;
+      }
+      if ((r = offsets(tmp, cnt, off, N, st))) return r;
+      CK(cudaMemsetAsync(flag, 0, sizeof(int32_t) * ((size_t)N + 1), st));
+      k_nonempty<<<nblk(N), T, 0, st>>>(N, off, flag);
+      if ((r = offsets(tmp, flag, row, N, st))) return r;
+      k_bnd_fold<<<nblk(N), T, 0, st>>>(N, g, off, val2, I.grp, I.bwt, row, D.bidx, D.bdata);
+      k_copy1<<<1, 1, 0, st>>>(row + N, fin + 1 + l);
     }
     if (mixed) {
       if ((r = s->alloc(&D.w4f, (size_t)NE))) return r;
@@ -675,38 +669,29 @@ int device_prepare(mgcfd_solver* s, const std::vector<MeshInput>& meshes) {
   for (int l = 0; l + 1 < nlevels; l++) {
     DevLevel& F = s->L[(size_t)l];
     DevLevel& Cl = s->L[(size_t)l + 1];
-    if ((r = s->alloc(&F.n2mg, (size_t)F.n)) || (r = s->alloc(&F.dvec, (size_t)F.n)) ||
-        (r = s->alloc(&Cl.ch_off, (size_t)Cl.n + 1)) || (r = s->alloc(&Cl.ch_list, (size_t)F.n)))
+    const int32_t NF = F.n, NC = Cl.n;
+    if ((r = s->alloc(&F.n2mg, (size_t)NF)) || (r = s->alloc(&F.dvec, (size_t)NF)) ||
+        (r = s->alloc(&Cl.ch_off, (size_t)NC + 1)) || (r = s->alloc(&Cl.ch_list, (size_t)NF)))
       return r;
-    Cl.nfine = F.n;
-    if ((r = lanes.fork())) return r;
-    for (int m = 0; m < nseg; m++) {
-      const cudaStream_t st = lanes.stream(m);
-      Temp& tmp = lanes.temp(m);
-      const int32_t nf = meshes[(size_t)m].levels[l].nnodes, nc = meshes[(size_t)m].levels[l + 1].nnodes;
-      const int32_t noff_f = s->seg_noff[(size_t)l][(size_t)m], noff_c = s->seg_noff[(size_t)l + 1][(size_t)m];
-      int32_t *key, *val, *key2, *cnt, *off, *list;
-      if ((r = tmp.get(&key, (size_t)nf)) || (r = tmp.get(&val, (size_t)nf)) || (r = tmp.get(&key2, (size_t)nf)) ||
-          (r = tmp.get(&cnt, (size_t)nc + 1)) || (r = tmp.get(&off, (size_t)nc + 1)) || (r = tmp.get(&list, (size_t)nf)))
-        return r;
-      CK(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * ((size_t)nc + 1), st));
-      const LevelTmp& TF = lt[(size_t)m][(size_t)l];
-      const LevelTmp& TC = lt[(size_t)m][(size_t)l + 1];
-      k_mg<<<nblk(nf), T, 0, st>>>(nf, nc, noff_c, TF.perm, TF.n2mg_in, TC.inv, TF.xyz, TC.xyz, F.n2mg + noff_f,
-                                   reinterpret_cast<double*>(F.dvec) + 4 * (size_t)noff_f, key, val, cnt, err);
-      if ((r = sort_pairs(tmp, key, key2, val, list, nf, bits_for(nc), st))) return r;
-      if ((r = offsets(tmp, cnt, off, nc, st))) return r;
-      k_offset_copy<<<nblk(nf), T, 0, st>>>(nf, list, noff_f, Cl.ch_list + noff_f);
-      k_offset_copy<<<nblk(nc), T, 0, st>>>(nc, off, noff_f, Cl.ch_off + noff_c);
-    }
-    if ((r = lanes.join())) return r;
-    k_fill<<<1, 1, 0, st>>>(1, F.n, Cl.ch_off + Cl.n);
+    Cl.nfine = NF;
+    int32_t *key, *val, *key2, *cnt;
+    if ((r = tmp.get(&key, (size_t)NF)) || (r = tmp.get(&val, (size_t)NF)) || (r = tmp.get(&key2, (size_t)NF)) ||
+        (r = tmp.get(&cnt, (size_t)NC + 1)))
+      return r;
+    CK(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * ((size_t)NC + 1), st));
+    k_mg<<<nblk(NF), T, 0, st>>>(NF, nseg, seg(l).noff, seg(l + 1).noff, F.perm, in[(size_t)l].n2mg,
+                                 in[(size_t)l + 1].inv, in[(size_t)l].xyz, in[(size_t)l + 1].xyz, F.n2mg,
+                                 reinterpret_cast<double*>(F.dvec), key, val, cnt, err);
+    if ((r = sort_pairs(tmp, key, key2, val, Cl.ch_list, NF, bits_for(NC), st))) return r;
+    if ((r = offsets(tmp, cnt, Cl.ch_off, NC, st))) return r;
   }
   CK(cudaGetLastError());
-  unsigned h_err = 0;
-  CK(cudaMemcpyAsync(&h_err, err, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+  std::vector<unsigned> h_fin(1 + (size_t)nlevels, 0);
+  CK(cudaMemcpyAsync(h_fin.data(), fin, sizeof(unsigned) * h_fin.size(), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
-  if (h_err) return set_error(MGCFD_ERR_INVALID, "mesh has " + std::to_string(h_err) + " map entries out of range");
+  for (int l = 0; l < nlevels; l++) s->L[(size_t)l].nbrows = (int32_t)h_fin[1 + (size_t)l];
+  if (h_fin[0])
+    return set_error(MGCFD_ERR_INVALID, "mesh has " + std::to_string(h_fin[0]) + " map entries out of range");
   return MGCFD_OK;
 }
 

@@ -55,6 +55,21 @@ namespace {
 
 constexpr int kNodeThreads = 128;
 
+// Keep freed solver and setup memory in the device's default pool, so that
+// repeated solves (batches, serving) do not map fresh memory from the
+// driver for every allocation.
+void keep_freed_memory(int dev) {
+  static std::once_flag once[kMaxDevices];
+  if (dev < 0 || dev >= kMaxDevices) return;
+  std::call_once(once[dev], [dev] {
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      uint64_t keep = ~0ull;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+  });
+}
+
 // ---------------------------------------------------------------------------
 // Kernels.
 
@@ -982,17 +997,7 @@ extern "C" int mgcfd_solver_create(int32_t nlevels, const mgcfd_level_view* leve
   }
   mgcfd_freestream_init(mach, aoa_deg, &s->ff);
 
-  static std::once_flag pool_once[kMaxDevices];
-  if (s->device >= 0 && s->device < kMaxDevices)
-    std::call_once(pool_once[s->device], [dev = s->device] {
-      // Keep freed solver memory in this process's pool so repeated solves
-      // (bench, serving) do not go back to the driver for every allocation.
-      cudaMemPool_t pool;
-      if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
-        uint64_t keep = ~0ull;
-        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
-      }
-    });
+  keep_freed_memory(s->device);
   s->L.resize((size_t)nlevels);
   size_t max_n = 0;
   for (int l = 0; l < nlevels; l++) max_n = std::max(max_n, (size_t)levels[l].nnodes);
@@ -1094,6 +1099,7 @@ extern "C" int mgcfd_batch_create(int32_t nmeshes, int32_t nlevels, const mgcfd_
     CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
     s->owns_stream = true;
   }
+  keep_freed_memory(s->device);
   int r;
   std::vector<MeshInput> meshes((size_t)nmeshes);
   s->seg_ff.resize((size_t)nmeshes);

@@ -69,3 +69,49 @@ def test_legacy_mesh_on_device(tmp_path):
     assert s.synchronize() == 0
     for l in range(3):
         assert state_error(s.fetch(l), ref.get(l, O.Q_VARIABLES)) <= STATE_TOL
+
+
+@pytest.mark.parametrize("renumber", ["spatial", "none"])
+def test_batch_tables_are_shifted_single_mesh_tables(renumber):
+    """A batch is prepared as one set of concatenated levels; mesh m's tables
+    must equal those of mesh m prepared alone, shifted by its node, edge and
+    boundary-row offsets."""
+    nl = 3
+    meshes = [mgcfd.HostMesh.generate(n, nl, 40 + n) for n in (9, 12, 7, 10)]
+    machs, aoas = [0.5, 0.8, 0.65, 0.7], [1.0, 3.0, 0.0, 5.5]
+    batch = mgcfd.Batch(meshes, machs, aoas, increment="gather", renumber=renumber)
+    singles = [mgcfd.Solver(m, a, b, increment="gather", renumber=renumber) for m, a, b in zip(meshes, machs, aoas)]
+    for l in range(nl):
+        nn = [m.level(l).nnodes for m in meshes]
+        ne = [m.level(l).nedges for m in meshes]
+        noff = np.concatenate([[0], np.cumsum(nn)])
+        eoff = np.concatenate([[0], np.cumsum(ne)])
+        nc = [m.level(l + 1).nnodes for m in meshes] if l + 1 < nl else None
+        coff = np.concatenate([[0], np.cumsum(nc)]) if nc else None
+        fine_off = np.concatenate([[0], np.cumsum([m.level(l - 1).nnodes for m in meshes])]) if l > 0 else None
+        rows = [int((table(s, l, 6) >= 0).sum()) for s in singles]
+        roff = np.concatenate([[0], np.cumsum(rows)])
+        for t, (name, _) in TABLES.items():
+            parts = [table(s, l, t) for s in singles]
+            if name in ("PERM", "EDGES"):
+                parts = [p + noff[m] for m, p in enumerate(parts)]
+            elif name == "BIDX":
+                parts = [np.where(p >= 0, p + roff[m], p) for m, p in enumerate(parts)]
+            elif name == "N2MG" and coff is not None:
+                parts = [p + coff[m] for m, p in enumerate(parts)]
+            elif name in ("CH_OFF",) and fine_off is not None:
+                parts = [p[:-1] + fine_off[m] for m, p in enumerate(parts)] + [np.array([fine_off[-1]], np.int32)]
+            elif name == "CH_LIST" and fine_off is not None:
+                parts = [p + fine_off[m] for m, p in enumerate(parts)]
+            elif name in ("A_OFF", "B_OFF"):
+                parts = [p[:-1] + eoff[m] for m, p in enumerate(parts)] + [np.array([eoff[-1]], np.int32)]
+            elif name == "B_LIST":
+                parts = [p + eoff[m] for m, p in enumerate(parts)]
+            parts = [p for p in parts if p.size]
+            want = np.concatenate(parts) if parts else np.empty(0, TABLES[t][1])
+            got = table(batch, l, t)
+            assert got.shape == want.shape, (l, name)
+            np.testing.assert_array_equal(got, want.astype(got.dtype), err_msg=f"level {l} table {name}")
+    for s in singles:
+        s.close()
+    batch.close()
