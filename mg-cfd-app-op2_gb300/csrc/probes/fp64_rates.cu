@@ -103,19 +103,24 @@ __device__ __forceinline__ double widen_asm(float f) {  // asm packing, no speci
 
 // The node-sum pattern of the mixed-precision update: each thread widens 30
 // FP32 values read from memory (6 edges x 5 variables) and adds them into 5
-// FP64 sums.  op 0 = hardware cvt, 1 = f2d_bits, 2 = FP32 sums widened once.
-// The array (256 K threads x 30 floats) stays in L2, so the arithmetic shows.
+// FP64 sums.  op 0 = hardware cvt, 1 = f2d_bits, 2 = FP32 sums widened once,
+// 3..5 = other packings of the widened bits, 6 = the same sums of doubles read
+// from memory (no widening at all).  The arrays (256 K threads x 30 values)
+// stay in L2, so the arithmetic shows.
 template <int OP>
-__global__ void k_node_sums(int n, const float* __restrict__ fe, double* __restrict__ out) {
+__global__ void k_node_sums(int n, const float* __restrict__ fe, const double* __restrict__ fd,
+                            double* __restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double F[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
   float G[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
   const float* p = fe + 30 * (int64_t)i;
+  const double* q = fd + 30 * (int64_t)i;
   for (int e = 0; e < 6; e++)
 #pragma unroll
     for (int k = 0; k < 5; k++) {
-      const float x = p[5 * e + k];
+      const float x = OP == 6 ? 0.f : p[5 * e + k];
+      if (OP == 6) F[k] += q[5 * e + k];
       if (OP == 0) F[k] += (double)x;
       if (OP == 1) F[k] += mgcfd::f2d_bits(x);
       if (OP == 2) G[k] += x;
@@ -179,13 +184,17 @@ int main() {
   float* fe;
   CK(cudaMalloc(&fe, sizeof(float) * 30 * (size_t)nsum));
   CK(cudaMemset(fe, 0x3f, sizeof(float) * 30 * (size_t)nsum));  // every float 0x3f3f3f3f = 0.747: normal
+  double* fd;
+  CK(cudaMalloc(&fd, sizeof(double) * 30 * (size_t)nsum));
+  CK(cudaMemset(fd, 0x3f, sizeof(double) * 30 * (size_t)nsum));  // 0x3f3f...3f: a normal double
   auto sums = [&](auto kernel) {
     return timed([&] {
-      for (int r = 0; r < 20; r++) kernel<<<(nsum + 255) / 256, 256>>>(nsum, fe, od);
+      for (int r = 0; r < 20; r++) kernel<<<(nsum + 255) / 256, 256>>>(nsum, fe, fd, od);
     });
   };
   const float t_s0 = sums(k_node_sums<0>), t_s1 = sums(k_node_sums<1>), t_s2 = sums(k_node_sums<2>);
   const float t_s3 = sums(k_node_sums<3>), t_s4 = sums(k_node_sums<4>), t_s5 = sums(k_node_sums<5>);
+  const float t_s6 = sums(k_node_sums<6>);
   CK(cudaGetLastError());
   const uint32_t an = 64u << 20;  // 512 MB of doubles: atomics go to HBM
   double* arr;
@@ -209,15 +218,16 @@ int main() {
          "\"rsqrt_g_per_s\": %.1f, \"rsqrt_dfma_eq\": %.2f, \"cvt_d2f2d_dfma_eq\": %.2f, "
          "\"intpipe_d2f2d_dfma_eq\": %.2f, \"widen_add_dfma_eq\": {\"add_only\": %.2f, \"hw_cvt\": %.2f, "
          "\"f2d_bits\": %.2f}, \"node_sums_us\": {\"hw_cvt\": %.1f, \"f2d_bits\": %.1f, \"fp32_then_once\": %.1f, \"hilo\": %.1f, "
-         "\"i64\": %.1f, \"asm_normal_only\": %.1f}, "
+         "\"i64\": %.1f, \"asm_normal_only\": %.1f, \"doubles_from_memory\": %.1f}, "
          "\"red_f64_hbm_g_per_s\": %.1f, \"d2d_copy_gb_per_s\": %.1f}\n",
          p.name, p.multiProcessorCount, dfma_per_s / 1e9, 2 * dfma_per_s / 1e12,
          2 * 8.0 * ops / (t_ffma * 1e-3) / 1e12, uops / (t_rcp * 1e-3) / 1e9, eq(t_rcp, uops),
          uops / (t_sqrt * 1e-3) / 1e9, eq(t_sqrt, uops), uops / (t_rsqrt * 1e-3) / 1e9, eq(t_rsqrt, uops),
          eq(t_cvt, uops), eq(t_cvti, uops), eq(t_w0, uops), eq(t_w1, uops), eq(t_w2, uops),
          1e3 * t_s0 / 20, 1e3 * t_s1 / 20, 1e3 * t_s2 / 20, 1e3 * t_s3 / 20, 1e3 * t_s4 / 20, 1e3 * t_s5 / 20,
+         1e3 * t_s6 / 20,
          (double)per * kN / (t_red * 1e-3) / 1e9,
          2.0 * big * 8 / (t_copy * 1e-3) / 1e9);
-  cudaFree(od); cudaFree(of); cudaFree(arr); cudaFree(src); cudaFree(dst); cudaFree(fe);
+  cudaFree(od); cudaFree(of); cudaFree(arr); cudaFree(src); cudaFree(dst); cudaFree(fe); cudaFree(fd);
   return 0;
 }
