@@ -232,9 +232,11 @@ def run_gb300(args):
         # The FP64 flux sweep is bound by FP64 issue, not HBM: the same launch
         # against the measured FP64 FMA rate.
         f = prof["fp64"]
-        ach = f["ops_per_edge"] * E / (flux_ms * 1e-3) / 1e9
+        per_edge = "ops_per_edge" in f
+        ach = (f["ops_per_edge"] * E if per_edge else f["ops_per_node"] * N) / (flux_ms * 1e-3) / 1e9
         fp64_roof = {"bound": "fp64", "achieved": round(ach, 1), "peak": f["peak_gops"], "unit": "G FP64 op/s",
-                     "frac": round(ach / f["peak_gops"], 4), "ops_per_edge": f["ops_per_edge"],
+                     "frac": round(ach / f["peak_gops"], 4),
+                     ("ops_per_edge" if per_edge else "ops_per_node"): f["ops_per_edge" if per_edge else "ops_per_node"],
                      "peak_source": f["peak_source"], "ncu_fp64_pipe_busy": f["pipe_busy_ncu"]}
     line = {
         "metric": "MG V-cycles/s at 8M nodes (200^3, 4 levels)",
