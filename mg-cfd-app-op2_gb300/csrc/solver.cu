@@ -385,6 +385,35 @@ __device__ __forceinline__ void add_boundary(const NodePrim& p, const double* __
   F[3] += b[5] * p.p;
 }
 
+// Level-0 norms of one block of kNodeThreads threads (every thread arrives):
+// sums through shared memory, halving the active threads each step down to
+// one warp, so every FP64 add is a useful one (a shuffle tree in each warp
+// would issue five per thread); then one atomic per sum.  A NaN or infinity
+// stops the solver (euler3d.cpp:539-548).
+__device__ __forceinline__ void block_norms(double* srms, double* srho, int* sbad, double r2, double rr, int bad,
+                                            DevStatus* st) {
+  const int t = threadIdx.x;
+  srms[t] = r2;
+  srho[t] = rr;
+  sbad[t] = bad;
+  __syncthreads();
+#pragma unroll
+  for (int w = kNodeThreads / 2; w >= 32; w >>= 1) {
+    if (t < w) { srms[t] += srms[t + w]; srho[t] += srho[t + w]; sbad[t] += sbad[t + w]; }
+    __syncthreads();
+  }
+  if (t < 32) {
+    r2 = warp_sum(srms[t]);
+    rr = warp_sum(srho[t]);
+    bad = warp_sum_int(sbad[t]);
+    if (t == 0) {
+      atomicAdd(&st->rms_acc, r2);
+      atomicAdd(&st->rho_acc, rr);
+      if (bad) { atomicAdd(&st->bad_count, bad); atomicOr(&st->halt, 1); }
+    }
+  }
+}
+
 // compute_bnd_node_flux_kernel + time_step_kernel (+ residual_kernel,
 // calc_rms_kernel and count_bad_vals in the last stage).  Plain solvers stop
 // everything on min_dt < 0 or NaN/Inf (the reference aborts); batched
@@ -561,50 +590,58 @@ __global__ void __launch_bounds__(kNodeThreads) k_update(UpdateArgs A) {
     if (s_bad[t]) atomicAdd(A.seg_bad + m0 + t, s_bad[t]);
     return;
   }
-  // Block sums through shared memory, halving the active threads each step
-  // down to one warp: every FP64 add is a useful one (a shuffle tree in each
-  // warp would issue five per thread).
-  const int t = threadIdx.x;
-  srms[t] = r2;
-  srho[t] = rr;
-  sbad[t] = bad;
-  __syncthreads();
-#pragma unroll
-  for (int w = kNodeThreads / 2; w >= 32; w >>= 1) {
-    if (t < w) { srms[t] += srms[t + w]; srho[t] += srho[t + w]; sbad[t] += sbad[t + w]; }
-    __syncthreads();
-  }
-  if (t < 32) {
-    r2 = warp_sum(srms[t]);
-    rr = warp_sum(srho[t]);
-    bad = warp_sum_int(sbad[t]);
-    if (threadIdx.x == 0) {
-      atomicAdd(&A.st->rms_acc, r2);
-      atomicAdd(&A.st->rho_acc, rr);
-      if (bad) { atomicAdd(&A.st->bad_count, bad); atomicOr(&A.st->halt, 1); }
-    }
-  }
+  block_norms(srms, srho, sbad, r2, rr, bad, A.st);
 }
 
 // up_pre/up/up_post (mg.h:29-64) as a gather over each coarse node's children.
-__global__ void k_restrict(int32_t nc, const int32_t* __restrict__ ch_off, const int32_t* __restrict__ ch_list,
-                           const double* __restrict__ frec, double* __restrict__ crec,
-                           const DevStatus* __restrict__ st) {
-  if (st->halt) return;
-  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= nc) return;
-  const int32_t lo = ch_off[c], hi = ch_off[c + 1];
-  if (hi == lo) return;  // no children: state unchanged (avg = 1 on untouched values)
-  double s[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-  for (int32_t j = lo; j < hi; j++) {
-    const double* r = frec + 8 * (int64_t)ch_list[j];
-#pragma unroll
-    for (int k = 0; k < 5; k++) s[k] += r[k];
+// NORMS (restriction from level 0 of a plain solver): the same pass also
+// takes calc_rms_kernel and count_bad_vals (validation.h:37-44, 102-115) of
+// the level-0 step just finished, since it reads every fine node's state once
+// and the residuals sit beside it.  Its blocks cover about eight fine nodes
+// per thread, so the block reductions are an eighth of those a fine-node
+// kernel would run.
+template <bool NORMS>
+__global__ void __launch_bounds__(kNodeThreads) k_restrict(int32_t nc, const int32_t* __restrict__ ch_off,
+                                                           const int32_t* __restrict__ ch_list,
+                                                           const double* __restrict__ frec, double* __restrict__ crec,
+                                                           const double* __restrict__ fres, DevStatus* st) {
+  __shared__ double srms[NORMS ? kNodeThreads : 1], srho[NORMS ? kNodeThreads : 1];
+  __shared__ int sbad[NORMS ? kNodeThreads : 1];
+  __shared__ int s_halt;
+  if (NORMS) {
+    if (threadIdx.x == 0) s_halt = st->halt;
+    __syncthreads();
+    if (s_halt) return;  // block-uniform: the reduction below synchronises
+  } else if (st->halt) {
+    return;
   }
-  const double avg = 1.0 / (double)(hi - lo);
-  double* r = crec + 8 * c;
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double q[5] = {0.0, 0.0, 0.0, 0.0, 0.0};  // sums of squared residuals, one chain per variable
+  int bad = 0;
+  const int32_t lo = c < nc ? ch_off[c] : 0, hi = c < nc ? ch_off[c + 1] : 0;
+  if (hi > lo) {  // no children: state unchanged (avg = 1 on untouched values)
+    double s[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int32_t j = lo; j < hi; j++) {  // unrolled: several children's loads in flight, adds still in order
+      const int64_t f = ch_list[j];
+      const double* r = frec + 8 * f;
 #pragma unroll
-  for (int k = 0; k < 5; k++) r[k] = s[k] * avg;
+      for (int k = 0; k < 5; k++) s[k] += r[k];
+      if (NORMS) {
+        const double* d = fres + 5 * f;
+#pragma unroll
+        for (int k = 0; k < 5; k++) {
+          q[k] += d[k] * d[k];
+          bad += not_finite(r[k]) ? 1 : 0;
+        }
+      }
+    }
+    const double avg = 1.0 / (double)(hi - lo);
+    double* r = crec + 8 * c;
+#pragma unroll
+    for (int k = 0; k < 5; k++) r[k] = s[k] * avg;
+  }
+  if (!NORMS) return;
+  block_norms(srms, srho, sbad, ((q[0] + q[1]) + (q[2] + q[3])) + q[4], q[0], bad, st);
 }
 
 // down_kernel (mg.h:66-88) with the parent offsets precomputed.
@@ -733,6 +770,14 @@ using StepFn = void (*)(const DevLevel&, unsigned long long*, const DevStatus*, 
 const StepFn kStepBegin[4] = {launch_step_begin<0, 0>, launch_step_begin<0, 1>, launch_step_begin<1, 0>,
                               launch_step_begin<1, 1>};
 
+// Where the level-0 norms (calc_rms_kernel, count_bad_vals) are taken: in
+// the last RK stage, or -- for plain multi-level solvers with the fused
+// stage, whose warps finish at uneven times and idle at the stage's block
+// reduction -- in the restriction that follows, which reads the same state
+// and residuals (measured: 203.1 -> 206.4 V-cycles/s at 8M nodes; the FP64
+// stage loses 1% the same way, so it keeps them).
+bool norms_in_restrict(const mgcfd_solver* s) { return s->fused && s->nseg == 1 && s->L.size() > 1; }
+
 // One smoothing step at `level` (euler3d.cpp:467-550).
 int enqueue_smooth(mgcfd_solver* s, int level) {
   DevLevel& D = s->L[(size_t)level];
@@ -782,7 +827,7 @@ int enqueue_smooth(mgcfd_solver* s, int level) {
       }
     }
     UpdateArgs A;
-    A.n = D.n; A.level0 = level == 0; A.inv_div = 1.0 / (double)(kRK + 1 - rk);
+    A.n = D.n; A.level0 = level == 0 && !norms_in_restrict(s); A.inv_div = 1.0 / (double)(kRK + 1 - rk);
     A.rec = D.rec; A.rec32 = D.rec32; A.old = D.old; A.flux = D.flux; A.fe = D.fe; A.fe32 = D.fe32;
     A.a_off = D.a_off; A.b_off = D.b_off; A.b_list = D.b_list; A.inv_vol = D.inv_vol; A.bidx = D.bidx;
     A.bdata = D.bdata; A.res = D.res; A.dt_key = key; A.st = s->st;
@@ -829,7 +874,12 @@ int enqueue_iteration(mgcfd_solver* s) {
     s->level++;
     DevLevel& F = s->L[(size_t)s->level - 1];
     DevLevel& Cl = s->L[(size_t)s->level];
-    k_restrict<<<grid(Cl.n, kNodeThreads), kNodeThreads, 0, s->stream>>>(Cl.n, Cl.ch_off, Cl.ch_list, F.rec, Cl.rec, s->st);
+    if (s->level == 1 && norms_in_restrict(s))  // level-0 norms of the step just smoothed
+      k_restrict<true><<<grid(Cl.n, kNodeThreads), kNodeThreads, 0, s->stream>>>(Cl.n, Cl.ch_off, Cl.ch_list, F.rec,
+                                                                                 Cl.rec, F.res, s->st);
+    else
+      k_restrict<false><<<grid(Cl.n, kNodeThreads), kNodeThreads, 0, s->stream>>>(Cl.n, Cl.ch_off, Cl.ch_list, F.rec,
+                                                                                  Cl.rec, nullptr, s->st);
     s->launches++;
     if (s->level == levels - 1) s->up = false;
   } else {
