@@ -621,9 +621,10 @@ __global__ void __launch_bounds__(kNodeThreads) k_restrict(int32_t nc, const int
   const int32_t lo = c < nc ? ch_off[c] : 0, hi = c < nc ? ch_off[c + 1] : 0;
   if (hi > lo) {  // no children: state unchanged (avg = 1 on untouched values)
     double s[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-    for (int32_t j = lo; j < hi; j++) {  // unrolled: several children's loads in flight, adds still in order
+    for (int32_t j = lo; j < hi; j++) {
       const int64_t f = ch_list[j];
-      const double* r = frec + 8 * f;
+      const double4_32a x = *reinterpret_cast<const double4_32a*>(frec + 8 * f);  // one 32-byte access
+      const double r[5] = {x.x, x.y, x.z, x.w, frec[8 * f + 4]};
 #pragma unroll
       for (int k = 0; k < 5; k++) s[k] += r[k];
       if (NORMS) {
@@ -653,10 +654,19 @@ __global__ void k_prolong(int32_t nf, const int32_t* __restrict__ n2mg, const do
   if (i >= nf) return;
   const int64_t c = n2mg[i];
   const double4_32a d = dvec[i];
-  const double dd[5] = {d.w, d.x, d.y, d.z, d.w};
-  double* r = frec + 8 * i;
-#pragma unroll
-  for (int k = 0; k < 5; k++) r[k] -= dd[k] * (cres[5 * c + k] - fres[5 * i + k]);
+  // The record's first four values as one 32-byte access, the fifth alone.
+  double4_32a* r4 = reinterpret_cast<double4_32a*>(frec + 8 * i);
+  double4_32a x = r4[0];
+  double x4 = frec[8 * i + 4];
+  const double* cr = cres + 5 * c;
+  const double* fr = fres + 5 * i;
+  x.x -= d.w * (cr[0] - fr[0]);
+  x.y -= d.x * (cr[1] - fr[1]);
+  x.z -= d.y * (cr[2] - fr[2]);
+  x.w -= d.z * (cr[3] - fr[3]);
+  x4 -= d.w * (cr[4] - fr[4]);
+  r4[0] = x;
+  frec[8 * i + 4] = x4;
 }
 
 // Far-field terms w.F_ff of every folded boundary row for a new freestream
