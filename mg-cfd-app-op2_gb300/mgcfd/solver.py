@@ -76,6 +76,13 @@ class Solver:
         _lib.check(self._lib.mgcfd_solver_fetch(self._h, level, quantity, out.ctypes.data_as(_lib.c_double_p)))
         return out
 
+    def norms(self):
+        """(status, rms_l0, density_rms_l0) after synchronising: the level-0
+        residual norms of the last level-0 smoothing step (euler3d.cpp:533-537)."""
+        rms, rho = C.c_double(), C.c_double()
+        st = self._lib.mgcfd_solver_mesh_status(self._h, 0, C.byref(rms), C.byref(rho))
+        return st, rms.value, rho.value
+
     def stats(self) -> _lib.SolverStats:
         s = _lib.SolverStats()
         _lib.check(self._lib.mgcfd_solver_get_stats(self._h, C.byref(s)))

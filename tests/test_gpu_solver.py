@@ -184,13 +184,16 @@ def test_legacy_volumes_match_oracle():
         assert state_error(s.fetch(l), ref2.get(l, O.Q_VARIABLES)) <= STATE_TOL
 
 
-def test_nan_state_reports_bad_values():
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_nan_state_reports_bad_values(precision):
+    # mixed precision uses the fused stage, whose level-0 NaN count is taken
+    # in the restriction that follows the step; FP64 counts in the last stage
     mesh = mgcfd.HostMesh.generate(8, 2, 3)
     levels = mesh.levels()
     bad = [mgcfd.Level(**{k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in L.__dict__.items()
                           if k != "owner"}) for L in levels]
     bad[0].edge_weights[0, :] = np.nan  # poisons the flux of two nodes at level 0
-    s = mgcfd.Solver(bad, 0.5, 3.0)
+    s = mgcfd.Solver(bad, 0.5, 3.0, precision=precision)
     s.run(2)
     assert s.synchronize() == mgcfd._lib.ERR_BAD_VALUES
     assert "Bad variable values" in mgcfd._lib.load().mgcfd_last_error().decode()
@@ -207,3 +210,36 @@ def test_solve_entry_point_matches_solver():
     assert s.synchronize() == 0
     for l in range(2):
         np.testing.assert_array_equal(outs[l], s.fetch(l))
+
+
+def _norms(mesh, cycles, **opts):
+    s = mgcfd.Solver(mesh, 0.7, 2.0, **opts)
+    s.run(cycles)
+    st, rms, rho = s.norms()
+    assert st == 0
+    res = s.fetch(0, mgcfd.Q_RESIDUALS)
+    s.close()
+    return rms, rho, res
+
+
+@pytest.mark.parametrize("nl", [1, 3])
+def test_level0_norms_match_residuals_and_oracle(nl):
+    """rms of the last level-0 step (euler3d.cpp:533-537), taken in the last RK
+    stage (FP64, gather) or in the restriction after it (fused stage): both
+    equal sqrt(sum res^2 / N) of the residual the solver returns, and the
+    FP64 value matches the oracle's residual."""
+    mesh = mgcfd.HostMesh.generate(12, nl, 77)
+    n0 = mesh.level(0).nnodes
+    cycles = 3
+    ref = _oracle(mesh.levels(), 0.7, 2.0, cycles)
+    r_ref = ref.get(0, O.Q_RESIDUALS)
+    rms_ref = np.sqrt(np.sum(r_ref ** 2) / n0)
+    rms64, rho64, res64 = _norms(mesh, cycles)
+    assert rms64 == pytest.approx(np.sqrt(np.sum(res64 ** 2) / n0), rel=1e-12)
+    assert rho64 == pytest.approx(np.sqrt(np.sum(res64[:, 0] ** 2) / n0), rel=1e-12)
+    assert rms64 == pytest.approx(rms_ref, rel=1e-6)
+    rms_f, rho_f, res_f = _norms(mesh, cycles, precision="mixed", increment="fused")
+    rms_g, rho_g, res_g = _norms(mesh, cycles, precision="mixed", increment="gather")
+    np.testing.assert_array_equal(res_f, res_g)  # same residuals, norms from different kernels
+    assert rms_f == pytest.approx(rms_g, rel=1e-12) and rho_f == pytest.approx(rho_g, rel=1e-12)
+    assert rms_f == pytest.approx(np.sqrt(np.sum(res_f ** 2) / n0), rel=1e-12)
