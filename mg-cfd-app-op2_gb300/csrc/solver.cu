@@ -28,14 +28,17 @@
 //                         primitives for the next stage; in the last stage
 //                         residual, and at level 0 the rms and NaN/Inf count }
 //   (fused strategy, mixed precision: no k_flux; k_update computes each of
-//   its node's edge fluxes itself from the stage's input primitives)
+//   its node's edge fluxes itself from the stage's input primitives, and a
+//   plain multi-level solver takes the level-0 rms and NaN/Inf count in the
+//   restriction that follows instead of the last stage)
 // then k_restrict (coarse nodes, children mean, mg.h:29-64) or k_prolong
 // (fine nodes, mg.h:66-88), and under a stop rule k_cycle_end after each
 // V-cycle.
 //
 // Failure handling: min_dt < 0 and NaN/Inf at level 0 set a sticky device
 // status word; every later kernel sees it and returns, so the run stops at the
-// same point the reference aborts.  The host reads the status on synchronize.
+// same point the reference aborts (with the fused stage, one restriction
+// later).  The host reads the status on synchronize.
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
