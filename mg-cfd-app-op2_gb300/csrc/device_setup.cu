@@ -124,10 +124,17 @@ __global__ void k_seg_of(int32_t n, const int32_t* __restrict__ off, int32_t nse
 // ---- node order -------------------------------------------------------------
 
 // Per-mesh bounding boxes as ordered keys: lo[3m + d], hi[3m + d].  A warp
-// whose nodes share one mesh reduces first and updates once.
+// whose nodes share one mesh reduces first; warps of the block's first mesh
+// combine in shared memory, so the common case costs one global atomic per
+// block and dimension (a handful of addresses take every update).
 __global__ void k_bbox(int32_t n, const double* __restrict__ xyz, Seg g, unsigned long long* __restrict__ lo,
                        unsigned long long* __restrict__ hi) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ unsigned long long s_lo[3], s_hi[3];
+  const int64_t i0 = (int64_t)blockIdx.x * blockDim.x;
+  const int32_t mb = seg_of(g.noff, g.nseg, i0);  // the block's first mesh
+  if (threadIdx.x < 3) { s_lo[threadIdx.x] = ~0ull; s_hi[threadIdx.x] = 0ull; }
+  __syncthreads();
+  const int64_t i = i0 + threadIdx.x;
   const bool in = i < n;
   const int32_t m = in ? seg_of(g.noff, g.nseg, i) : -1;
   const int32_t m0 = __shfl_sync(0xffffffffu, m, 0);
@@ -138,14 +145,37 @@ __global__ void k_bbox(int32_t n, const double* __restrict__ xyz, Seg g, unsigne
       const unsigned long long kmin = warp_min_u64(in ? k : ~0ull);
       const unsigned long long kmax = ~warp_min_u64(in ? ~k : ~0ull);
       if ((threadIdx.x & 31) == 0 && m0 >= 0) {
-        atomicMin(&lo[3 * m0 + d], kmin);
-        atomicMax(&hi[3 * m0 + d], kmax);
+        if (m0 == mb) {
+          atomicMin(&s_lo[d], kmin);
+          atomicMax(&s_hi[d], kmax);
+        } else {
+          atomicMin(&lo[3 * m0 + d], kmin);
+          atomicMax(&hi[3 * m0 + d], kmax);
+        }
       }
     } else if (in) {
       atomicMin(&lo[3 * m + d], k);
       atomicMax(&hi[3 * m + d], k);
     }
   }
+  __syncthreads();
+  if (threadIdx.x < 3 && s_lo[threadIdx.x] != ~0ull) {
+    atomicMin(&lo[3 * mb + threadIdx.x], s_lo[threadIdx.x]);
+    atomicMax(&hi[3 * mb + threadIdx.x], s_hi[threadIdx.x]);
+  }
+}
+
+// Each mesh's quantisation per dimension (as spatial_order() in setup.cpp):
+// box[6m + d] = the low end, box[6m + 3 + d] = 2097151 / span or 0.
+__global__ void k_box_scale(int32_t nseg, const unsigned long long* __restrict__ lo,
+                            const unsigned long long* __restrict__ hi, double* __restrict__ box) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 3 * nseg) return;
+  const int m = t / 3, d = t % 3;
+  const double a = dkey_inv(lo[3 * m + d]), b = dkey_inv(hi[3 * m + d]);
+  const double span = __dsub_rn(b, a);
+  box[6 * m + d] = a;
+  box[6 * m + 3 + d] = (b > a && isfinite(span)) ? __ddiv_rn(2097151.0, span) : 0.0;
 }
 
 __device__ __forceinline__ uint64_t spread3(uint64_t x) {
@@ -160,18 +190,14 @@ __device__ __forceinline__ uint64_t spread3(uint64_t x) {
 
 // Same quantisation as spatial_order() in setup.cpp, against the node's own
 // mesh's box.
-__global__ void k_morton(int32_t n, const double* __restrict__ xyz, Seg g, const unsigned long long* __restrict__ lo,
-                         const unsigned long long* __restrict__ hi, unsigned long long* __restrict__ key,
-                         int32_t* __restrict__ val) {
+__global__ void k_morton(int32_t n, const double* __restrict__ xyz, Seg g, const double* __restrict__ box,
+                         unsigned long long* __restrict__ key, int32_t* __restrict__ val) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const int32_t m = seg_of(g.noff, g.nseg, i);
+  const double* bx = box + 6 * seg_of(g.noff, g.nseg, i);
   uint64_t q[3];
   for (int d = 0; d < 3; d++) {
-    const double a = dkey_inv(lo[3 * m + d]), b = dkey_inv(hi[3 * m + d]);
-    const double span = __dsub_rn(b, a);
-    const double scale = (b > a && isfinite(span)) ? __ddiv_rn(2097151.0, span) : 0.0;
-    double t = __dmul_rn(__dsub_rn(xyz[3 * i + d], a), scale);
+    double t = __dmul_rn(__dsub_rn(xyz[3 * i + d], bx[d]), bx[3 + d]);
     if (!(t > 0.0)) t = 0.0;
     if (t > 2097151.0) t = 2097151.0;
     q[d] = (uint64_t)t;
@@ -558,8 +584,11 @@ int device_prepare(mgcfd_solver* s, const std::vector<MeshInput>& meshes) {
         return r;
       CK(cudaMemsetAsync(lo, 0xff, 24 * (size_t)nseg, st));
       CK(cudaMemsetAsync(hi, 0, 24 * (size_t)nseg, st));
+      double* box;
+      if ((r = tmp.get(&box, 6 * (size_t)nseg))) return r;
       k_bbox<<<nblk(N), T, 0, st>>>(N, I.xyz, g, lo, hi);
-      k_morton<<<nblk(N), T, 0, st>>>(N, I.xyz, g, lo, hi, key, val);
+      k_box_scale<<<nblk(3 * (int64_t)nseg), T, 0, st>>>(nseg, lo, hi, box);
+      k_morton<<<nblk(N), T, 0, st>>>(N, I.xyz, g, box, key, val);
       if (nseg == 1) {
         if ((r = sort_pairs(tmp, key, key2, val, D.perm, N, 63, st))) return r;
       } else {
