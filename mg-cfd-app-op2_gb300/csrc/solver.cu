@@ -420,9 +420,12 @@ __device__ __forceinline__ void block_norms(double* srms, double* srho, int* sba
 // compute_bnd_node_flux_kernel + time_step_kernel (+ residual_kernel,
 // calc_rms_kernel and count_bad_vals in the last stage).  Plain solvers stop
 // everything on min_dt < 0 or NaN/Inf (the reference aborts); batched
-// solvers mark the failing mesh and leave the others running.
+// solvers mark the failing mesh and leave the others running.  The fused
+// stage with pair sums is latency-bound: capped at 48 registers (10 blocks
+// per SM, a few bytes spilled) it runs 2% faster; the FP64-sum form gains
+// nothing from the cap and keeps its registers.
 template <bool GATHER, bool LAST, bool MIXED, bool SEG, bool PAIR = false, bool FUSED = false>
-__global__ void __launch_bounds__(kNodeThreads) k_update(UpdateArgs A) {
+__global__ void __launch_bounds__(kNodeThreads, (FUSED && PAIR) ? 10 : 1) k_update(UpdateArgs A) {
   __shared__ double srms[LAST ? kNodeThreads : 1];
   __shared__ double srho[LAST ? kNodeThreads : 1];
   __shared__ int sbad[LAST ? kNodeThreads : 1];
