@@ -117,8 +117,8 @@ class ClockSampler:
         mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows)}
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_min_mhz": min(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
 
 
 def run_gb300(args):
@@ -379,30 +379,33 @@ def run_batch(args):
         return statistics.median(ts), outs
 
     repeats = 3
-    t0 = time.perf_counter()
-    solve_sequential(precision="fp64")  # warm-up pass (pool, graphs, clocks)
-    line["warmup_s"] = round(time.perf_counter() - t0, 3)
-    line["timing"] = f"median wall time of {repeats} runs, each from host meshes to level-0 results on the host"
-    t_seq, seq = timed(solve_sequential, precision="fp64")
-    results = {"sequential_fp64": nm / t_seq}
-    for prec in ("fp64", "mixed"):
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as sampler:
         t0 = time.perf_counter()
-        best, timings = autotune.tune_batch(meshes, machs, aoas, precision=prec)
-        t_tune = time.perf_counter() - t0
-        solve_batch(**best)
-        dt, outs = timed(solve_batch, **best)
-        results[f"batched_{prec}"] = nm / dt
-        err = max(float(np.max(np.abs(a - b) / np.maximum(np.abs(b).max(axis=0), 1e-300))) for a, b in zip(outs, seq))
-        line[f"batched_{prec}_tuning"] = {"chosen": best, "ms_per_cycle": {f"{k[0]}/{k[1]}": round(v, 3)
-                                                                           for k, v in timings.items()},
-                                          "tuning_s": round(t_tune, 3), "max_rel_err_vs_fp64_sequential": err}
-        if prec == "mixed":  # the same batch with compensated FP32-pair node sums
-            pair = dict(best, accumulation="pair32")
-            solve_batch(**pair)
-            dt, outs = timed(solve_batch, **pair)
-            results["batched_mixed_pair32"] = nm / dt
-            line["batched_mixed_pair32_max_rel_err_vs_fp64_sequential"] = max(
-                float(np.max(np.abs(a - b) / np.maximum(np.abs(b).max(axis=0), 1e-300))) for a, b in zip(outs, seq))
+        solve_sequential(precision="fp64")  # warm-up pass (pool, graphs, clocks)
+        line["warmup_s"] = round(time.perf_counter() - t0, 3)
+        line["timing"] = f"median wall time of {repeats} runs, each from host meshes to level-0 results on the host"
+        t_seq, seq = timed(solve_sequential, precision="fp64")
+        results = {"sequential_fp64": nm / t_seq}
+        for prec in ("fp64", "mixed"):
+            t0 = time.perf_counter()
+            best, timings = autotune.tune_batch(meshes, machs, aoas, precision=prec)
+            t_tune = time.perf_counter() - t0
+            solve_batch(**best)
+            dt, outs = timed(solve_batch, **best)
+            results[f"batched_{prec}"] = nm / dt
+            err = max(float(np.max(np.abs(a - b) / np.maximum(np.abs(b).max(axis=0), 1e-300)))
+                      for a, b in zip(outs, seq))
+            line[f"batched_{prec}_tuning"] = {"chosen": best, "ms_per_cycle": {f"{k[0]}/{k[1]}": round(v, 3)
+                                                                               for k, v in timings.items()},
+                                              "tuning_s": round(t_tune, 3), "max_rel_err_vs_fp64_sequential": err}
+            if prec == "mixed":  # the same batch with compensated FP32-pair node sums
+                pair = dict(best, accumulation="pair32")
+                solve_batch(**pair)
+                dt, outs = timed(solve_batch, **pair)
+                results["batched_mixed_pair32"] = nm / dt
+                line["batched_mixed_pair32_max_rel_err_vs_fp64_sequential"] = max(
+                    float(np.max(np.abs(a - b) / np.maximum(np.abs(b).max(axis=0), 1e-300))) for a, b in zip(outs, seq))
+    line["clocks"] = sampler.summary()
     line["value"] = round(results["batched_fp64"], 3)
     line["results_solves_per_s"] = {k: round(v, 3) for k, v in results.items()}
     line["speedup_batched_fp64_vs_sequential"] = round(results["batched_fp64"] / results["sequential_fp64"], 3)
@@ -478,10 +481,11 @@ def run_serve(args):
                 "resident_mesh_hits": int(st["cache_hits"])}
 
     serve("served_mixed", 0)  # warm-up: CUDA context, memory pool, module load
-    capacity = {f: serve(f, 0) for f in forms}
-    plain_cap = capacity["plain_fp64"]["solves_per_s"]
-    rates = [f * plain_cap for f in args.serve_rate_multiples]
-    sweep = {f: [serve(f, r) for r in rates] for f in forms}
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as sampler:
+        capacity = {f: serve(f, 0) for f in forms}
+        plain_cap = capacity["plain_fp64"]["solves_per_s"]
+        rates = [f * plain_cap for f in args.serve_rate_multiples]
+        sweep = {f: [serve(f, r) for r in rates] for f in forms}
     cap = {f: capacity[f]["solves_per_s"] for f in forms}
     line = {"metric": "served solves/s and p50/p99 latency (Poisson stream), vs the plain FP64 path",
             "unit": "solves/s", "higher_is_better": True, "n_gpus": 1,
@@ -495,7 +499,7 @@ def run_serve(args):
             "speedup_served_mixed_vs_plain_fp64": round(cap["served_mixed"] / cap["plain_fp64"], 3),
             "speedup_served_mixed_pair32_vs_plain_fp64": round(cap["served_mixed_pair32"] / cap["plain_fp64"], 3),
             "speedup_served_fp64_vs_plain_fp64": round(cap["served_fp64"] / cap["plain_fp64"], 3),
-            "capacity_runs": capacity, "sweep": sweep}
+            "capacity_runs": capacity, "sweep": sweep, "clocks": sampler.summary()}
     print(json.dumps(line), flush=True)
 
 
