@@ -422,10 +422,11 @@ __device__ __forceinline__ void block_norms(double* srms, double* srho, int* sba
 // everything on min_dt < 0 or NaN/Inf (the reference aborts); batched
 // solvers mark the failing mesh and leave the others running.  The fused
 // stage with pair sums is latency-bound: capped at 48 registers (10 blocks
-// per SM, a few bytes spilled) it runs 2% faster; the FP64-sum form gains
-// nothing from the cap and keeps its registers.
+// per SM, a few bytes spilled) it runs 2% faster.  Every other form keeps the
+// compiler's own register choice: a minimum of 0 blocks is no constraint,
+// whereas a minimum of 1 lets it grow to 70-80 registers and lose occupancy.
 template <bool GATHER, bool LAST, bool MIXED, bool SEG, bool PAIR = false, bool FUSED = false>
-__global__ void __launch_bounds__(kNodeThreads, (FUSED && PAIR) ? 10 : 1) k_update(UpdateArgs A) {
+__global__ void __launch_bounds__(kNodeThreads, (FUSED && PAIR) ? 10 : 0) k_update(UpdateArgs A) {
   __shared__ double srms[LAST ? kNodeThreads : 1];
   __shared__ double srho[LAST ? kNodeThreads : 1];
   __shared__ int sbad[LAST ? kNodeThreads : 1];
