@@ -121,6 +121,27 @@ class ClockSampler:
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
 
 
+def pinned_levels(levels, keep):
+    """Copies of a mesh's level arrays in page-locked host memory (the inputs
+    of the end-to-end, batch and serve measurements); `keep` holds the
+    buffers alive."""
+    import numpy as np
+    import torch
+
+    import mgcfd
+
+    def pin(a):
+        if a is None:
+            return None
+        t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+        keep.append(t)
+        return t.numpy()
+
+    return [mgcfd.Level(coords=pin(L.coords), edge_to_nodes=pin(L.edge_to_nodes), bnd_to_node=pin(L.bnd_to_node),
+                        bnd_group=pin(L.bnd_group), edge_weights=pin(L.edge_weights), bnd_weights=pin(L.bnd_weights),
+                        node_to_mg=pin(L.node_to_mg), n_axis=L.n_axis, volumes=pin(L.volumes)) for L in levels]
+
+
 def run_gb300(args):
     import ctypes as C
 
@@ -185,15 +206,7 @@ def run_gb300(args):
     # End to end through the host-buffer entry point, pinned host memory.
     levels = mesh.levels()
     pinned = []
-
-    def pin(a):
-        t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
-        pinned.append(t)
-        return t.numpy()
-
-    hl = [mgcfd.Level(coords=pin(L.coords), edge_to_nodes=pin(L.edge_to_nodes), bnd_to_node=pin(L.bnd_to_node),
-                      bnd_group=pin(L.bnd_group), edge_weights=pin(L.edge_weights), bnd_weights=pin(L.bnd_weights),
-                      node_to_mg=pin(L.node_to_mg) if L.node_to_mg is not None else None) for L in levels]
+    hl = pinned_levels(levels, pinned)
     outs = [torch.empty((L.nnodes, 5), dtype=torch.float64).pin_memory() for L in levels]
     views = mgcfd.level_views_from_arrays(hl)
     out_ptrs = (_lib.c_double_p * len(outs))(*[C.cast(o.data_ptr(), _lib.c_double_p) for o in outs])
@@ -332,8 +345,9 @@ def run_reference(args):
 def run_batch(args):
     """Batched solves: 64 meshes (lattice edge log-uniform 16..96, Mach U(0.3, 0.8),
     AoA U(0, 6) degrees, 3 levels, 20 V-cycles) solved in one batch against 64
-    sequential plain solves.  Every solve is timed through the host-buffer API:
-    upload, device setup, the V-cycles and the download of level 0."""
+    sequential plain solves.  Every solve is timed through the host-buffer API
+    from page-locked host buffers: upload, device setup, the V-cycles and the
+    download of level 0."""
     import numpy as np
     import torch  # noqa: F401  (CUDA context for the timers below)
 
@@ -344,9 +358,11 @@ def run_batch(args):
     sizes = np.exp(rng.uniform(np.log(16), np.log(96), nm)).round().astype(int)
     machs = rng.uniform(0.3, 0.8, nm).tolist()
     aoas = rng.uniform(0.0, 6.0, nm).tolist()
-    meshes = [mgcfd.HostMesh.generate(int(n), 3, 1000 + i) for i, n in enumerate(sizes)]
+    host_meshes = [mgcfd.HostMesh.generate(int(n), 3, 1000 + i) for i, n in enumerate(sizes)]
+    keep = []
+    meshes = [pinned_levels(m.levels(), keep) for m in host_meshes]  # inputs in page-locked host memory
     cycles = 20
-    total_nodes = sum(m.level(0).nnodes for m in meshes)
+    total_nodes = sum(m[0].nnodes for m in meshes)
 
     def solve_batch(**o):
         b = mgcfd.Batch(meshes, machs, aoas, **o)
@@ -369,7 +385,7 @@ def run_batch(args):
     line = {"metric": f"batched solves/s ({nm} meshes, 16^3-96^3 lattices, 3 levels, {cycles} V-cycles)",
             "unit": "solves/s", "higher_is_better": True, "n_gpus": 1, "data": "synthetic: seeded lattices",
             "config": {"workload": f"{nm} meshes, {total_nodes} level-0 nodes in total, sizes {sizes.min()}^3.."
-                                   f"{sizes.max()}^3"}}
+                                   f"{sizes.max()}^3", "inputs": "page-locked host memory"}}
     def timed(fn, **o):  # median wall time of `repeats` runs, and the last run's results
         ts = []
         for _ in range(repeats):
@@ -431,11 +447,12 @@ def run_serve(args):
 
     import mgcfd
     rng = np.random.default_rng(11)
-    pool = []
+    pool, keep = [], []
     for i in range(args.serve_pool):
         nodes = float(np.exp(rng.uniform(np.log(20e3), np.log(4e6))))
         n = max(8, int(round(nodes ** (1.0 / 3.0))))
-        pool.append(mgcfd.HostMesh.generate(n, int(rng.integers(3, 5)), 500 + i))
+        m = mgcfd.HostMesh.generate(n, int(rng.integers(3, 5)), 500 + i)
+        pool.append(pinned_levels(m.levels(), keep))  # requests arrive in page-locked host memory
     R = args.serve_requests
     picks = rng.integers(0, len(pool), R)
     machs = rng.uniform(0.3, 0.85, R)
@@ -460,7 +477,8 @@ def run_serve(args):
                 delay = t_start + arrivals[k] - time.perf_counter()
                 if delay > 0:
                     time.sleep(delay)
-                srv.submit(pool[picks[k]], float(machs[k]), float(aoas[k]), resident=resident[form])
+                key = int(picks[k]) + 1 if resident[form] else None  # same pool mesh = same resident mesh
+                srv.submit(pool[picks[k]], float(machs[k]), float(aoas[k]), mesh_key=key, resident=resident[form])
 
         th = threading.Thread(target=feeder)
         th.start()
@@ -491,10 +509,11 @@ def run_serve(args):
             "unit": "solves/s", "higher_is_better": True, "n_gpus": 1,
             "data": "synthetic: seeded jittered lattices",
             "config": {"workload": f"{R} requests over a pool of {len(pool)} meshes "
-                                   f"({min(m.level(0).nnodes for m in pool)}..{max(m.level(0).nnodes for m in pool)} "
+                                   f"({min(m[0].nnodes for m in pool)}..{max(m[0].nnodes for m in pool)} "
                                    "level-0 nodes, 3-4 levels), 50 V-cycles or residual drop 1e-6, "
                                    "HBM budget 150 GB",
-                       "slots": args.serve_slots, "rate_multiples_of_plain_capacity": args.serve_rate_multiples},
+                       "slots": args.serve_slots, "rate_multiples_of_plain_capacity": args.serve_rate_multiples,
+                       "inputs": "page-locked host memory"},
             "value": cap["served_mixed"], "capacity_solves_per_s": cap,
             "speedup_served_mixed_vs_plain_fp64": round(cap["served_mixed"] / cap["plain_fp64"], 3),
             "speedup_served_mixed_pair32_vs_plain_fp64": round(cap["served_mixed_pair32"] / cap["plain_fp64"], 3),
