@@ -388,6 +388,27 @@ __device__ __forceinline__ void add_boundary(const NodePrim& p, const double* __
   F[3] += b[5] * p.p;
 }
 
+// A node's edges in the gather order: those where it is end a (a contiguous
+// range of the edge list), then those where it is end b (through b_list).  The
+// node kernels walk both in one loop of deg iterations, so every lane of a
+// warp runs as many iterations as its own node has edges.  With one loop per
+// end, a warp ran each loop for its lane with the most edges of that end (the
+// a/b split of a node's edges varies with the numbering) and issued the FP64
+// adds for the idle lanes too.
+struct EdgeRange {
+  int32_t a0, na, b0, deg;
+};
+
+template <class Args>
+__device__ __forceinline__ EdgeRange edge_range(const Args& A, int64_t i) {
+  EdgeRange r;
+  r.a0 = A.a_off[i];
+  r.na = A.a_off[i + 1] - r.a0;
+  r.b0 = A.b_off[i];
+  r.deg = r.na + (A.b_off[i + 1] - r.b0);
+  return r;
+}
+
 // Level-0 norms of one block of kNodeThreads threads (every thread arrives):
 // sums through shared memory, halving the active threads each step down to
 // one warp, so every FP64 add is a useful one (a shuffle tree in each warp
@@ -481,20 +502,20 @@ __global__ void __launch_bounds__(kNodeThreads, (FUSED && PAIR) ? 10 : 0) k_upda
 #pragma unroll
       for (int k = 0; k < 5; k++) F[k] = 0.0;
       float f[5];
-      for (int32_t e = A.a_off[i]; e < A.a_off[i + 1]; e++) {
-        edge_flux_f32(me, load_rec32(A.rec32_in, A.e2n[e].y), A.w4f[e], f);
+      const EdgeRange er = edge_range(A, i);
+      for (int32_t j = 0; j < er.deg; j++) {
+        const bool end_a = j < er.na;
+        const int32_t ja = end_a ? er.a0 + j : 0, jb = end_a ? 0 : er.b0 + j - er.na;  // both in range
+        const NodePrimF o = load_rec32(A.rec32_in, end_a ? A.e2n[ja].y : A.b_nbr[jb]);
+        const float4 w = end_a ? A.w4f[ja] : A.b_w4f[jb];
+        NodePrimF ea = me, eb = o;  // the edge's end a and end b
+        if (!end_a) { ea = o; eb = me; }
+        edge_flux_f32(ea, eb, w, f);
 #pragma unroll
         for (int k = 0; k < 5; k++) {
-          if (PAIR) two_sum_acc(hi[k], lo[k], f[k]);
-          else F[k] += f2d_bits(f[k]);
-        }
-      }
-      for (int32_t j = A.b_off[i]; j < A.b_off[i + 1]; j++) {
-        edge_flux_f32(load_rec32(A.rec32_in, A.b_nbr[j]), me, A.b_w4f[j], f);
-#pragma unroll
-        for (int k = 0; k < 5; k++) {
-          if (PAIR) two_sum_acc(hi[k], lo[k], -f[k]);
-          else F[k] -= f2d_bits(f[k]);
+          const float x = end_a ? f[k] : -f[k];  // node b receives -f
+          if (PAIR) two_sum_acc(hi[k], lo[k], x);
+          else F[k] += f2d_bits(x);
         }
       }
       if (PAIR) {
@@ -505,26 +526,35 @@ __global__ void __launch_bounds__(kNodeThreads, (FUSED && PAIR) ? 10 : 0) k_upda
       // Unevaluated FP32 pairs (hi, lo) fed by error-free TwoSum steps;
       // one FP64 add per variable at the end.
       float hi[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, lo[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-      for (int32_t e = A.a_off[i]; e < A.a_off[i + 1]; e++)
+      const EdgeRange er = edge_range(A, i);
+      for (int32_t j = 0; j < er.deg; j++) {
+        const bool end_a = j < er.na;
+        const int64_t e = end_a ? er.a0 + j : A.b_list[end_a ? 0 : er.b0 + j - er.na];
 #pragma unroll
-        for (int k = 0; k < 5; k++) two_sum_acc(hi[k], lo[k], A.fe32[5 * (int64_t)e + k]);
-      for (int32_t j = A.b_off[i]; j < A.b_off[i + 1]; j++) {
-        const int64_t e = A.b_list[j];
-#pragma unroll
-        for (int k = 0; k < 5; k++) two_sum_acc(hi[k], lo[k], -A.fe32[5 * e + k]);
+        for (int k = 0; k < 5; k++) {
+          const float x = A.fe32[5 * e + k];
+          two_sum_acc(hi[k], lo[k], end_a ? x : -x);
+        }
       }
 #pragma unroll
       for (int k = 0; k < 5; k++) F[k] = f2d_bits(hi[k]) + f2d_bits(lo[k]);
     } else if (GATHER) {
 #pragma unroll
       for (int k = 0; k < 5; k++) F[k] = 0.0;
-      for (int32_t e = A.a_off[i]; e < A.a_off[i + 1]; e++)
+      const EdgeRange er = edge_range(A, i);
+      for (int32_t j = 0; j < er.deg; j++) {
+        const bool end_a = j < er.na;
+        const int64_t e = end_a ? er.a0 + j : A.b_list[end_a ? 0 : er.b0 + j - er.na];
 #pragma unroll
-        for (int k = 0; k < 5; k++) F[k] += MIXED ? f2d_bits(A.fe32[5 * (int64_t)e + k]) : A.fe[5 * (int64_t)e + k];
-      for (int32_t j = A.b_off[i]; j < A.b_off[i + 1]; j++) {
-        const int64_t e = A.b_list[j];
-#pragma unroll
-        for (int k = 0; k < 5; k++) F[k] -= MIXED ? f2d_bits(A.fe32[5 * e + k]) : A.fe[5 * e + k];
+        for (int k = 0; k < 5; k++) {  // F - x as F + (-x): the same bits, one add instruction for both ends
+          if (MIXED) {
+            const float x = A.fe32[5 * e + k];
+            F[k] += f2d_bits(end_a ? x : -x);
+          } else {
+            const double x = A.fe[5 * e + k];
+            F[k] += end_a ? x : negate(x);
+          }
+        }
       }
     } else {
       double* fl = A.flux + 5 * i;
