@@ -558,7 +558,8 @@ def main():
     ap.add_argument("--batch-meshes", type=int, default=64)
     ap.add_argument("--serve-requests", type=int, default=240)
     ap.add_argument("--serve-pool", type=int, default=24)
-    ap.add_argument("--serve-rate-multiples", type=float, nargs="+", default=[0.5, 0.9, 2.0])
+    ap.add_argument("--serve-rate-multiples", type=float, nargs="*", default=[0.5, 0.9, 2.0],
+                    help="Poisson rates as multiples of the plain path's capacity (none: capacity only)")
     ap.add_argument("--serve-slots", type=int, default=16)
     args = ap.parse_args()
     if args.warmup < 0 or args.steps < 1:
