@@ -309,7 +309,8 @@ int mgcfd_solver_num_meshes(const mgcfd_solver* s);
 int mgcfd_solver_fetch_mesh(mgcfd_solver* s, int32_t mesh, int32_t level, int32_t quantity, double* host_out);
 /* Synchronises; returns mesh `mesh`'s status (MGCFD_OK, MGCFD_ERR_NEGATIVE_DT
  * or MGCFD_ERR_BAD_VALUES) and its last level-0 residual norms (all
- * variables as euler3d.cpp:537, and density only); either output may be NULL. */
+ * variables as euler3d.cpp:537, and density only); either output may be NULL.
+ * A plain (one-mesh) solver is mesh 0. */
 int mgcfd_solver_mesh_status(mgcfd_solver* s, int32_t mesh, double* rms_l0, double* rho_rms_l0);
 /* Back to the state right after create (freestream, counters zeroed). */
 int mgcfd_solver_reset(mgcfd_solver* s);
