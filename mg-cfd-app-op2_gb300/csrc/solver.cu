@@ -251,7 +251,10 @@ __global__ void __launch_bounds__(kNodeThreads) k_step_begin(int32_t n, double* 
   if (threadIdx.x < 32) {
     key = threadIdx.x < kNodeThreads / 32 ? smin[threadIdx.x] : ~0ull;
     key = warp_min_u64(key);
-    if (threadIdx.x == 0 && key != ~0ull) atomicMin(dt_key, key);
+    // Keys only decrease, so a block whose minimum is not below the current
+    // value skips its atomic: most of the grid's same-address atomics go away.
+    if (threadIdx.x == 0 && key != ~0ull && key < *reinterpret_cast<volatile unsigned long long*>(dt_key))
+      atomicMin(dt_key, key);
   }
 }
 
