@@ -345,7 +345,8 @@ enum {
   MGCFD_T_CH_LIST = 11,  /* int32 [N_fine]                                                */
   MGCFD_T_A_OFF = 12,    /* int32 [N+1]    gather strategy only                          */
   MGCFD_T_B_OFF = 13,    /* int32 [N+1]    gather strategy only                          */
-  MGCFD_T_B_LIST = 14    /* int32 [E]      gather strategy only                          */
+  MGCFD_T_B_LIST = 14,   /* int32 [E]      gather strategy only                          */
+  MGCFD_T_WEIGHTS32 = 15 /* f32   [E][4]   the same as WEIGHTS, mixed precision only      */
 };
 /* Copies table `table` of `level` into host_out if capacity_bytes suffices;
  * *bytes receives the table's size (0 if the table does not exist).  With

@@ -6,7 +6,9 @@
 //   * geometry: calculate_cell_volumes + dampen_ewt (misc.h:40-84) per edge
 //     with explicitly rounded operations, and each node's volume summed over
 //     its incident edges in increasing edge id -- the reference's sequential
-//     order, so volumes are bit-identical to the reference;
+//     order, so volumes are bit-identical to the reference (the mixed-
+//     precision form computes the per-edge geometry in FP32 and sums the
+//     volumes in FP64);
 //   * edges oriented a < b and stably sorted by (a, b); CSR tables by counting
 //     and prefix sums;
 //   * boundary entries folded per node in entry order; multigrid tables.
@@ -222,8 +224,17 @@ __device__ __forceinline__ double sq3(double a, double b, double c) {
   return __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), __dmul_rn(c, c));
 }
 
+// FP32 geometry of the mixed-precision form, the same steps in FP32 (IEEE
+// round-to-nearest; setup.cpp computes the same on the host): the coordinate
+// differences and the input weights are taken in FP64 and rounded once.
+__device__ __forceinline__ float sq3f(float a, float b, float c) {
+  return __fadd_rn(__fadd_rn(__fmul_rn(a, a), __fmul_rn(b, b)), __fmul_rn(c, c));
+}
+
 // Per edge: global input end nodes (-1 where the entry is out of range),
-// volume contribution tv and damped weights w.
+// volume contribution tv and damped weights w (F32: computed in FP32 and
+// stored widened, for the mixed-precision form).
+template <bool F32>
 __global__ void k_edge_geometry(int32_t ne, Seg g, const int32_t* __restrict__ e2n, const double* __restrict__ xyz,
                                 const double* __restrict__ ewt_in, int32_t* __restrict__ ge2n,
                                 double* __restrict__ tv, double* __restrict__ w, unsigned* __restrict__ err) {
@@ -249,6 +260,16 @@ __global__ void k_edge_geometry(int32_t ne, Seg g, const int32_t* __restrict__ e
   }
   double d[3];
   for (int i = 0; i < 3; i++) d[i] = __dsub_rn(xyz[3 * (int64_t)b + i], xyz[3 * (int64_t)a + i]);
+  if (F32) {
+    float df[3], wf[3];
+    for (int i = 0; i < 3; i++) { df[i] = d2f_bits(d[i]); wf[i] = d2f_bits(wi[i]); }
+    const float dist = __fsqrt_rn(sq3f(df[0], df[1], df[2]));
+    const float area = __fsqrt_rn(sq3f(wf[0], wf[1], wf[2]));
+    tv[e] = f2d_bits(__fmul_rn(__fmul_rn((float)((1.0 / 3.0) * 0.5), dist), area));
+    for (int i = 0; i < 3; i++)
+      w[3 * e + i] = f2d_bits(__fmul_rn(__fdiv_rn(__fmul_rn(__fdiv_rn(df[i], dist), area), dist), 1e-7f));
+    return;
+  }
   const double dist = __dsqrt_rn(sq3(d[0], d[1], d[2]));
   const double area = __dsqrt_rn(sq3(wi[0], wi[1], wi[2]));
   tv[e] = __dmul_rn(__dmul_rn((1.0 / 3.0) * 0.5, dist), area);
@@ -309,6 +330,7 @@ __global__ void k_edge_keys(int32_t ne, const int32_t* __restrict__ ge2n, const 
   flip[e] = f;
 }
 
+template <bool F32>
 __global__ void k_edge_finalize(int32_t ne, Seg g, const unsigned long long* __restrict__ key,
                                 const int32_t* __restrict__ order, const double* __restrict__ w,
                                 const unsigned char* __restrict__ flip, int2* __restrict__ e2n,
@@ -321,11 +343,20 @@ __global__ void k_edge_finalize(int32_t ne, Seg g, const unsigned long long* __r
   e2n[k] = make_int2(a, b);
   double x = w[3 * e], y = w[3 * e + 1], z = w[3 * e + 2];
   if (flip[e]) { x = -x; y = -y; z = -z; }
-  const double mag = __dsqrt_rn(sq3(x, y, z));
-  w4[4 * k + 0] = __dmul_rn(-0.5, x);
-  w4[4 * k + 1] = __dmul_rn(-0.5, y);
-  w4[4 * k + 2] = __dmul_rn(-0.5, z);
-  w4[4 * k + 3] = __dmul_rn(__dmul_rn(-mag, sc), 0.5);
+  if (F32) {  // the FP32 weights, stored widened (exact)
+    const float xf = d2f_bits(x), yf = d2f_bits(y), zf = d2f_bits(z);
+    const float mag = __fsqrt_rn(sq3f(xf, yf, zf));
+    w4[4 * k + 0] = f2d_bits(__fmul_rn(-0.5f, xf));
+    w4[4 * k + 1] = f2d_bits(__fmul_rn(-0.5f, yf));
+    w4[4 * k + 2] = f2d_bits(__fmul_rn(-0.5f, zf));
+    w4[4 * k + 3] = f2d_bits(__fmul_rn(__fmul_rn(-mag, d2f_bits(sc)), 0.5f));
+  } else {
+    const double mag = __dsqrt_rn(sq3(x, y, z));
+    w4[4 * k + 0] = __dmul_rn(-0.5, x);
+    w4[4 * k + 1] = __dmul_rn(-0.5, y);
+    w4[4 * k + 2] = __dmul_rn(-0.5, z);
+    w4[4 * k + 3] = __dmul_rn(__dmul_rn(-mag, sc), 0.5);
+  }
   atomicAdd(acnt + a, 1);
   atomicAdd(bcnt + b, 1);
 }
@@ -608,7 +639,8 @@ int device_prepare(mgcfd_solver* s, const std::vector<MeshInput>& meshes) {
     int32_t* ge2n;
     if ((r = tmp.get(&tv, (size_t)NE)) || (r = tmp.get(&wd, 3 * (size_t)NE)) || (r = tmp.get(&ge2n, 2 * (size_t)NE)))
       return r;
-    if (NE) k_edge_geometry<<<nblk(NE), T, 0, st>>>(NE, g, I.e2n, I.xyz, I.ewt, ge2n, tv, wd, err);
+    if (NE && mixed) k_edge_geometry<true><<<nblk(NE), T, 0, st>>>(NE, g, I.e2n, I.xyz, I.ewt, ge2n, tv, wd, err);
+    else if (NE) k_edge_geometry<false><<<nblk(NE), T, 0, st>>>(NE, g, I.e2n, I.xyz, I.ewt, ge2n, tv, wd, err);
     if (any_computed_volumes) {
       int32_t *ikey, *ival, *ikey2, *ival2, *cnt, *off;
       if ((r = tmp.get(&ikey, 2 * (size_t)NE)) || (r = tmp.get(&ival, 2 * (size_t)NE)) ||
@@ -637,7 +669,8 @@ int device_prepare(mgcfd_solver* s, const std::vector<MeshInput>& meshes) {
       if (NE) {
         k_edge_keys<<<nblk(NE), T, 0, st>>>(NE, ge2n, I.inv, key, val, flip);
         if ((r = sort_pairs(tmp, key, key2, val, order, NE, 32 + bits_for(N), st))) return r;
-        k_edge_finalize<<<nblk(NE), T, 0, st>>>(NE, g, key2, order, wd, flip, D.e2n, w4all, acnt, bcnt);
+        if (mixed) k_edge_finalize<true><<<nblk(NE), T, 0, st>>>(NE, g, key2, order, wd, flip, D.e2n, w4all, acnt, bcnt);
+        else k_edge_finalize<false><<<nblk(NE), T, 0, st>>>(NE, g, key2, order, wd, flip, D.e2n, w4all, acnt, bcnt);
       }
       if (s->gather) {
         int32_t *bkey, *bval, *bkey2;

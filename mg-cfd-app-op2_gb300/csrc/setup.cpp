@@ -158,7 +158,7 @@ int validate_views(int32_t nlevels, const mgcfd_level_view* lv, bool check_maps)
 }
 
 int prepare_mesh(int32_t nlevels, const mgcfd_level_view* lv, const mgcfd_freestream& ff, int renumber,
-                 std::vector<PreparedLevel>* out) {
+                 bool fp32_geometry, std::vector<PreparedLevel>* out) {
   int vr = validate_views(nlevels, lv, true);
   if (vr) return vr;
   out->assign((size_t)nlevels, PreparedLevel());
@@ -184,7 +184,24 @@ int prepare_mesh(int32_t nlevels, const mgcfd_level_view* lv, const mgcfd_freest
       for (int32_t i = 0; i < n; i++) vol_in[(size_t)i] = v.volumes[i];
       for (size_t k = 0; k < ewt.size(); k++) ewt[k] = v.edge_weights[k] * 1e-7;
     }
-    for (int32_t e = 0; e < ne && !v.volumes; e++) {
+    for (int32_t e = 0; e < ne && !v.volumes && fp32_geometry; e++) {
+      // The mixed-precision form's geometry: the same steps in FP32, from the
+      // FP64 coordinate differences and input weights rounded once (the
+      // device computes the same, device_setup.cu).
+      const int32_t a = v.edge_to_nodes[2 * (size_t)e], b = v.edge_to_nodes[2 * (size_t)e + 1];
+      float d[3], wf[3];
+      for (int i = 0; i < 3; i++) {
+        d[i] = (float)(v.coords[3 * (size_t)b + i] - v.coords[3 * (size_t)a + i]);
+        wf[i] = (float)v.edge_weights[3 * (size_t)e + i];
+      }
+      const float dist = std::sqrt((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]);
+      const float area = std::sqrt((wf[0] * wf[0] + wf[1] * wf[1]) + wf[2] * wf[2]);
+      const float tv = ((float)((1.0 / 3.0) * 0.5) * dist) * area;
+      vol_in[(size_t)a] += (double)tv;
+      vol_in[(size_t)b] += (double)tv;
+      for (int i = 0; i < 3; i++) ewt[3 * (size_t)e + i] = (double)((((d[i] / dist) * area) / dist) * 1e-7f);
+    }
+    for (int32_t e = 0; e < ne && !v.volumes && !fp32_geometry; e++) {
       const int32_t a = v.edge_to_nodes[2 * (size_t)e], b = v.edge_to_nodes[2 * (size_t)e + 1];
       double d[3], dist = 0.0, area = 0.0;
       for (int i = 0; i < 3; i++) {
@@ -236,6 +253,15 @@ int prepare_mesh(int32_t nlevels, const mgcfd_level_view* lv, const mgcfd_freest
       P.e2n[2 * (size_t)k] = na[(size_t)e];
       P.e2n[2 * (size_t)k + 1] = nb_[(size_t)e];
       const double* w = &ewt[3 * (size_t)e];
+      if (fp32_geometry) {
+        const float x = (float)w[0], y = (float)w[1], z = (float)w[2];
+        const float mag = std::sqrt((x * x + y * y) + z * z);
+        P.w4[4 * (size_t)k + 0] = (double)(-0.5f * x);
+        P.w4[4 * (size_t)k + 1] = (double)(-0.5f * y);
+        P.w4[4 * (size_t)k + 2] = (double)(-0.5f * z);
+        P.w4[4 * (size_t)k + 3] = (double)((-mag * (float)sc) * 0.5f);
+        continue;
+      }
       const double mag = std::sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
       P.w4[4 * (size_t)k + 0] = -0.5 * w[0];  // flux.h:147 factor_x etc.
       P.w4[4 * (size_t)k + 1] = -0.5 * w[1];

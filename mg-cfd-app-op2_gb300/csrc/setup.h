@@ -36,9 +36,12 @@ struct PreparedLevel {
 // Sizes, null pointers and (when check_maps) every map entry of the views.
 int validate_views(int32_t nlevels, const mgcfd_level_view* levels, bool check_maps);
 
-// Returns MGCFD_OK or an error status (message via set_error).
+// Returns MGCFD_OK or an error status (message via set_error).  With
+// fp32_geometry (the mixed-precision form) the per-edge geometry -- volume
+// contributions, damped weights and |w| -- is computed in FP32; volumes are
+// still summed in FP64.
 int prepare_mesh(int32_t nlevels, const mgcfd_level_view* levels, const mgcfd_freestream& ff, int renumber,
-                 std::vector<PreparedLevel>* out);
+                 bool fp32_geometry, std::vector<PreparedLevel>* out);
 
 // Node orderings (new id -> input id).
 void spatial_order(const double* xyz, int32_t n, std::vector<int32_t>* perm);

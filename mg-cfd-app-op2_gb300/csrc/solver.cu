@@ -1112,7 +1112,7 @@ extern "C" int mgcfd_solver_create(int32_t nlevels, const mgcfd_level_view* leve
     s->seg_noff.assign((size_t)nlevels, std::vector<int32_t>(2, 0));
     for (int l = 0; l < nlevels; l++) s->seg_noff[(size_t)l][1] = levels[l].nnodes;
     try {
-      r = prepare_mesh(nlevels, levels, s->ff, s->opt.renumber, &P);
+      r = prepare_mesh(nlevels, levels, s->ff, s->opt.renumber, s->opt.precision == MGCFD_PRECISION_MIXED, &P);
     } catch (const std::bad_alloc&) {
       return set_error(MGCFD_ERR_NOMEM, "host allocation failed while preparing the mesh");
     }
@@ -1434,6 +1434,7 @@ extern "C" int mgcfd_solver_table(mgcfd_solver* s, int32_t level, int32_t table,
     case MGCFD_T_A_OFF: src = D.a_off; n = D.a_off ? 4ll * (D.n + 1) : 0; break;
     case MGCFD_T_B_OFF: src = D.b_off; n = D.b_off ? 4ll * (D.n + 1) : 0; break;
     case MGCFD_T_B_LIST: src = D.b_list; n = D.b_list ? 4ll * D.ne : 0; break;
+    case MGCFD_T_WEIGHTS32: src = D.w4f; n = D.w4f ? 16ll * D.ne : 0; break;
     default: return set_error(MGCFD_ERR_INVALID, "mgcfd_solver_table: unknown table");
   }
   *bytes = src ? n : 0;

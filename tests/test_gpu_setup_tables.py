@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 TABLES = {0: ("PERM", np.int32), 1: ("EDGES", np.int32), 2: ("WEIGHTS", np.float64), 3: ("VOLUMES", np.float64),
           4: ("INV_VOL", np.float64), 5: ("CBRT_VOL", np.float64), 6: ("BIDX", np.int32), 7: ("BDATA", np.float64),
           8: ("N2MG", np.int32), 9: ("DVEC", np.float64), 10: ("CH_OFF", np.int32), 11: ("CH_LIST", np.int32),
-          12: ("A_OFF", np.int32), 13: ("B_OFF", np.int32), 14: ("B_LIST", np.int32)}
+          12: ("A_OFF", np.int32), 13: ("B_OFF", np.int32), 14: ("B_LIST", np.int32), 15: ("WEIGHTS32", np.float32)}
 
 
 def table(solver, level, t):
@@ -30,11 +30,14 @@ def table(solver, level, t):
     return out
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("n,nl,renumber", [(11, 3, "spatial"), (16, 4, "spatial"), (9, 2, "none"), (24, 3, "spatial")])
-def test_device_tables_equal_host_tables(n, nl, renumber):
+def test_device_tables_equal_host_tables(n, nl, renumber, precision):
+    """Mixed precision computes the per-edge geometry in FP32, on the device and
+    on the host alike: its weights and volumes must agree bit for bit too."""
     mesh = mgcfd.HostMesh.generate(n, nl, 300 + n)
-    dev = mgcfd.Solver(mesh, 0.8, 3.0, increment="gather", renumber=renumber)
-    host = mgcfd.Solver(mesh, 0.8, 3.0, increment="gather", renumber=renumber, host_setup=True)
+    dev = mgcfd.Solver(mesh, 0.8, 3.0, increment="gather", renumber=renumber, precision=precision)
+    host = mgcfd.Solver(mesh, 0.8, 3.0, increment="gather", renumber=renumber, host_setup=True, precision=precision)
     for l in range(nl):
         for t, (name, _) in TABLES.items():
             a, b = table(dev, l, t), table(host, l, t)
