@@ -171,7 +171,7 @@ double wall() {
 }
 
 int fail(int st) {
-  std::printf("%s\n", mgcfd_last_error());
+  std::printf("%s: %s\n", mgcfd_status_string(st), mgcfd_last_error());
   return 1;
 }
 
