@@ -17,6 +17,9 @@
 //   * factor_a == factor_b up to association order, so the edge flux is
 //     computed once and added to node a and subtracted from node b (the
 //     negation is a sign-bit flip on the integer pipe);
+//   * the dissipation fac * (x_a - x_b) joins the central terms' per-end
+//     coefficients: x_a * (u_a.h + fac) + x_b * (u_b.h - fac), two FMAs per
+//     variable instead of a subtraction, a multiplication and two FMAs;
 //   * |w| and -|w|*smoothing*0.5 are constant after setup and precomputed,
 //     and the weight is kept as h = -w/2 so the central term needs no
 //     multiplication by -1/2 (exact: a power-of-two scaling).
@@ -66,19 +69,26 @@ __device__ __forceinline__ NodePrim node_prim(double rho, double mx, double my, 
 
 // flux.h:41-208 for one edge: returns the increment f of node a; node b
 // receives -f.  h = -w/2 for the edge weight w, wfac = -|w| * smoothing_coefficient * 0.5.
-// About 35 FP64 operations.
+// With fac = wfac (s_a + s_b) the dissipation factor, ga = u_a.h + fac and
+// gb = u_b.h - fac:
+//   f_rho = rho_a ga + rho_b gb                    (rho_a u_a.h = m_a.h)
+//   f_m   = m_a ga + m_b gb + (p_a + p_b) h
+//   f_E   = E_a ga + E_b gb + p_a u_a.h + p_b u_b.h
+// 27 FP64 operations, each written as the FMA or operation it issues, so no
+// kernel that inlines this can contract it differently.
 __device__ __forceinline__ void edge_flux(const NodePrim& a, const NodePrim& b, double hx, double hy, double hz,
                                           double wfac, double f[5]) {
-  const double mha = a.mx * hx + a.my * hy + a.mz * hz;  // -(m_a . w)/2
-  const double mhb = b.mx * hx + b.my * hy + b.mz * hz;
-  const double uha = mha * a.rinv, uhb = mhb * b.rinv;    // -(u . w)/2
-  const double fac = wfac * (a.s + b.s);
+  const double mha = fma(a.mz, hz, fma(a.my, hy, a.mx * hx));  // -(m_a . w)/2
+  const double mhb = fma(b.mz, hz, fma(b.my, hy, b.mx * hx));
+  const double uha = mha * a.rinv, uhb = mhb * b.rinv;          // -(u . w)/2
+  const double sab = a.s + b.s;
+  const double ga = fma(wfac, sab, uha), gb = fma(-wfac, sab, uhb);
   const double pp = a.p + b.p;
-  f[0] = fac * (a.rho - b.rho) + (mha + mhb);
-  f[1] = fac * (a.mx - b.mx) + (a.mx * uha + b.mx * uhb + pp * hx);
-  f[2] = fac * (a.my - b.my) + (a.my * uha + b.my * uhb + pp * hy);
-  f[3] = fac * (a.mz - b.mz) + (a.mz * uha + b.mz * uhb + pp * hz);
-  f[4] = fac * (a.rhoE - b.rhoE) + ((a.rhoE + a.p) * uha + (b.rhoE + b.p) * uhb);
+  f[0] = fma(a.rho, ga, b.rho * gb);
+  f[1] = fma(a.mx, ga, fma(b.mx, gb, pp * hx));
+  f[2] = fma(a.my, ga, fma(b.my, gb, pp * hy));
+  f[3] = fma(a.mz, ga, fma(b.mz, gb, pp * hz));
+  f[4] = fma(a.rhoE, ga, fma(b.rhoE, gb, fma(a.p, uha, b.p * uhb)));
 }
 
 // -x by flipping the sign bit of the high word with an integer instruction.
