@@ -528,7 +528,7 @@ def run_rates(args):
     device copy), measured on this GPU: the denominators of the FP64 cost
     model the kernels are designed against."""
     from mgcfd import _build
-    src = _build.CSRC / "probes" / "fp64_rates.cu"
+    src = ROOT / "tests" / "native" / "fp64_rates.cu"  # a probe, not part of the library
     exe = _build.OBJ / "fp64_rates"
     exe.parent.mkdir(parents=True, exist_ok=True)
     subprocess.run([_build._nvcc(), *_build.ARCH, "-O3", "-std=c++17", f"-I{_build.CSRC}", str(src), "-o", str(exe)],

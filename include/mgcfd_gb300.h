@@ -216,7 +216,10 @@ int mgcfd_op_down(int32_t nfine, int32_t ncoarse, const int32_t* node_to_mg, dou
  * Every call shares the array and clears the part it uses; calls that
  * overlap on the GPU race and give wrong results.  The first call on each
  * device looks up the array's address (cudaGetSymbolAddress); make it
- * before any stream capture.  Out-of-range map entries are skipped. */
+ * before any stream capture (inside one it fails with MGCFD_ERR_INVALID).
+ * Calls outside a capture look the address up again, so it stays right
+ * after a cudaDeviceReset.  Out-of-range map entries are skipped and
+ * counted in mgcfd_op_map_errors. */
 int mgcfd_op_restrict_noalloc(int32_t nfine, int32_t ncoarse, const int32_t* node_to_mg,
                               const double* fine_variables, double* coarse_variables, void* stream);
 /* Number of elements the mapped entry points above skipped because a map

@@ -16,4 +16,8 @@ constexpr int kNVar = 5;         // const.h:38-41: [rho, rho*u, rho*v, rho*w, rh
 int set_error(int status, const std::string& msg);
 void clear_error();
 
+// Skips counted by mgcfd_op_restrict_noalloc (restrict_noalloc.cu), which
+// mgcfd_op_map_errors adds to the other entry points' count.
+int restrict_noalloc_map_errors(unsigned long long* count, bool reset);
+
 }  // namespace mgcfd

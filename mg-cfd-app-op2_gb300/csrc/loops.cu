@@ -545,6 +545,9 @@ extern "C" int mgcfd_op_map_errors(int64_t* count, int32_t reset) {
     e = cudaMemcpyToSymbol(g_map_errors, &zero, sizeof(zero));
   }
   if (e != cudaSuccess) return set_error(MGCFD_ERR_CUDA, std::string("mgcfd_op_map_errors: ") + cudaGetErrorString(e));
-  *count = (int64_t)v;
+  unsigned long long w = 0;
+  const int r = restrict_noalloc_map_errors(&w, reset != 0);
+  if (r) return r;
+  *count = (int64_t)(v + w);
   return MGCFD_OK;
 }

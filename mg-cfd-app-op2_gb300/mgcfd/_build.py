@@ -4,11 +4,7 @@ Outputs (all git-ignored, rebuilt when a source is newer than the output):
   mg-cfd-app-op2_gb300/lib/libmgcfd_gb300.so   the product: CUDA kernels + C ABI
   mg-cfd-app-op2_gb300/bin/euler3d_gb300        euler3d-compatible command line driver
   mg-cfd-app-op2_gb300/bin/mgcfd_renumber       standalone mesh renumbering tool
-  oracle/_build/liboracle.so                    the oracle (C restatement), test-only
-  oracle/_build/mgcfd_oracle_run                the oracle as a timed CPU baseline, test-only
-  oracle/_ref/euler3d_ref                       reference euler3d.cpp against the OP2
-                                                stand-in (only where the reference
-                                                sources are present)
+(The checkers under oracle/ have their own recipe, oracle/recipe.py.)
 
 CUDA code is compiled for sm_103a only.  Host C/C++ is compiled with
 -ffp-contract=off so results are identical on x86_64 and aarch64 hosts.
@@ -31,10 +27,6 @@ CLI = PKG / "bin" / "euler3d_gb300"
 RENUMBER_CLI = PKG / "bin" / "mgcfd_renumber"
 TOOLS = {"euler3d_gb300.cpp": CLI, "mgcfd_renumber.cpp": RENUMBER_CLI}
 OBJ = PKG / "_build"
-ORACLE = ROOT / "oracle"
-ORACLE_LIB = ORACLE / "_build" / "liboracle.so"
-ORACLE_RUN = ORACLE / "_build" / "mgcfd_oracle_run"
-REF_BIN = ORACLE / "_ref" / "euler3d_ref"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
@@ -119,50 +111,5 @@ def build_library(force: bool = False, jobs: int | None = None) -> Path:
     return LIB
 
 
-def build_oracle(force: bool = False) -> Path:
-    """Compile the oracle restatement (test infrastructure only)."""
-    src = ORACLE / "mgcfd_oracle.c"
-    hdr = ORACLE / "mgcfd_oracle.h"
-    run_src = ORACLE / "oracle_run.c"
-    ORACLE_LIB.parent.mkdir(parents=True, exist_ok=True)
-    force = force or not _stamp_ok(ORACLE_LIB.parent)
-    cflags = ["-O2", "-std=c11", "-ffp-contract=off", "-fopenmp", "-fPIC"]
-    if force or _stale(ORACLE_LIB, [src, hdr]):
-        _run(["gcc", *cflags, "-shared", "-o", str(ORACLE_LIB), str(src), "-lm"])
-    if run_src.exists() and (force or _stale(ORACLE_RUN, [src, hdr, run_src])):
-        _run(["gcc", *cflags, "-o", str(ORACLE_RUN), str(run_src), str(src), "-lm"])
-    _write_stamp(ORACLE_LIB.parent)
-    return ORACLE_LIB
-
-
-def reference_dir() -> Path | None:
-    p = Path(os.environ.get("MGCFD_REFERENCE_DIR", "/root/reference"))
-    return p if (p / "euler3d.cpp").exists() else None
-
-
-def build_reference(force: bool = False) -> Path | None:
-    """Compile the unmodified reference driver against the OP2 stand-in.
-
-    Only possible where the reference sources exist; returns None elsewhere.
-    """
-    ref = reference_dir()
-    if ref is None:
-        return None
-    deps = [ORACLE / "ref_main.cpp", ORACLE / "op2shim" / "op2shim.cpp", ORACLE / "op2shim" / "op_seq.h",
-            ORACLE / "op2shim" / "op_hdf5.h", CSRC / "h5lite.cpp", CSRC / "h5lite.h"]
-    deps += sorted(ref.glob("*.h")) + [ref / "euler3d.cpp"]
-    if force or not _stamp_ok(REF_BIN.parent) or _stale(REF_BIN, deps):
-        REF_BIN.parent.mkdir(parents=True, exist_ok=True)
-        _run(["g++", "-O2", "-std=c++14", "-ffp-contract=off", "-w",
-              f"-I{ORACLE / 'op2shim'}", f"-I{CSRC}", f"-I{ref}",
-              "-o", str(REF_BIN), str(ORACLE / "ref_main.cpp"), str(ORACLE / "op2shim" / "op2shim.cpp"),
-              str(CSRC / "h5lite.cpp")])
-        _write_stamp(REF_BIN.parent)
-    return REF_BIN
-
-
 def build_all(force: bool = False) -> None:
-    with cf.ThreadPoolExecutor(max_workers=3) as ex:
-        futs = [ex.submit(build_library, force), ex.submit(build_oracle, force), ex.submit(build_reference, force)]
-        for f in futs:
-            f.result()
+    build_library(force)

@@ -17,8 +17,8 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent
-sys.path.insert(0, str(ROOT / "mg-cfd-app-op2_gb300"))
-from mgcfd import _build  # noqa: E402
+sys.path.insert(0, str(HERE))
+import recipe as _recipe  # noqa: E402  (oracle/recipe.py)
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -38,8 +38,8 @@ _LIB = None
 def lib():
     global _LIB
     if _LIB is None:
-        _build.build_oracle()
-        L = C.CDLL(str(_build.ORACLE_LIB))
+        _recipe.build_oracle()
+        L = C.CDLL(str(_recipe.ORACLE_LIB))
         L.orc_freestream_init.argtypes = [C.c_double, C.c_double, C.POINTER(Freestream)]
         L.orc_mesh_create.restype = C.c_void_p
         L.orc_mesh_create.argtypes = [C.c_int]
@@ -124,7 +124,7 @@ class OracleRun:
 
 def run_reference_binary(workdir, ncycles, mach, aoa, extra_args=(), prefix="solution."):
     """Run oracle/_ref/euler3d_ref on workdir/input.dat; returns CompletedProcess."""
-    exe = _build.build_reference()
+    exe = _recipe.build_reference()
     if exe is None:
         raise FileNotFoundError("reference sources are not available on this host")
     env = dict(os.environ, MGCFD_MACH=repr(float(mach)), MGCFD_AOA_DEG=repr(float(aoa)))

@@ -18,13 +18,14 @@ def pytest_configure(config):
 def built():
     """Builds the library, the oracle and (where possible) the reference binary once."""
     from mgcfd import _build
+    import recipe as oracle_build  # oracle/recipe.py
     _build.build_library()
-    _build.build_oracle()
-    _build.build_reference()
+    oracle_build.build_oracle()
+    oracle_build.build_reference()
     yield
 
 
 @pytest.fixture(scope="session")
 def reference_available():
-    from mgcfd import _build
-    return _build.reference_dir() is not None
+    import recipe as oracle_build
+    return oracle_build.reference_dir() is not None

@@ -4,7 +4,8 @@
 // atomics to an HBM-resident array, and a device-to-device copy.  Each rate
 // is reported per second and in FP64-FMA equivalents, the unit the kernels'
 // cost model counts in.  Prints one JSON object.  Not part of the library;
-// built and run by `python bench.py --mode rates`.
+// built and run by `python bench.py --mode rates` and by
+// tests/test_gpu_rates.py, which checks the FP64 FMA rate the roofline uses.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdio.h>

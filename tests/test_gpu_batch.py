@@ -80,12 +80,28 @@ def test_mixed_precision_batch(meshes, increment, accumulation):
             s.close()
 
 
-def test_residual_norms_match_oracle(meshes):
-    b = mgcfd.Batch(meshes[:2], MACH[:2], AOA[:2])
-    b.run(2)
-    for m in range(2):
+@pytest.mark.parametrize("increment", ["atomic", "gather"])
+def test_residual_norms_match_oracle(meshes, increment):
+    """Each mesh's level-0 residual norm (calc_rms_kernel, validation.h:37-44,
+    summed over the mesh and taken as sqrt(rms / N) at euler3d.cpp:533-537)
+    against the oracle's own calc_rms on its residual after the same cycles:
+    the last level-0 smoothing step is the first step of the last cycle in
+    both.  Summation order moves the residuals by ~1e-22 against residuals of
+    ~1e-6, so the FP64 bar holds for the norms."""
+    cycles = 2
+    b = mgcfd.Batch(meshes[:4], MACH[:4], AOA[:4], increment=increment)
+    b.run(cycles)
+    assert b.synchronize() == 0
+    for m in range(4):
         st, rms, rho = b.mesh_status(m)
         run = O.OracleRun(meshes[m].levels())
-        assert run.run(MACH[m], AOA[m], 2)[0] == 0
-        # the last level-0 smoothing is the first step of the last cycle
-        assert st == 0 and rms > 0 and rho > 0
+        assert run.run(MACH[m], AOA[m], cycles)[0] == 0
+        res = run.get(0, O.Q_RESIDUALS)
+        n0 = res.shape[0]
+        rms_ref = np.sqrt(O.lib().orc_loop_calc_rms(n0, O.dptr(np.ascontiguousarray(res))) / n0)
+        rho_ref = np.sqrt(O.lib().orc_loop_calc_rms(n0, O.dptr(np.ascontiguousarray(
+            np.column_stack([res[:, 0], np.zeros((n0, 4))])))) / n0)
+        assert st == 0
+        assert rms == pytest.approx(rms_ref, rel=STATE_TOL, abs=0.0), (m, rms, rms_ref)
+        assert rho == pytest.approx(rho_ref, rel=STATE_TOL, abs=0.0), (m, rho, rho_ref)
+        run.close()

@@ -9,6 +9,7 @@ import pytest
 import mgcfd
 from mgcfd import ops
 import oracle as O
+from parity import STATE_TOL, state_error
 
 pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
@@ -120,13 +121,13 @@ def test_flux_edge_and_boundary(case, level):
     O.lib().orc_loop_compute_flux_edge(L.nedges, ip(L.edge_to_nodes), dp(var), dp(ewt), C.c_double(ff.smoothing_coefficient),
                                        dp(exp))
     got = host(flux)
-    np.testing.assert_allclose(got, exp, rtol=1e-9, atol=1e-11 * np.abs(exp).max())
+    assert state_error(got, exp) <= STATE_TOL, state_error(got, exp)
     ops.compute_bnd_node_flux(L.nbnd, n, dev(L.bnd_to_node).data_ptr(), dev(L.bnd_group).data_ptr(),
                               dev(bwt).data_ptr(), dev(var).data_ptr(), mgcfd.freestream(0.7, 2.0), flux.data_ptr())
     O.lib().orc_loop_compute_bnd_node_flux(L.nbnd, ip(L.bnd_to_node), ip(L.bnd_group), dp(bwt), dp(var),
                                            C.byref(ff), dp(exp))
     got = host(flux)
-    np.testing.assert_allclose(got, exp, rtol=1e-9, atol=1e-11 * np.abs(exp).max())
+    assert state_error(got, exp) <= STATE_TOL, state_error(got, exp)
 
 
 def test_time_step_residual_rms_bad(case):
@@ -242,4 +243,4 @@ def test_out_of_range_map_entries_are_skipped(case):
     exp = np.zeros((n, 5))
     O.lib().orc_loop_compute_flux_edge(int(keep.sum()), ip(e_ok), dp(var), dp(w_ok),
                                        C.c_double(ff.smoothing_coefficient), dp(exp))
-    np.testing.assert_allclose(host(flux), exp, rtol=1e-9, atol=1e-11 * np.abs(exp).max())
+    assert state_error(host(flux), exp) <= STATE_TOL

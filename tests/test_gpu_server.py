@@ -8,7 +8,7 @@ import pytest
 import mgcfd
 from mgcfd import server
 import oracle as O
-from parity import STATE_TOL, state_error
+from parity import MIXED_TOL, STATE_TOL, per_variable_errors, state_error
 
 pytestmark = pytest.mark.gpu
 
@@ -48,6 +48,36 @@ def test_alone_equals_mix_bitwise_with_gather(meshes):
         ref = O.OracleRun(meshes[i].levels())
         assert ref.run(CASES[i][3], CASES[i][4], 4)[0] == 0
         assert state_error(vm, ref.get(0, O.Q_VARIABLES)) <= STATE_TOL
+
+
+@pytest.mark.parametrize("accumulation", ["fp64", "pair32"])
+def test_served_mixed_alone_equals_mix_bitwise(meshes, accumulation):
+    """The served mixed-precision form (fused node-centric stage, FP64 or
+    compensated FP32-pair node sums): every request gives the same bits alone
+    and in a mix of overlapping requests, and stays within the mixed bar of
+    the FP64 oracle."""
+    cycles = 4
+    alone = {}
+    for i in range(len(CASES)):
+        srv = mgcfd.Server(max_active=1, precision="mixed", increment="fused", accumulation=accumulation,
+                           max_cycles=cycles)
+        alone.update(run_requests(srv, meshes, [i]))
+        srv.close()
+    srv = mgcfd.Server(max_active=4, precision="mixed", increment="fused", accumulation=accumulation,
+                       max_cycles=cycles)
+    mix = run_requests(srv, meshes, range(len(CASES)))
+    st = srv.stats()
+    srv.close()
+    assert st["completed"] == len(CASES) and st["failed"] == 0 and st["peak_active"] >= 2
+    for i in range(len(CASES)):
+        ra, va = alone[i]
+        rm, vm = mix[i]
+        assert ra["status"] == rm["status"] == 0 and ra["cycles"] == rm["cycles"] == cycles
+        np.testing.assert_array_equal(va, vm)
+        ref = O.OracleRun(meshes[i].levels())
+        assert ref.run(CASES[i][3], CASES[i][4], cycles)[0] == 0
+        mx, l2 = per_variable_errors(vm, ref.get(0, O.Q_VARIABLES))
+        assert mx.max() <= MIXED_TOL and l2.max() <= MIXED_TOL, (i, mx, l2)
 
 
 def test_alone_equals_mix_within_tolerance_with_atomics(meshes):

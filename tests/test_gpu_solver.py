@@ -237,7 +237,9 @@ def test_level0_norms_match_residuals_and_oracle(nl):
     rms64, rho64, res64 = _norms(mesh, cycles)
     assert rms64 == pytest.approx(np.sqrt(np.sum(res64 ** 2) / n0), rel=1e-12)
     assert rho64 == pytest.approx(np.sqrt(np.sum(res64[:, 0] ** 2) / n0), rel=1e-12)
-    assert rms64 == pytest.approx(rms_ref, rel=1e-6)
+    # The residual is the last step's change (~1e-6 against a state of ~1);
+    # summation order moves it by ~1e-22, so the FP64 bar applies to its norm.
+    assert rms64 == pytest.approx(rms_ref, rel=STATE_TOL, abs=0.0)
     rms_f, rho_f, res_f = _norms(mesh, cycles, precision="mixed", increment="fused")
     rms_g, rho_g, res_g = _norms(mesh, cycles, precision="mixed", increment="gather")
     np.testing.assert_array_equal(res_f, res_g)  # same residuals, norms from different kernels

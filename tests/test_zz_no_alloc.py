@@ -20,27 +20,31 @@ pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 
 
-def _restrict_with_caller_scratch(F, Cl, fine, coarse0):
+def _restrict_with_caller_scratch(nfine, ncoarse, node_to_mg, fine, coarse0):
     cv = torch.from_numpy(coarse0.copy()).cuda()
     fv = torch.from_numpy(np.ascontiguousarray(fine)).cuda()
-    m = torch.from_numpy(np.ascontiguousarray(F.node_to_mg)).cuda()
-    scratch = torch.zeros(Cl.nnodes, dtype=torch.int32, device="cuda")
-    ops.up_pre(F.nnodes, Cl.nnodes, m.data_ptr(), cv.data_ptr(), scratch.data_ptr())
-    ops.up(F.nnodes, Cl.nnodes, m.data_ptr(), fv.data_ptr(), cv.data_ptr(), scratch.data_ptr())
-    ops.up_post(Cl.nnodes, cv.data_ptr(), scratch.data_ptr())
+    m = torch.from_numpy(np.ascontiguousarray(node_to_mg)).cuda()
+    scratch = torch.zeros(ncoarse, dtype=torch.int32, device="cuda")
+    ops.up_pre(nfine, ncoarse, m.data_ptr(), cv.data_ptr(), scratch.data_ptr())
+    ops.up(nfine, ncoarse, m.data_ptr(), fv.data_ptr(), cv.data_ptr(), scratch.data_ptr())
+    ops.up_post(ncoarse, cv.data_ptr(), scratch.data_ptr())
     torch.cuda.synchronize()
     return cv.cpu().numpy()
 
 
-def _restrict_noalloc(F, Cl, fine, coarse0):
+def _restrict_noalloc(nfine, ncoarse, node_to_mg, fine, coarse0):
     cv = torch.from_numpy(coarse0.copy()).cuda()
     fv = torch.from_numpy(np.ascontiguousarray(fine)).cuda()
-    m = torch.from_numpy(np.ascontiguousarray(F.node_to_mg)).cuda()
+    m = torch.from_numpy(np.ascontiguousarray(node_to_mg)).cuda()
     lib = _lib.load()
-    _lib.check(lib.mgcfd_op_restrict_noalloc(F.nnodes, Cl.nnodes, C.c_void_p(m.data_ptr()),
+    _lib.check(lib.mgcfd_op_restrict_noalloc(nfine, ncoarse, C.c_void_p(m.data_ptr()),
                                              C.c_void_p(fv.data_ptr()), C.c_void_p(cv.data_ptr()), None))
     torch.cuda.synchronize()
     return cv.cpu().numpy()
+
+
+def _states(rng, ff, n):
+    return np.tile(ff, (n, 1)) * (1.0 + 0.01 * rng.standard_normal((n, 5)))
 
 
 def test_restrict_noalloc_matches_caller_scratch_twice():
@@ -49,11 +53,42 @@ def test_restrict_noalloc_matches_caller_scratch_twice():
     rng = np.random.default_rng(3)
     ff = np.array(mgcfd.freestream(0.6, 4.0).ff_variable[:])
     for call in range(2):  # the second call must start from cleared counts
-        fine = np.tile(ff, (F.nnodes, 1)) * (1.0 + 0.01 * rng.standard_normal((F.nnodes, 5)))
-        coarse0 = np.tile(ff, (Cl.nnodes, 1)) * (1.0 + 0.01 * rng.standard_normal((Cl.nnodes, 5)))
-        expect = _restrict_with_caller_scratch(F, Cl, fine, coarse0)
-        got = _restrict_noalloc(F, Cl, fine, coarse0)
+        fine, coarse0 = _states(rng, ff, F.nnodes), _states(rng, ff, Cl.nnodes)
+        expect = _restrict_with_caller_scratch(F.nnodes, Cl.nnodes, F.node_to_mg, fine, coarse0)
+        got = _restrict_noalloc(F.nnodes, Cl.nnodes, F.node_to_mg, fine, coarse0)
         np.testing.assert_allclose(got, expect, rtol=1e-14, err_msg=f"call {call}")
+
+
+def test_restrict_noalloc_larger_then_smaller_level():
+    """A call on a larger coarse level leaves higher counts in the shared
+    array; the next, smaller call must neither see nor use them."""
+    mesh = mgcfd.HostMesh.generate(26, 3, 17)
+    rng = np.random.default_rng(5)
+    ff = np.array(mgcfd.freestream(0.7, 2.0).ff_variable[:])
+    for lf in (0, 1):  # level 0 -> 1 (larger coarse level), then level 1 -> 2
+        F, Cl = mesh.level(lf), mesh.level(lf + 1)
+        fine, coarse0 = _states(rng, ff, F.nnodes), _states(rng, ff, Cl.nnodes)
+        expect = _restrict_with_caller_scratch(F.nnodes, Cl.nnodes, F.node_to_mg, fine, coarse0)
+        got = _restrict_noalloc(F.nnodes, Cl.nnodes, F.node_to_mg, fine, coarse0)
+        np.testing.assert_allclose(got, expect, rtol=1e-14, err_msg=f"fine level {lf}")
+
+
+def test_restrict_noalloc_skips_and_counts_out_of_range_entries():
+    mesh = mgcfd.HostMesh.generate(12, 2, 23)
+    F, Cl = mesh.level(0), mesh.level(1)
+    rng = np.random.default_rng(9)
+    ff = np.array(mgcfd.freestream(0.5, 1.0).ff_variable[:])
+    node_to_mg = F.node_to_mg.copy()
+    bad = rng.choice(F.nnodes, 5, replace=False)
+    node_to_mg[bad[:3]] = Cl.nnodes  # one past the end
+    node_to_mg[bad[3:]] = -1
+    fine, coarse0 = _states(rng, ff, F.nnodes), _states(rng, ff, Cl.nnodes)
+    ops.map_errors(reset=True)
+    expect = _restrict_with_caller_scratch(F.nnodes, Cl.nnodes, node_to_mg, fine, coarse0)
+    assert ops.map_errors(reset=True) == 2 * len(bad)  # up_pre and up each skip and count them
+    got = _restrict_noalloc(F.nnodes, Cl.nnodes, node_to_mg, fine, coarse0)
+    assert ops.map_errors(reset=True) == len(bad)
+    np.testing.assert_allclose(got, expect, rtol=1e-14)
 
 
 def test_restrict_noalloc_rejects_oversized_level():
