@@ -11,10 +11,13 @@ Mach 0.8, angle of attack 3 degrees, FP64.  One step = one V-cycle
   python bench.py --mode batch     # 64 uneven meshes in one launch per stage
   python bench.py --mode serve     # Poisson request stream, p50/p99 latency
 
-Prints one JSON line.  `value` is V-cycles/s with the mesh resident in HBM,
+Prints one JSON line.  `value` is V-cycles/s with the mesh resident in HBM
+(the default CUDA-graph path, timed with CUDA events on the solver's stream),
 `e2e` is V-cycles/s through the host-buffer entry point mgcfd_solve (mesh
 upload, setup, 25 V-cycles, download of every level's state), and `roofline`
-describes the level-0 edge-flux kernel.  --impl reference times the CPU
+describes the level-0 edge-flux kernel.  The same line carries the
+mixed-precision workload on the same mesh (`mixed`) and served solves on a
+fresh-mesh request stream against the plain FP64 path (`served`).  --impl reference times the CPU
 restatement of the reference path (OpenMP, all host threads) on the same
 mesh.  Under torchrun each rank runs an independent replica (the solve does
 not shard across GPUs); value is the sum over ranks.
@@ -36,6 +39,7 @@ sys.path.insert(0, str(ROOT / "mg-cfd-app-op2_gb300"))
 
 MACH, AOA, NLEVELS, SEED = 0.8, 3.0, 4, 20240501
 E2E_CYCLES = 25
+MIXED_CYCLES = 25  # the mixed-precision workload's cycle count
 
 
 def algorithmic_flux_bytes(nnodes: int, nedges: int, precision: str = "fp64", increment: str = "atomic") -> int:
@@ -142,10 +146,69 @@ def pinned_levels(levels, keep):
                         node_to_mg=pin(L.node_to_mg), n_axis=L.n_axis, volumes=pin(L.volumes)) for L in levels]
 
 
+def flux_roofline(precision, increment, n, N, E, flux_ms):
+    """Roofline of the level-0 edge-flux kernel (the fused stage for mixed
+    precision): algorithmic bytes per launch over the CUDA-event launch time,
+    against the measured HBM copy rate, plus the FP64-pipe roofline where the
+    committed ncu profile gives the FP64 work per unit."""
+    peak, peak_kind = measured_peaks()
+    bytes_per_sweep = algorithmic_flux_bytes(N, E, precision, increment)
+    achieved = bytes_per_sweep / (flux_ms * 1e-3) / 1e9
+    prof = committed_profile(f"flux_edge_{precision}_{increment}.json") or {}
+    traffic = prof.get("dram_bytes_per_launch_scaled_to_bench") if n == 200 else None
+    fp64_roof = None
+    if prof.get("fp64"):
+        # FP64 kernels are bound by FP64 issue, not HBM: the same launch
+        # against the measured FP64 FMA rate.
+        f = prof["fp64"]
+        key = "ops_per_edge" if "ops_per_edge" in f else "ops_per_node"
+        ach = f[key] * (E if key == "ops_per_edge" else N) / (flux_ms * 1e-3) / 1e9
+        fp64_roof = {"bound": "fp64", "achieved": round(ach, 1), "peak": f["peak_gops"], "unit": "G FP64 op/s",
+                     "frac": round(ach / f["peak_gops"], 4), key: f[key], "peak_source": f["peak_source"],
+                     "ncu_fp64_pipe_busy": f["pipe_busy_ncu"]}
+    kernel = ("k_update fused stage (level-0 edge fluxes + time step)" if increment == "fused"
+              else "k_flux (level-0 edge flux sweep)")
+    return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": traffic, "kernel": kernel,
+            "flux_ms_per_launch": round(flux_ms, 4), "algorithmic_bytes_per_launch": bytes_per_sweep,
+            "peak_source": peak_kind, "fp64": fp64_roof}
+
+
+def timed_cycles(solver, stream, cycles):
+    """Device time of `cycles` V-cycles (CUDA-graph replays) enqueued on the
+    solver's own stream, between two CUDA events recorded on that stream."""
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    solver.run(cycles)
+    e1.record(stream)
+    status = solver.synchronize()
+    e1.synchronize()
+    return e0.elapsed_time(e1) * 1e-3, status
+
+
+def kernel_times(mesh, cycles, **opts):
+    """Mean CUDA-event time of a level-0 edge-flux launch (the fused stage in
+    mixed precision).  A separate solver records events around those launches,
+    which takes it off the CUDA-graph path, so this pass is not the timed one."""
+    import mgcfd
+    from mgcfd import _lib
+    s = mgcfd.Solver(mesh, MACH, AOA, time_kernels=True, **opts)
+    s.run(3)
+    if s.synchronize() != 0:
+        raise RuntimeError(_lib.load().mgcfd_last_error().decode())
+    st0 = s.stats()
+    s.run(cycles)
+    if s.synchronize() != 0:
+        raise RuntimeError(_lib.load().mgcfd_last_error().decode())
+    st1 = s.stats()
+    s.close()
+    return (st1.flux_ms_l0 - st0.flux_ms_l0) / max(1, st1.flux_sweeps_l0 - st0.flux_sweeps_l0)
+
+
 def run_gb300(args):
     import ctypes as C
 
-    import numpy as np
     import torch
 
     import mgcfd
@@ -159,8 +222,13 @@ def run_gb300(args):
     mesh = mgcfd.HostMesh.generate(args.n, NLEVELS, SEED)
     L0 = mesh.level(0)
     N, E = L0.nnodes, L0.nedges
-    solver = mgcfd.Solver(mesh, MACH, AOA, precision=args.precision, increment=args.increment,
-                          renumber=args.renumber, accumulation=args.accumulation, time_kernels=True)
+    inc = args.increment if args.increment != "auto" else ("fused" if args.precision == "mixed" else "atomic")
+    variant = dict(precision=args.precision, increment=args.increment, renumber=args.renumber,
+                   accumulation=args.accumulation)
+    # The timed region: the production path, one CUDA graph per V-cycle on
+    # the solver's stream, timed with CUDA events on that stream.
+    stream = torch.cuda.Stream()
+    solver = mgcfd.Solver(mesh, MACH, AOA, stream=stream.cuda_stream, **variant)
     solver.run(args.warmup)
     if solver.synchronize() != 0:
         raise RuntimeError(_lib.load().mgcfd_last_error().decode())
@@ -173,35 +241,17 @@ def run_gb300(args):
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
         t0 = time.perf_counter()
-        solver.run(args.steps)
-        status = solver.synchronize()
-        torch.cuda.synchronize()
+        secs, status = timed_cycles(solver, stream, args.steps)
         t1 = time.perf_counter()
     barrier()
     if status != 0:
         raise RuntimeError(_lib.load().mgcfd_last_error().decode())
     st1 = solver.stats()
-    value, elapsed = replicas.job_throughput(args.steps, t1 - t0, dist, device="cuda")
-    flux_ms = (st1.flux_ms_l0 - st0.flux_ms_l0) / max(1, st1.flux_sweeps_l0 - st0.flux_sweeps_l0)
+    value, elapsed = replicas.job_throughput(args.steps, secs, dist, device="cuda")
     launches = int(st1.kernel_launches - st0.kernel_launches)
-    precision_error = None
-    if args.precision == "mixed":
-        # Final level-0 state against an FP64 solve of the same cycles:
-        # per-variable max and L2 relative error (density, 3 momenta, energy).
-        got = solver.fetch(0)
-        ref_solver = mgcfd.Solver(mesh, MACH, AOA, precision="fp64", renumber=args.renumber)
-        ref_solver.run(args.warmup + args.steps)
-        if ref_solver.synchronize() != 0:
-            raise RuntimeError(_lib.load().mgcfd_last_error().decode())
-        ref = ref_solver.fetch(0)
-        ref_solver.close()
-        d = got - ref
-        precision_error = {
-            "variables": ["rho", "rho_u", "rho_v", "rho_w", "rho_E"],
-            "max_rel": [float(np.max(np.abs(d[:, k])) / np.max(np.abs(ref[:, k]))) for k in range(5)],
-            "l2_rel": [float(np.linalg.norm(d[:, k]) / np.linalg.norm(ref[:, k])) for k in range(5)],
-            "cycles": args.warmup + args.steps, "against": "FP64 solve of the same mesh and cycles"}
     solver.close()
+    # Per-kernel events in their own pass (off the graph path).
+    flux_ms = kernel_times(mesh, args.kernel_cycles, **variant)
 
     # End to end through the host-buffer entry point, pinned host memory.
     levels = mesh.levels()
@@ -210,8 +260,7 @@ def run_gb300(args):
     outs = [torch.empty((L.nnodes, 5), dtype=torch.float64).pin_memory() for L in levels]
     views = mgcfd.level_views_from_arrays(hl)
     out_ptrs = (_lib.c_double_p * len(outs))(*[C.cast(o.data_ptr(), _lib.c_double_p) for o in outs])
-    opts = mgcfd.options(precision=args.precision, increment=args.increment, renumber=args.renumber,
-                         accumulation=args.accumulation)
+    opts = mgcfd.options(**variant)
     lib = _lib.load()
     h2d = sum(a.nbytes for L in hl for a in (L.coords, L.edge_to_nodes, L.bnd_to_node, L.bnd_group, L.edge_weights,
                                               L.bnd_weights) + ((L.node_to_mg,) if L.node_to_mg is not None else ()))
@@ -225,8 +274,12 @@ def run_gb300(args):
     te1 = time.perf_counter()
     barrier()
     e2e_value, e2e_elapsed = replicas.job_throughput(e2e_steps * E2E_CYCLES, te1 - te0, dist, device="cuda")
+    del pinned, hl, outs
 
-    cpu = None
+    mixed = served = cpu = None
+    if rank == 0 and not args.no_extra_forms:
+        mixed = mixed_section(mesh, args, N, E, stream, value if args.precision == "fp64" else None)
+        served = served_section(args)
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(levels, args.cpu_cycles)
 
@@ -234,23 +287,6 @@ def run_gb300(args):
         if dist:
             dist.destroy_process_group()
         return
-    peak, peak_kind = measured_peaks()
-    inc = args.increment if args.increment != "auto" else ("fused" if args.precision == "mixed" else "atomic")
-    bytes_per_sweep = algorithmic_flux_bytes(N, E, args.precision, inc)
-    achieved = bytes_per_sweep / (flux_ms * 1e-3) / 1e9
-    prof = committed_profile(f"flux_edge_{args.precision}_{inc}.json") or {}
-    traffic = prof.get("dram_bytes_per_launch_scaled_to_bench") if args.n == 200 else None
-    fp64_roof = None
-    if prof.get("fp64"):
-        # The FP64 flux sweep is bound by FP64 issue, not HBM: the same launch
-        # against the measured FP64 FMA rate.
-        f = prof["fp64"]
-        per_edge = "ops_per_edge" in f
-        ach = (f["ops_per_edge"] * E if per_edge else f["ops_per_node"] * N) / (flux_ms * 1e-3) / 1e9
-        fp64_roof = {"bound": "fp64", "achieved": round(ach, 1), "peak": f["peak_gops"], "unit": "G FP64 op/s",
-                     "frac": round(ach / f["peak_gops"], 4),
-                     ("ops_per_edge" if per_edge else "ops_per_node"): f["ops_per_edge" if per_edge else "ops_per_node"],
-                     "peak_source": f["peak_source"], "ncu_fp64_pipe_busy": f["pipe_busy_ncu"]}
     line = {
         "metric": "MG V-cycles/s at 8M nodes (200^3, 4 levels)",
         "value": round(value, 3),
@@ -264,30 +300,212 @@ def run_gb300(args):
         "vs_baseline": None,
         "dtype": "f64" if args.precision == "fp64" else "f32-flux/f64-accumulate",
         "data": "synthetic: seeded jittered 200^3 lattice, permuted ids",
-        "config": {"workload": f"{args.n}^3 jittered lattice, {NLEVELS} levels, Mach {MACH}, AoA {AOA} deg, "
-                               f"{N} nodes / {E} edges on level 0",
-                   "precision": args.precision, "increment": inc, "renumber": args.renumber,
-                   "accumulation": args.accumulation if args.precision == "mixed" else "fp64",
-                   "l2": "inputs larger than L2 (level-0 state and edges ~2.4 GB), no flush",
-                   "parallelism": f"replicas x{world}"},
-        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": traffic,
-                     "kernel": ("k_update fused stage (level-0 edge fluxes + time step)" if inc == "fused"
-                                else "k_flux (level-0 edge flux sweep)"), "flux_ms_per_launch": round(flux_ms, 4),
-                     "algorithmic_bytes_per_launch": bytes_per_sweep, "peak_source": peak_kind,
-                     "fp64": fp64_roof},
+        "config": line_config(args, N, E),
+        "variant": {"increment": inc, "renumber": args.renumber,
+                    "accumulation": args.accumulation if args.precision == "mixed" else "fp64",
+                    "parallelism": f"replicas x{world}"},
+        "timing": "CUDA events on the solver's stream around the timed V-cycles, each one CUDA-graph replay "
+                  f"(the default path); wall clock {round(t1 - t0, 4)} s for the same region",
+        "roofline": dict(flux_roofline(args.precision, inc, args.n, N, E, flux_ms),
+                         timing=f"mean CUDA-event time of the level-0 launches over {args.kernel_cycles} V-cycles "
+                                "of a second solver that records events around them (no CUDA graph)"),
         "e2e": {"value": round(e2e_value, 3), "unit": "cycles/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "step": f"mgcfd_solve: upload mesh, setup, {E2E_CYCLES} V-cycles, download all levels",
                 "steps": e2e_steps},
         "gpu_launches": launches,
-        "precision_error": precision_error,
         "clocks": clocks.summary(),
+        "mixed": mixed,
+        "served": served,
         "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def line_config(args, N, E):
+    """The config both arms print for the same workload."""
+    return {"workload": f"{args.n}^3 jittered lattice, {NLEVELS} levels, Mach {MACH}, AoA {AOA} deg, "
+                        f"{N} nodes / {E} edges on level 0",
+            "precision": args.precision,
+            "l2": "inputs larger than L2 (level-0 state and edges ~2.4 GB), no flush"}
+
+
+def mixed_section(mesh, args, N, E, stream, fp64_value):
+    """The mixed-precision workload on the same mesh: edge-flux arithmetic and
+    geometry in FP32, node sums, time step and norms in FP64 (FP64 node sums,
+    or compensated FP32-pair sums).  V-cycles/s on the CUDA-graph path, the
+    fused stage's roofline, and each variable's max and L2 relative error of
+    the final state after 25 V-cycles against the FP64 solve."""
+    import numpy as np
+
+    import mgcfd
+    from mgcfd import _lib
+    cycles = MIXED_CYCLES
+    ref = mgcfd.Solver(mesh, MACH, AOA, stream=stream.cuda_stream)
+    ref.run(cycles)
+    if ref.synchronize() != 0:
+        raise RuntimeError(_lib.load().mgcfd_last_error().decode())
+    want = [ref.fetch(l) for l in range(NLEVELS)]
+    ref.close()
+    out = {"workload": f"{args.n}^3 lattice, {NLEVELS} levels, Mach {MACH}, AoA {AOA} deg, fused node-centric stage",
+           "error_against": f"FP64 solve of the same mesh after {cycles} V-cycles",
+           "variables": ["rho", "rho_u", "rho_v", "rho_w", "rho_E"]}
+    for acc in ("fp64", "pair32"):
+        opts = dict(precision="mixed", increment="fused", renumber=args.renumber, accumulation=acc)
+        s = mgcfd.Solver(mesh, MACH, AOA, stream=stream.cuda_stream, **opts)
+        s.run(args.warmup)
+        if s.synchronize() != 0:
+            raise RuntimeError(_lib.load().mgcfd_last_error().decode())
+        secs, st = timed_cycles(s, stream, args.steps)
+        if st != 0:
+            raise RuntimeError(_lib.load().mgcfd_last_error().decode())
+        s.reset()
+        s.run(cycles)
+        if s.synchronize() != 0:
+            raise RuntimeError(_lib.load().mgcfd_last_error().decode())
+        got = [s.fetch(l) for l in range(NLEVELS)]
+        s.close()
+        mx = np.abs(got[0] - want[0]).max(axis=0) / np.abs(want[0]).max(axis=0)
+        l2 = np.linalg.norm(got[0] - want[0], axis=0) / np.linalg.norm(want[0], axis=0)
+        worst = max(float((np.abs(g - w).max(axis=0) / np.abs(w).max(axis=0)).max()) for g, w in zip(got, want))
+        out[f"accumulation_{acc}"] = {
+            "value": round(args.steps / secs, 3), "unit": "cycles/s",
+            "speedup_vs_fp64_value": round(args.steps / secs / fp64_value, 3) if fp64_value else None,
+            "max_rel_l0": [float(f"{x:.3e}") for x in mx], "l2_rel_l0": [float(f"{x:.3e}") for x in l2],
+            "max_rel_all_levels": float(f"{worst:.3e}"),
+            "roofline": flux_roofline("mixed", "fused", args.n, N, E, kernel_times(mesh, args.kernel_cycles, **opts))}
+    return out
+
+
+def generate_pool(specs, keep):
+    """Seeded lattice meshes (n, levels, seed) generated on host threads (the
+    generator releases the interpreter lock) and copied to page-locked memory."""
+    import concurrent.futures as cf
+
+    import mgcfd
+
+    def one(spec):
+        n, nl, seed = spec
+        return mgcfd.HostMesh.generate(n, nl, seed)
+
+    with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
+        meshes = list(ex.map(one, specs))
+    return [pinned_levels(m.levels(), keep) for m in meshes]
+
+
+def serve_specs(count, rng, seed0):
+    """Request meshes as the serving workload draws them: node count
+    log-uniform in 20K..4M (a cubic lattice of that size), 3 or 4 levels."""
+    import numpy as np
+    out = []
+    for i in range(count):
+        nodes = float(np.exp(rng.uniform(np.log(20e3), np.log(4e6))))
+        out.append((max(8, int(round(nodes ** (1.0 / 3.0)))), int(rng.integers(3, 5)), seed0 + i))
+    return out
+
+
+SERVE_FORMS = {"plain_fp64": dict(slots=1, precision="fp64"),
+               "served_fp64": dict(precision="fp64"),
+               "served_mixed": dict(precision="mixed"),
+               "served_mixed_pair32": dict(precision="mixed", accumulation="pair32")}
+
+
+def serve_stream(pool, picks, machs, aoas, gaps, form, rate, slots, reuse, want_results=False):
+    """Serve one request stream with one form; returns (summary, results).
+    rate = 0 queues every request at once (capacity).  With reuse, requests on
+    the same pool mesh share a resident mesh key; without it every request
+    uploads and sets up its mesh (a fresh mesh as far as the server knows)."""
+    import threading
+
+    import numpy as np
+
+    import mgcfd
+    o = dict(SERVE_FORMS[form])
+    active = o.pop("slots", slots)
+    srv = mgcfd.Server(hbm_budget_gb=150.0, max_active=active, max_cycles=50, residual_drop=1e-6, **o)
+    R = len(picks)
+    t_start = time.perf_counter()
+    arrivals = np.cumsum(gaps / rate) if rate else np.zeros(R)
+    ids = {}
+
+    def feeder():
+        for k in range(R):
+            delay = t_start + arrivals[k] - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            key = int(picks[k]) + 1 if (reuse and form != "plain_fp64") else 0
+            rid = srv.submit(pool[picks[k]], float(machs[k]), float(aoas[k]), mesh_key=key,
+                             resident=key != 0, want_result=want_results)
+            ids[rid] = k
+
+    th = threading.Thread(target=feeder)
+    th.start()
+    th.join()
+    srv.drain(3600)
+    t_end = time.perf_counter()
+    polled = srv.poll()
+    st = srv.stats()
+    srv.close()
+    res = [r for r, _ in polled]
+    results = {ids[r["id"]]: (r, v) for r, v in polled}
+    lat = np.array([r["finish_s"] - r["submit_s"] for r in res])
+    ok = sum(1 for r in res if r["status"] == 0)
+    return {"rate_per_s": round(rate, 3) if rate else "all at once",
+            "solves_per_s": round(len(res) / (t_end - t_start), 3),
+            "p50_ms": round(1e3 * float(np.percentile(lat, 50)), 2),
+            "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 2), "ok": ok, "failed": len(res) - ok,
+            "mean_cycles": round(float(np.mean([r["cycles"] for r in res])), 2),
+            "peak_active": int(st["peak_active"]), "peak_budget_gb": round(st["peak_bytes"] / 2 ** 30, 2),
+            "resident_mesh_hits": int(st["cache_hits"])}, results
+
+
+def served_section(args):
+    """Served solves on a fresh-mesh stream: every request is its own seeded
+    mesh (the pool is as large as the request count), so no form reuses a
+    resident mesh.  The plain FP64 path (one solve at a time) against the
+    served forms (up to --serve-slots overlapping requests), at capacity and
+    at one Poisson rate below the plain path's capacity."""
+    import numpy as np
+    rng = np.random.default_rng(29)
+    R = args.line_serve_requests
+    keep = []
+    pool = generate_pool(serve_specs(R, rng, 7000), keep)
+    picks = np.arange(R)
+    machs = rng.uniform(0.3, 0.85, R)
+    aoas = rng.uniform(0.0, 6.0, R)
+    gaps = rng.exponential(1.0, R)
+    serve_stream(pool, picks[:4], machs, aoas, gaps, "served_mixed", 0, args.serve_slots, False)  # warm-up
+    cap, results = {}, {}
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as sampler:
+        for f in SERVE_FORMS:
+            cap[f], results[f] = serve_stream(pool, picks, machs, aoas, gaps, f, 0, args.serve_slots, False,
+                                              want_results=f != "served_fp64")
+        rate = args.line_serve_rate * cap["plain_fp64"]["solves_per_s"]
+        at_rate = {f: serve_stream(pool, picks, machs, aoas, gaps, f, rate, args.serve_slots, False)[0]
+                   for f in ("plain_fp64", "served_mixed", "served_mixed_pair32")}
+    err = {}
+    for f in ("served_mixed", "served_mixed_pair32"):
+        worst, same = 0.0, 0
+        for k, (r, v) in results[f].items():
+            rp, vp = results["plain_fp64"][k]
+            if r["status"] == rp["status"] == 0 and r["cycles"] == rp["cycles"]:
+                same += 1
+                worst = max(worst, float((np.abs(v - vp).max(axis=0) / np.abs(vp).max(axis=0)).max()))
+        err[f] = {"max_rel_vs_plain_fp64": float(f"{worst:.3e}"), "requests_compared": same}
+    sizes = [L[0].nnodes for L in pool]
+    c = {f: cap[f]["solves_per_s"] for f in cap}
+    return {"metric": "served solves/s and p50/p99 latency, fresh mesh per request, vs the plain FP64 path",
+            "workload": f"{R} requests, each its own seeded lattice mesh ({min(sizes)}..{max(sizes)} level-0 nodes, "
+                        "3-4 levels), Mach U(0.3,0.85), AoA U(0,6) deg, 50 V-cycles or residual drop 1e-6, "
+                        "HBM budget 150 GB, inputs in page-locked host memory; no mesh stays resident",
+            "slots": args.serve_slots, "capacity_solves_per_s": c,
+            "speedup_served_mixed_vs_plain_fp64": round(c["served_mixed"] / c["plain_fp64"], 3),
+            "speedup_served_mixed_pair32_vs_plain_fp64": round(c["served_mixed_pair32"] / c["plain_fp64"], 3),
+            "speedup_served_fp64_vs_plain_fp64": round(c["served_fp64"] / c["plain_fp64"], 3),
+            "poisson": {"rate_multiple_of_plain_capacity": args.line_serve_rate, "runs": at_rate},
+            "final_state_error": err, "capacity_runs": cap, "clocks": sampler.summary()}
 
 
 def cpu_baseline(levels, cycles):
@@ -331,9 +549,8 @@ def run_reference(args):
         "warmup": args.warmup, "ms_per_step": round(1e3 * secs / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic: seeded jittered 200^3 lattice, permuted ids",
-        "config": {"workload": f"{args.n}^3 jittered lattice, {NLEVELS} levels, Mach {MACH}, AoA {AOA} deg, "
-                               f"{L0.nnodes} nodes / {L0.nedges} edges on level 0",
-                   "implementation": "CPU restatement of the reference path (oracle/mgcfd_oracle.c), OpenMP"},
+        "config": line_config(args, L0.nnodes, L0.nedges),
+        "implementation": "CPU restatement of the reference path (oracle/mgcfd_oracle.c), OpenMP over coloured edges",
         "cpu_baseline": {"value": round(value, 4), "unit": "cycles/s", "cores": threads, "kind": "port",
                          "sample": f"{args.steps} V-cycles after {args.warmup} warm-up cycles"},
         "e2e": {"value": round(value, 4), "unit": "cycles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -431,94 +648,58 @@ def run_batch(args):
 
 def run_serve(args):
     """Serving: a Poisson stream of requests, each a seeded lattice mesh with
-    node count log-uniform in 20K..4M (a pool of distinct meshes drawn per
-    request), Mach U(0.3, 0.85), AoA U(0, 6) degrees, 3 or 4 levels, run until
-    the level-0 density residual falls to 1e-6 of its first value or 50
-    V-cycles, under a 150 GB HBM budget.  Three forms serve the same stream:
-      plain_fp64    one FP64 solve at a time (the plain path),
-      served_fp64   FP64, up to --serve-slots requests overlapping,
-      served_mixed  mixed precision, up to --serve-slots requests overlapping.
-    Capacity is solves/s with every request queued at once; then each form
-    serves Poisson arrivals at rates that are multiples of the plain path's
-    capacity, reporting p50/p99 latency (submit to result) and solves/s."""
-    import threading
-
+    node count log-uniform in 20K..4M, Mach U(0.3, 0.85), AoA U(0, 6)
+    degrees, 3 or 4 levels, run until the level-0 density residual falls to
+    1e-6 of its first value or 50 V-cycles, under a 150 GB HBM budget.  Four
+    forms serve the same stream:
+      plain_fp64           one FP64 solve at a time (the plain path),
+      served_fp64          FP64, up to --serve-slots requests overlapping,
+      served_mixed         mixed precision, overlapping,
+      served_mixed_pair32  mixed precision with compensated FP32-pair sums.
+    Requests draw their meshes from a pool of --serve-pool distinct meshes
+    (default: one per request, at most 128, to bound host memory).  Without
+    --serve-reuse no form keeps a mesh resident, so every request uploads and
+    sets up its mesh, as a fresh mesh would; with it the served forms also
+    report a labelled variant that keeps pool meshes resident between
+    requests.  Capacity is solves/s with every request queued at once; then
+    each form serves Poisson arrivals at rates that are multiples of the plain
+    path's capacity, reporting p50/p99 latency (submit to result)."""
     import numpy as np
-
-    import mgcfd
     rng = np.random.default_rng(11)
-    pool, keep = [], []
-    for i in range(args.serve_pool):
-        nodes = float(np.exp(rng.uniform(np.log(20e3), np.log(4e6))))
-        n = max(8, int(round(nodes ** (1.0 / 3.0))))
-        m = mgcfd.HostMesh.generate(n, int(rng.integers(3, 5)), 500 + i)
-        pool.append(pinned_levels(m.levels(), keep))  # requests arrive in page-locked host memory
     R = args.serve_requests
-    picks = rng.integers(0, len(pool), R)
+    P = args.serve_pool or min(R, 128)
+    keep = []
+    pool = generate_pool(serve_specs(P, rng, 500), keep)
+    picks = np.arange(R) % P if P >= R else rng.integers(0, P, R)
     machs = rng.uniform(0.3, 0.85, R)
     aoas = rng.uniform(0.0, 6.0, R)
     gaps = rng.exponential(1.0, R)  # unit-rate inter-arrival times, scaled per rate
-    # plain_fp64 is the plain path: one FP64 solve at a time, each uploading and
-    # setting up its mesh.  The served forms overlap requests and keep meshes
-    # resident between requests (same pool mesh = same mesh key).
-    forms = {"plain_fp64": dict(max_active=1, precision="fp64"),
-             "served_fp64": dict(max_active=args.serve_slots, precision="fp64"),
-             "served_mixed": dict(max_active=args.serve_slots, precision="mixed"),
-             "served_mixed_pair32": dict(max_active=args.serve_slots, precision="mixed", accumulation="pair32")}
-    resident = {"plain_fp64": False, "served_fp64": True, "served_mixed": True, "served_mixed_pair32": True}
-
-    def serve(form, rate):
-        srv = mgcfd.Server(hbm_budget_gb=150.0, max_cycles=50, residual_drop=1e-6, **forms[form])
-        t_start = time.perf_counter()
-        arrivals = np.cumsum(gaps / rate) if rate else np.zeros(R)
-
-        def feeder():
-            for k in range(R):
-                delay = t_start + arrivals[k] - time.perf_counter()
-                if delay > 0:
-                    time.sleep(delay)
-                key = int(picks[k]) + 1 if resident[form] else None  # same pool mesh = same resident mesh
-                srv.submit(pool[picks[k]], float(machs[k]), float(aoas[k]), mesh_key=key, resident=resident[form])
-
-        th = threading.Thread(target=feeder)
-        th.start()
-        th.join()
-        srv.drain(3600)
-        t_end = time.perf_counter()
-        res = [r for r, _ in srv.poll()]
-        st = srv.stats()
-        srv.close()
-        lat = np.array([r["finish_s"] - r["submit_s"] for r in res])
-        ok = sum(1 for r in res if r["status"] == 0)
-        return {"rate_per_s": round(rate, 3) if rate else "all at once",
-                "solves_per_s": round(len(res) / (t_end - t_start), 3),
-                "p50_ms": round(1e3 * float(np.percentile(lat, 50)), 2),
-                "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 2), "ok": ok, "failed": len(res) - ok,
-                "mean_cycles": round(float(np.mean([r["cycles"] for r in res])), 2),
-                "peak_active": int(st["peak_active"]), "peak_budget_gb": round(st["peak_bytes"] / 2 ** 30, 2),
-                "resident_mesh_hits": int(st["cache_hits"])}
-
-    serve("served_mixed", 0)  # warm-up: CUDA context, memory pool, module load
+    serve_stream(pool, picks[:4], machs, aoas, gaps, "served_mixed", 0, args.serve_slots, False)  # warm-up
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as sampler:
-        capacity = {f: serve(f, 0) for f in forms}
+        capacity = {f: serve_stream(pool, picks, machs, aoas, gaps, f, 0, args.serve_slots, False)[0]
+                    for f in SERVE_FORMS}
+        reuse = ({f"{f}_resident": serve_stream(pool, picks, machs, aoas, gaps, f, 0, args.serve_slots, True)[0]
+                  for f in SERVE_FORMS if f != "plain_fp64"} if args.serve_reuse else {})
         plain_cap = capacity["plain_fp64"]["solves_per_s"]
         rates = [f * plain_cap for f in args.serve_rate_multiples]
-        sweep = {f: [serve(f, r) for r in rates] for f in forms}
-    cap = {f: capacity[f]["solves_per_s"] for f in forms}
+        sweep = {f: [serve_stream(pool, picks, machs, aoas, gaps, f, r, args.serve_slots, False)[0] for r in rates]
+                 for f in SERVE_FORMS}
+    cap = {f: capacity[f]["solves_per_s"] for f in SERVE_FORMS}
+    sizes = [L[0].nnodes for L in pool]
     line = {"metric": "served solves/s and p50/p99 latency (Poisson stream), vs the plain FP64 path",
             "unit": "solves/s", "higher_is_better": True, "n_gpus": 1,
             "data": "synthetic: seeded jittered lattices",
-            "config": {"workload": f"{R} requests over a pool of {len(pool)} meshes "
-                                   f"({min(m[0].nnodes for m in pool)}..{max(m[0].nnodes for m in pool)} "
+            "config": {"workload": f"{R} requests over {P} distinct meshes ({min(sizes)}..{max(sizes)} "
                                    "level-0 nodes, 3-4 levels), 50 V-cycles or residual drop 1e-6, "
-                                   "HBM budget 150 GB",
+                                   "HBM budget 150 GB; no mesh kept resident in the headline forms",
                        "slots": args.serve_slots, "rate_multiples_of_plain_capacity": args.serve_rate_multiples,
                        "inputs": "page-locked host memory"},
             "value": cap["served_mixed"], "capacity_solves_per_s": cap,
             "speedup_served_mixed_vs_plain_fp64": round(cap["served_mixed"] / cap["plain_fp64"], 3),
             "speedup_served_mixed_pair32_vs_plain_fp64": round(cap["served_mixed_pair32"] / cap["plain_fp64"], 3),
             "speedup_served_fp64_vs_plain_fp64": round(cap["served_fp64"] / cap["plain_fp64"], 3),
-            "capacity_runs": capacity, "sweep": sweep, "clocks": sampler.summary()}
+            "capacity_runs": capacity, "resident_mesh_variant": reuse or None, "sweep": sweep,
+            "clocks": sampler.summary()}
     print(json.dumps(line), flush=True)
 
 
@@ -557,10 +738,21 @@ def main():
     ap.add_argument("--mode", default="plain", choices=["plain", "batch", "serve", "rates"])
     ap.add_argument("--batch-meshes", type=int, default=64)
     ap.add_argument("--serve-requests", type=int, default=240)
-    ap.add_argument("--serve-pool", type=int, default=24)
+    ap.add_argument("--serve-pool", type=int, default=0,
+                    help="distinct meshes the requests draw from (0: one per request, at most 128)")
+    ap.add_argument("--serve-reuse", action="store_true",
+                    help="also report the served forms with pool meshes kept resident between requests")
     ap.add_argument("--serve-rate-multiples", type=float, nargs="*", default=[0.5, 0.9, 2.0],
                     help="Poisson rates as multiples of the plain path's capacity (none: capacity only)")
     ap.add_argument("--serve-slots", type=int, default=16)
+    ap.add_argument("--kernel-cycles", type=int, default=5,
+                    help="V-cycles of the separate per-kernel event pass behind the roofline")
+    ap.add_argument("--no-extra-forms", action="store_true",
+                    help="plain line only: skip the mixed-precision and served sections")
+    ap.add_argument("--line-serve-requests", type=int, default=64,
+                    help="requests (each its own mesh) of the served section of the plain line")
+    ap.add_argument("--line-serve-rate", type=float, default=0.8,
+                    help="Poisson rate of the served section, as a multiple of the plain path's capacity")
     args = ap.parse_args()
     if args.warmup < 0 or args.steps < 1:
         ap.error("need --steps >= 1 and --warmup >= 0")
