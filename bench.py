@@ -10,6 +10,7 @@ Mach 0.8, angle of attack 3 degrees, FP64.  One step = one V-cycle
                   [--precision fp64|mixed] [--increment atomic|gather] [--n 200]
   python bench.py --mode batch     # 64 uneven meshes in one launch per stage
   python bench.py --mode serve     # Poisson request stream, p50/p99 latency
+  python bench.py --mode loops     # the V-cycle through the per-loop entry points
 
 Prints one JSON line.  `value` is V-cycles/s with the mesh resident in HBM
 (the default CUDA-graph path, timed with CUDA events on the solver's stream),
@@ -703,6 +704,116 @@ def run_serve(args):
     print(json.dumps(line), flush=True)
 
 
+def run_loops(args):
+    """The reference's V-cycle driven loop by loop through the per-loop entry
+    points (mgcfd.LoopSolver: every op_par_loop of euler3d.cpp:413-641 one
+    mgcfd_op_* call on device dats in OP2 layout, as an OP2 host stub bound to
+    this library would issue them), on the same 8M-node mesh:
+      file_order  the mesh's own numbering (node ids randomly permuted): the
+                  edge-flux plan reorders the nodes (Cuthill-McKee on the GPU)
+      renumbered  the mesh after the renumbering tool (Morton order): the
+                  plan keeps the caller's order
+      plan_free   file order with plans off (the naive per-loop kernels), a
+                  few cycles, for contrast
+    V-cycles/s from CUDA events on the driver's stream; the level-0 edge-flux
+    call (primitives, flux, scatter) timed alone with events; the first cycle
+    (upload, set-up loops, plan builds) reported separately; the final state
+    checked against the device-resident solver after the same cycles."""
+    import numpy as np
+    import torch
+
+    import mgcfd
+    from mgcfd import ops
+    mesh = mgcfd.HostMesh.generate(args.n, NLEVELS, SEED)
+    L0 = mesh.level(0)
+    N, E = L0.nnodes, L0.nedges
+    total = 1 + args.warmup + args.steps
+    ref = mgcfd.Solver(mesh, MACH, AOA)
+    ref.run(total)
+    assert ref.synchronize() == 0
+    want = ref.fetch(0)
+    ref.close()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stream = torch.cuda.Stream()
+    ref = mgcfd.Solver(mesh, MACH, AOA, stream=stream.cuda_stream)
+    ref.run(args.warmup)
+    ref.synchronize()
+    secs, _ = timed_cycles(ref, stream, args.steps)
+    solver_value = args.steps / secs
+    ref.close()
+    peak, peak_kind = measured_peaks()
+    forms = {"file_order": ("auto", mesh), "renumbered": ("auto", mesh.renumber("spatial"))}
+    out = {}
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as sampler:
+        for name, (mode, m) in forms.items():
+            ops.plans_mode(mode)
+            t0 = time.perf_counter()
+            s = mgcfd.LoopSolver(m, MACH, AOA, stream=stream)
+            s.run(1)
+            st, _ = s.synchronize()
+            first = time.perf_counter() - t0
+            s.run(args.warmup)
+            s.synchronize()
+            e0.record(stream)
+            s.run(args.steps)
+            e1.record(stream)
+            st, rms = s.synchronize()
+            secs = e0.elapsed_time(e1) * 1e-3
+            got = s.fetch(0)
+            if name == "renumbered":  # back to the file order of the reference solution
+                perm = np.empty(N, np.int64)
+                perm[:] = mgcfd.renumber_nodes("spatial", L0.coords)
+                back = np.empty_like(got)
+                back[perm] = got
+                got = back
+            err = float((np.abs(got - want).max(axis=0) / np.abs(want).max(axis=0)).max())
+            d = s.L[0]
+            reps = 10
+            e0.record(stream)
+            for _ in range(reps):
+                ops.compute_flux_edge(E, N, d["e2n"].data_ptr(), d["var"].data_ptr(), d["ewt"].data_ptr(),
+                                      s.ff.smoothing_coefficient, d["flux"].data_ptr(), s.s)
+            e1.record(stream)
+            stream.synchronize()
+            flux_ms = e0.elapsed_time(e1) / reps
+            info = ops.plans_info()
+            s.close()
+            byt = algorithmic_flux_bytes(N, E)
+            out[name] = {"value": round(args.steps / secs, 3), "unit": "cycles/s", "status": st,
+                         "first_cycle_s": round(first, 3), "plans": info,
+                         "max_rel_vs_solver": float(f"{err:.3e}"),
+                         "flux_call_ms": round(flux_ms, 4),
+                         "flux_call_vs_solver_flux": None,
+                         "roofline": {"bound": "hbm", "achieved": round(byt / (flux_ms * 1e-3) / 1e9, 1), "peak": peak,
+                                      "unit": "GB/s", "frac": round(byt / (flux_ms * 1e-3) / 1e9 / peak, 4),
+                                      "algorithmic_bytes_per_launch": byt, "peak_source": peak_kind}}
+        ops.plans_mode("off")
+        s = mgcfd.LoopSolver(mesh, MACH, AOA, stream=stream)
+        s.run(1)
+        s.synchronize()
+        e0.record(stream)
+        s.run(args.loops_plan_free_cycles)
+        e1.record(stream)
+        st, _ = s.synchronize()
+        out["plan_free"] = {"value": round(args.loops_plan_free_cycles / (e0.elapsed_time(e1) * 1e-3), 3),
+                            "unit": "cycles/s", "status": st, "cycles": args.loops_plan_free_cycles}
+        s.close()
+        ops.plans_mode("auto")
+    solver_flux_ms = kernel_times(mesh, args.kernel_cycles)
+    for name in ("file_order", "renumbered"):
+        out[name]["flux_call_vs_solver_flux"] = round(out[name]["flux_call_ms"] / solver_flux_ms, 3)
+    line = {"metric": "MG V-cycles/s at 8M nodes through the per-loop entry points (OP2 dat layout)",
+            "unit": "cycles/s", "higher_is_better": True, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "data": "synthetic: seeded jittered 200^3 lattice, permuted ids",
+            "config": line_config(args, N, E),
+            "value": out["file_order"]["value"], "forms": out,
+            "device_solver": {"value": round(solver_value, 3), "unit": "cycles/s",
+                              "flux_ms_per_launch": round(solver_flux_ms, 4)},
+            "timing": "CUDA events on the driver's stream; globals stay on the device (no host wait per loop)",
+            "clocks": sampler.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def run_rates(args):
     """Issue rates of the arithmetic the kernels are built from (FP64/FP32
     FMA, reciprocal, square root, rsqrt, format conversions, FP64 atomics,
@@ -735,7 +846,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-cycles", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--mode", default="plain", choices=["plain", "batch", "serve", "rates"])
+    ap.add_argument("--mode", default="plain", choices=["plain", "batch", "serve", "rates", "loops"])
+    ap.add_argument("--loops-plan-free-cycles", type=int, default=2)
     ap.add_argument("--batch-meshes", type=int, default=64)
     ap.add_argument("--serve-requests", type=int, default=240)
     ap.add_argument("--serve-pool", type=int, default=0,
@@ -764,6 +876,8 @@ def main():
         run_serve(args)
     elif args.mode == "rates":
         run_rates(args)
+    elif args.mode == "loops":
+        run_loops(args)
     else:
         run_gb300(args)
 

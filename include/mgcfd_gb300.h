@@ -222,6 +222,39 @@ int mgcfd_op_down(int32_t nfine, int32_t ncoarse, const int32_t* node_to_mg, dou
  * counted in mgcfd_op_map_errors. */
 int mgcfd_op_restrict_noalloc(int32_t nfine, int32_t ncoarse, const int32_t* node_to_mg,
                               const double* fine_variables, double* coarse_variables, void* stream);
+/* Execution plans of the per-loop entry points.  As OP2's CUDA backend builds
+ * and caches a plan for an indirect loop on its first call (op_plan_get),
+ * mgcfd_op_compute_flux_edge and mgcfd_op_up_pre / mgcfd_op_up build one per
+ * map on first use and reuse it on every later call with the same map
+ * pointer and set sizes:
+ *   - edge flux: a locality order of the nodes (the caller's own when its
+ *     edges join nearby ids, else a Cuthill-McKee order built on the GPU),
+ *     the edges sorted in it, and work space; each call computes every
+ *     node's primitives once, the edge fluxes with FP64 atomics that stay in
+ *     L2, and adds the increments onto the caller's rows.  |w| is kept per
+ *     edge and recomputed only when the weight's bits change;
+ *   - restriction: the children of every coarse node, so up_kernel is a
+ *     gather with no atomics (results independent of scheduling).
+ * A plan holds integer structure derived from the map only: the map's
+ * contents must not change while it is cached (OP2 maps are immutable too).
+ * Building a plan synchronises the caller's stream; a first call made while
+ * the stream captures a CUDA graph runs the plan-free kernel instead.  Calls
+ * on the same map share the plan's work space: issue them in stream order.
+ * Before freeing a map, or reusing its memory for another map, release its
+ * plans with mgcfd_op_plan_release(map) (plans on the current device built
+ * from that pointer); mgcfd_op_plans_release frees every plan.  Both
+ * synchronise the device.  mgcfd_op_plans_mode selects how plans built
+ * from then on order the nodes (AUTO: the caller's order unless more than a
+ * tenth of the edges join ids over max(65536, N/128) apart; REORDER: always
+ * the Cuthill-McKee order; CALLER_ORDER: never) or switches plans off (OFF:
+ * plan-free kernels for every later call).  mgcfd_op_plans_info reports the
+ * plans held (any pointer may be NULL).  These have no counterpart in the
+ * reference's source: OP2 does this inside its runtime. */
+enum { MGCFD_PLANS_OFF = 0, MGCFD_PLANS_AUTO = 1, MGCFD_PLANS_REORDER = 2, MGCFD_PLANS_CALLER_ORDER = 3 };
+int mgcfd_op_plans_mode(int32_t mode);
+int mgcfd_op_plan_release(const void* map);
+int mgcfd_op_plans_release(void);
+int mgcfd_op_plans_info(int64_t* edge_plans, int64_t* child_plans, int64_t* reordered, int64_t* device_bytes);
 /* Number of elements the mapped entry points above skipped because a map
  * entry was outside [0, set size) since the last reset; reset != 0 zeroes the
  * counter.  Reads a device counter: call after the streams used are idle. */

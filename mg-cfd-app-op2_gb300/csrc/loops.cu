@@ -2,15 +2,22 @@
 // reference V-cycle, over device arrays in OP2's dat layout (AoS,
 // [set size][dim], 0-based int32 maps).  Indirect OP_INC arguments use FP64
 // atomics (native red.global.add.f64); OP_MIN/OP_INC globals are reduced per
-// block and combined with one atomic per block, so no entry point needs
-// scratch memory.  Map entries are range-checked against the target set
-// size: an element with an out-of-range entry is skipped and counted in
-// g_map_errors (read by mgcfd_op_map_errors), never dereferenced.
+// block and combined with one atomic per block.  Map entries are
+// range-checked against the target set size: an element with an
+// out-of-range entry is skipped and counted in g_map_errors (read by
+// mgcfd_op_map_errors), never dereferenced.
+//
+// The edge flux and the restriction's up_pre/up loops run through an
+// execution plan cached per map (plans.cu), as OP2's CUDA backend caches one
+// per indirect loop: the plan-free kernels below remain for calls made while
+// plans are switched off, or while a stream captures a graph before the
+// map's plan exists.
 #include <cfloat>
 #include <cstdio>
 
 #include "common.h"
 #include "device_math.cuh"
+#include "plans.h"
 
 using namespace mgcfd;
 
@@ -35,6 +42,15 @@ __device__ unsigned long long g_map_errors;
 __device__ __forceinline__ bool in_range(int32_t i, int32_t n) { return (uint32_t)i < (uint32_t)n; }
 
 __device__ __forceinline__ void map_error() { atomicAdd(&g_map_errors, 1ull); }
+
+// Elements a plan left out, counted once per call as the plan-free kernels
+// count them.
+__global__ void k_add_map_errors(unsigned long long n) { atomicAdd(&g_map_errors, n); }
+
+int count_skipped(int64_t n, cudaStream_t s) {
+  if (n > 0) k_add_map_errors<<<1, 1, 0, s>>>((unsigned long long)n);
+  return MGCFD_OK;
+}
 
 #define MGCFD_GRID_STRIDE(i, n) \
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += (int64_t)gridDim.x * blockDim.x)
@@ -419,7 +435,16 @@ extern "C" int mgcfd_op_compute_flux_edge(int32_t ne, int32_t nn, const int32_t*
   CHECK_PTR(e2n, ne, "compute_flux_edge"); CHECK_PTR(v, ne, "compute_flux_edge");
   CHECK_PTR(ewt, ne, "compute_flux_edge"); CHECK_PTR(flux, ne, "compute_flux_edge");
   if (ne == 0) return MGCFD_OK;
-  k_flux_edge<<<grid_for(ne), kThreads, 0, STREAM(s)>>>(ne, nn, e2n, v, ewt, sc, flux);
+  EdgePlan* plan = nullptr;
+  int r = edge_plan_get(e2n, ne, nn, STREAM(s), &plan);
+  if (r) return r;
+  if (plan) {
+    int64_t skipped = 0;
+    if ((r = edge_plan_flux(plan, v, ewt, sc, flux, STREAM(s), &skipped))) return r;
+    count_skipped(skipped, STREAM(s));
+  } else {
+    k_flux_edge<<<grid_for(ne), kThreads, 0, STREAM(s)>>>(ne, nn, e2n, v, ewt, sc, flux);
+  }
   return launch_status("compute_flux_edge");
 }
 
@@ -503,7 +528,16 @@ extern "C" int mgcfd_op_up_pre(int32_t nf, int32_t nc, const int32_t* map, doubl
   CHECK_N(nc, "mgcfd_op_up_pre");
   CHECK_PTR(map, nf, "up_pre"); CHECK_PTR(cv, nf, "up_pre"); CHECK_PTR(scratch, nf, "up_pre");
   if (nf == 0) return MGCFD_OK;
-  k_up_pre<<<grid_for(nf), kThreads, 0, STREAM(s)>>>(nf, nc, map, cv, scratch);
+  ChildPlan* plan = nullptr;
+  int r = child_plan_get(map, nf, nc, STREAM(s), &plan);
+  if (r) return r;
+  if (plan) {
+    int64_t skipped = 0;
+    if ((r = child_plan_up_pre(plan, cv, scratch, STREAM(s), &skipped))) return r;
+    count_skipped(skipped, STREAM(s));
+  } else {
+    k_up_pre<<<grid_for(nf), kThreads, 0, STREAM(s)>>>(nf, nc, map, cv, scratch);
+  }
   return launch_status("up_pre");
 }
 
@@ -513,7 +547,16 @@ extern "C" int mgcfd_op_up(int32_t nf, int32_t nc, const int32_t* map, const dou
   CHECK_N(nc, "mgcfd_op_up");
   CHECK_PTR(map, nf, "up"); CHECK_PTR(fv, nf, "up"); CHECK_PTR(cv, nf, "up"); CHECK_PTR(scratch, nf, "up");
   if (nf == 0) return MGCFD_OK;
-  k_up<<<grid_for(nf), kThreads, 0, STREAM(s)>>>(nf, nc, map, fv, cv, scratch);
+  ChildPlan* plan = nullptr;
+  int r = child_plan_get(map, nf, nc, STREAM(s), &plan);
+  if (r) return r;
+  if (plan) {
+    int64_t skipped = 0;
+    if ((r = child_plan_up(plan, fv, cv, scratch, STREAM(s), &skipped))) return r;
+    count_skipped(skipped, STREAM(s));
+  } else {
+    k_up<<<grid_for(nf), kThreads, 0, STREAM(s)>>>(nf, nc, map, fv, cv, scratch);
+  }
   return launch_status("up");
 }
 

@@ -8,3 +8,4 @@ from .mesh import HostMesh, Level, freestream, h5_read, level_views_from_arrays,
 from .solver import Batch, Solver, options, solve  # noqa: F401
 from .solver import Q_FLUXES, Q_OLD_VARIABLES, Q_RESIDUALS, Q_STEP_FACTORS, Q_VARIABLES, Q_VOLUMES  # noqa: F401
 from .server import Server  # noqa: F401
+from .op2_vcycle import LoopSolver  # noqa: F401

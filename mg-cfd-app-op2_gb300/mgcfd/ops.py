@@ -112,3 +112,30 @@ def map_errors(reset=False) -> int:
     v = C.c_int64()
     _call("mgcfd_op_map_errors", C.byref(v), int(reset))
     return v.value
+
+
+PLANS = {"off": 0, "auto": 1, "reorder": 2, "caller_order": 3}
+
+
+def plans_mode(mode="auto"):
+    """How plans built from now on order the nodes ("auto", "reorder",
+    "caller_order"), or "off" for the plan-free kernels."""
+    _call("mgcfd_op_plans_mode", PLANS[mode])
+
+
+def plan_release(map_ptr):
+    """Free the plans built from the map at this device address (before the
+    map's memory is freed or reused; synchronises the device)."""
+    _call("mgcfd_op_plan_release", _p(map_ptr))
+
+
+def plans_release():
+    """Free every cached plan (synchronises the device)."""
+    _call("mgcfd_op_plans_release")
+
+
+def plans_info():
+    """{edge_plans, child_plans, reordered, device_bytes} of the plans held."""
+    v = [C.c_int64() for _ in range(4)]
+    _call("mgcfd_op_plans_info", *[C.byref(x) for x in v])
+    return dict(zip(("edge_plans", "child_plans", "reordered", "device_bytes"), (x.value for x in v)))

@@ -29,3 +29,20 @@ def built():
 def reference_available():
     import recipe as oracle_build
     return oracle_build.reference_dir() is not None
+
+
+@pytest.fixture(autouse=True)
+def release_plans(request):
+    """Per-loop execution plans are cached by map address; device buffers of
+    one test may reuse the addresses of another's, so every GPU test ends by
+    releasing the plans it built."""
+    yield
+    if request.node.get_closest_marker("gpu") is None:
+        return
+    from mgcfd import _lib
+    if _lib._LIB is None:
+        return
+    import torch
+    if torch.cuda.is_available():
+        _lib.check(_lib._LIB.mgcfd_op_plans_release())
+        _lib.check(_lib._LIB.mgcfd_op_plans_mode(1))  # MGCFD_PLANS_AUTO

@@ -29,6 +29,7 @@ def _restrict_with_caller_scratch(nfine, ncoarse, node_to_mg, fine, coarse0):
     ops.up(nfine, ncoarse, m.data_ptr(), fv.data_ptr(), cv.data_ptr(), scratch.data_ptr())
     ops.up_post(ncoarse, cv.data_ptr(), scratch.data_ptr())
     torch.cuda.synchronize()
+    ops.plan_release(m.data_ptr())  # the map's memory is freed on return
     return cv.cpu().numpy()
 
 
