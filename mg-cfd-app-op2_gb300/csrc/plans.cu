@@ -25,10 +25,11 @@
 //     order is not the caller's, the internal increments.
 // A call then runs three kernels: primitives of every node once (gathered
 // from the caller's state), the edge fluxes with FP64 atomics into internal
-// rows that sit close together (so they resolve in L2), and a scatter of the
-// internal increments back onto the caller's flux rows (plain read-add-write:
-// the order is a bijection).  With the caller's own order the last step is
-// skipped and the atomics go straight to the caller's rows.
+// rows that sit close together (so they resolve in L2), and the addition of
+// the internal increments onto the caller's flux rows (each caller row
+// gathers its internal row: the order is a bijection, no atomics).  With the
+// caller's own order the last step is skipped and the atomics go straight to
+// the caller's rows.
 //
 // Children plan (up_pre_kernel / up_kernel, mg.h:29-52; euler3d.cpp:581-588).
 // The fine-to-coarse map's children of every coarse node as a CSR list
@@ -67,6 +68,7 @@ struct EdgePlan {
   int64_t nbad = 0;         // edges skipped (an end out of range)
   bool permuted = false;    // internal order differs from the caller's
   int32_t* perm = nullptr;  // [nn] internal node -> caller node (permuted only)
+  int32_t* pos = nullptr;   // [nn] caller node -> internal node (permuted only)
   int2* e2n = nullptr;      // [nvalid] internal (a, b), a <= b, sorted
   int32_t* eref = nullptr;  // [nvalid] caller edge index, complemented when flipped
   double4_32a* memo = nullptr;  // [nvalid] (h, wfac) of the last weight seen
@@ -282,12 +284,10 @@ __global__ void k_fill_u64(int64_t n, unsigned long long v, unsigned long long* 
 
 // ---- edge plan kernels -------------------------------------------------------
 
-// Primitives of every node in internal order; with a permuted order also the
-// internal increments cleared.
+// Primitives of every node in internal order.
 template <bool PERM>
 __global__ void __launch_bounds__(kT) k_plan_prims(int32_t nn, const int32_t* __restrict__ perm,
-                                                   const double* __restrict__ var, double* __restrict__ rec,
-                                                   double* __restrict__ fl) {
+                                                   const double* __restrict__ var, double* __restrict__ rec) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nn) return;
   const int64_t c = PERM ? (int64_t)perm[i] : i;
@@ -296,10 +296,6 @@ __global__ void __launch_bounds__(kT) k_plan_prims(int32_t nn, const int32_t* __
   double4_32a* r = reinterpret_cast<double4_32a*>(rec + 8 * i);
   r[0] = make_double4_32a(p.rho, p.mx, p.my, p.mz);
   r[1] = make_double4_32a(p.rhoE, p.p, p.s, p.rinv);
-  if (PERM) {
-#pragma unroll
-    for (int k = 0; k < 5; k++) fl[5 * i + k] = 0.0;
-  }
 }
 
 __device__ __forceinline__ NodePrim plan_rec(const double* rec, int64_t i) {
@@ -359,15 +355,16 @@ __global__ void __launch_bounds__(128) k_plan_flux(int32_t ne, const int2* __res
   }
 }
 
-// The internal increments onto the caller's rows (a bijection: no atomics).
-__global__ void k_plan_scatter(int32_t nn, const int32_t* __restrict__ perm, const double* __restrict__ fl,
-                               double* __restrict__ flux) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nn) return;
-  double* o = flux + 5 * (int64_t)perm[i];
-  const double* x = fl + 5 * i;
-#pragma unroll
-  for (int k = 0; k < 5; k++) o[k] += x[k];
+// The internal increments onto the caller's rows: one thread per (caller
+// node, variable), so the caller's flux is read and written coalesced and
+// only the internal rows are gathered (five neighbouring threads share a
+// row).  A bijection: no atomics.
+__global__ void k_plan_gather(int64_t n5, const int32_t* __restrict__ pos, const double* __restrict__ fl,
+                              double* __restrict__ flux) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n5) return;
+  const int64_t c = j / 5;
+  flux[j] += fl[5 * (int64_t)pos[c] + (j - 5 * c)];
 }
 
 // ---- children plan -------------------------------------------------------------
@@ -437,7 +434,8 @@ int g_mode = MGCFD_PLANS_AUTO;
 
 void free_edge_plan(EdgePlan* P) {
   if (!P) return;
-  for (void* p : {(void*)P->perm, (void*)P->e2n, (void*)P->eref, (void*)P->memo, (void*)P->rec, (void*)P->fl})
+  for (void* p : {(void*)P->perm, (void*)P->pos, (void*)P->e2n, (void*)P->eref, (void*)P->memo, (void*)P->rec,
+                  (void*)P->fl})
     if (p) cudaFree(p);
   delete P;
 }
@@ -563,7 +561,8 @@ int build_edge_plan(const int32_t* e2n, int32_t ne, int32_t nn, int mode, cudaSt
   P->permuted = mode == MGCFD_PLANS_REORDER || (mode == MGCFD_PLANS_AUTO && h[1] * 10 > h[0]);
   int32_t* pos = nullptr;
   if (P->permuted) {
-    if ((r = S.get(&pos, (size_t)nn)) || (r = plan_alloc(&P->perm, (size_t)nn, &P->bytes))) return r;
+    if ((r = plan_alloc(&P->pos, (size_t)nn, &P->bytes)) || (r = plan_alloc(&P->perm, (size_t)nn, &P->bytes))) return r;
+    pos = P->pos;
     if ((r = cm_order(e2n, ne, nn, s, S, pos, P->perm))) return r;
   }
   unsigned long long *key, *key_out;
@@ -673,13 +672,14 @@ int edge_plan_flux(EdgePlan* P, const double* var, const double* ewt, double sc,
   const bool memo_valid = P->memo_sc == sc;  // false for NaN: never used yet
   P->memo_sc = sc;
   if (P->permuted) {
-    k_plan_prims<true><<<grid(P->nn), kT, 0, s>>>(P->nn, P->perm, var, P->rec, P->fl);
+    CK(cudaMemsetAsync(P->fl, 0, sizeof(double) * 5 * (size_t)P->nn, s));
+    k_plan_prims<true><<<grid(P->nn), kT, 0, s>>>(P->nn, P->perm, var, P->rec);
     if (P->nvalid > 0)
       k_plan_flux<true><<<grid(P->nvalid, 128), 128, 0, s>>>(P->nvalid, P->e2n, P->eref, ewt, P->memo,
                                                              memo_valid ? 1 : 0, sc, P->rec, P->fl);
-    k_plan_scatter<<<grid(P->nn), kT, 0, s>>>(P->nn, P->perm, P->fl, flux);
+    k_plan_gather<<<grid(5 * (int64_t)P->nn), kT, 0, s>>>(5 * (int64_t)P->nn, P->pos, P->fl, flux);
   } else {
-    k_plan_prims<false><<<grid(P->nn), kT, 0, s>>>(P->nn, nullptr, var, P->rec, nullptr);
+    k_plan_prims<false><<<grid(P->nn), kT, 0, s>>>(P->nn, nullptr, var, P->rec);
     if (P->nvalid > 0)
       k_plan_flux<false><<<grid(P->nvalid, 128), 128, 0, s>>>(P->nvalid, P->e2n, P->eref, ewt, P->memo,
                                                               memo_valid ? 1 : 0, sc, P->rec, flux);
