@@ -225,7 +225,7 @@ def run_gb300(args):
     N, E = L0.nnodes, L0.nedges
     inc = args.increment if args.increment != "auto" else ("fused" if args.precision == "mixed" else "atomic")
     variant = dict(precision=args.precision, increment=args.increment, renumber=args.renumber,
-                   accumulation=args.accumulation)
+                   accumulation=args.accumulation, stage_neighbour_ids=args.stage_ids)
     # The timed region: the production path, one CUDA graph per V-cycle on
     # the solver's stream, timed with CUDA events on that stream.
     stream = torch.cuda.Stream()
@@ -843,6 +843,8 @@ def main():
     ap.add_argument("--accumulation", default="fp64", choices=["fp64", "pair32"],
                     help="mixed precision node sums: FP64 adds, or compensated FP32 pairs")
     ap.add_argument("--n", type=int, default=200)
+    ap.add_argument("--stage-ids", action="store_true",
+                    help="fused mixed stage: stage neighbour ids in shared memory with cp.async (measured slower)")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-cycles", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")

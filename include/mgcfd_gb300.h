@@ -306,7 +306,11 @@ typedef struct mgcfd_solver_options {
                                 (always on for MGCFD_RENUMBER_RCM); same results      */
   int32_t accumulation;      /* MGCFD_ACCUM_*: how mixed precision sums the FP32
                                 edge fluxes of a node (gather increment only)      */
-  int32_t reserved[7];
+  int32_t stage_neighbour_ids; /* FUSED only: copy each block's neighbour ids into
+                                shared memory with cp.async before the edge loop
+                                (same results; measured slower on GB300, off by
+                                default)                                           */
+  int32_t reserved[6];
 } mgcfd_solver_options;
 
 typedef struct mgcfd_solver_stats {

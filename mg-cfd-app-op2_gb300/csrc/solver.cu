@@ -449,8 +449,26 @@ __device__ __forceinline__ void block_norms(double* srms, double* srho, int* sba
 // per SM, a few bytes spilled) it runs 2% faster.  Every other form keeps the
 // compiler's own register choice: a minimum of 0 blocks is no constraint,
 // whereas a minimum of 1 lets it grow to 70-80 registers and lose occupancy.
-template <bool GATHER, bool LAST, bool MIXED, bool SEG, bool PAIR = false, bool FUSED = false>
+// Fused stage, STAGE (option stage_neighbour_ids): the block's neighbour ids
+// (its contiguous ranges of the a-side and b-side edge lists, up to
+// kStageIds each) are copied into shared memory with cp.async at the start,
+// while the node's own data loads, so the edge loop's dependent chain is a
+// shared-memory id load and one gather.  Measured slower on GB300 (8M nodes:
+// 0.689 -> 0.713 ms with FP64 sums, 0.530 -> 0.577 ms with pair sums): the
+// long-scoreboard stalls fall (10.3 -> 9.4 per issue) but the L1 hit rate of
+// the neighbour gathers falls with the shared-memory carve-out (61% -> 53%)
+// and the copies add instructions.  Off by default.
+constexpr int kStageIds = 1024;
+
+__device__ __forceinline__ void cp_async4(int32_t* smem_dst, const int32_t* gsrc) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+template <bool GATHER, bool LAST, bool MIXED, bool SEG, bool PAIR = false, bool FUSED = false, bool STAGE = false>
 __global__ void __launch_bounds__(kNodeThreads, (FUSED && PAIR) ? 10 : 0) k_update(UpdateArgs A) {
+  __shared__ int32_t s_aid[STAGE ? kStageIds : 1], s_bid[STAGE ? kStageIds : 1];
   __shared__ double srms[LAST ? kNodeThreads : 1];
   __shared__ double srho[LAST ? kNodeThreads : 1];
   __shared__ int sbad[LAST ? kNodeThreads : 1];
@@ -459,6 +477,17 @@ __global__ void __launch_bounds__(kNodeThreads, (FUSED && PAIR) ? 10 : 0) k_upda
   __shared__ double s_rho[SEG && LAST ? kNodeThreads : 1];
   __shared__ int s_bad[SEG && LAST ? kNodeThreads : 1];
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int32_t a_base = 0, b_base = 0, a_cnt = 0, b_cnt = 0;
+  if (STAGE) {
+    const int64_t i0 = (int64_t)blockIdx.x * blockDim.x;
+    const int64_t i1 = i0 + blockDim.x < A.n ? i0 + blockDim.x : A.n;
+    a_base = A.a_off[i0];
+    b_base = A.b_off[i0];
+    a_cnt = min(A.a_off[i1] - a_base, kStageIds);
+    b_cnt = min(A.b_off[i1] - b_base, kStageIds);
+    for (int t = threadIdx.x; t < a_cnt; t += blockDim.x) cp_async4(s_aid + t, &A.e2n[a_base + t].y);
+    for (int t = threadIdx.x; t < b_cnt; t += blockDim.x) cp_async4(s_bid + t, A.b_nbr + b_base + t);
+  }
   // The node's own data is loaded before the block-uniform halt and min_dt
   // checks so that its latency overlaps them; nothing is written before.
   double o[5] = {0.0, 0.0, 0.0, 0.0, 0.0}, Fa[5] = {0.0, 0.0, 0.0, 0.0, 0.0}, ivol = 0.0;
@@ -473,6 +502,7 @@ __global__ void __launch_bounds__(kNodeThreads, (FUSED && PAIR) ? 10 : 0) k_upda
   }
   if (threadIdx.x == 0) s_halt = A.st->halt;
   if (SEG && LAST) { s_sum[threadIdx.x] = 0.0; s_rho[threadIdx.x] = 0.0; s_bad[threadIdx.x] = 0; }
+  if (STAGE) cp_async_wait_all();
   __syncthreads();
   if (s_halt) return;  // block-uniform: the reduction below synchronises
   int32_t mid = 0;
@@ -509,7 +539,14 @@ __global__ void __launch_bounds__(kNodeThreads, (FUSED && PAIR) ? 10 : 0) k_upda
       for (int32_t j = 0; j < er.deg; j++) {
         const bool end_a = j < er.na;
         const int32_t ja = end_a ? er.a0 + j : 0, jb = end_a ? 0 : er.b0 + j - er.na;  // both in range
-        const NodePrimF o = load_rec32(A.rec32_in, end_a ? A.e2n[ja].y : A.b_nbr[jb]);
+        int32_t nb;
+        if (STAGE) {
+          const int32_t ka = ja - a_base, kb = jb - b_base;
+          nb = end_a ? (ka < a_cnt ? s_aid[ka] : A.e2n[ja].y) : (kb < b_cnt ? s_bid[kb] : A.b_nbr[jb]);
+        } else {
+          nb = end_a ? A.e2n[ja].y : A.b_nbr[jb];
+        }
+        const NodePrimF o = load_rec32(A.rec32_in, nb);
         const float4 w = end_a ? A.w4f[ja] : A.b_w4f[jb];
         NodePrimF ea = me, eb = o;  // the edge's end a and end b
         if (!end_a) { ea = o; eb = me; }
@@ -802,14 +839,17 @@ void launch_update_pair(int grid_n, cudaStream_t st, const UpdateArgs& A) {
 const UpdateFn kUpdatePair[4] = {launch_update_pair<0, 0>, launch_update_pair<0, 1>, launch_update_pair<1, 0>,
                                  launch_update_pair<1, 1>};
 
-template <bool L, bool S, bool P>
+template <bool L, bool S, bool P, bool G = false>
 void launch_update_fused(int grid_n, cudaStream_t st, const UpdateArgs& A) {
-  k_update<true, L, true, S, P, true><<<grid_n, kNodeThreads, 0, st>>>(A);
+  k_update<true, L, true, S, P, true, G><<<grid_n, kNodeThreads, 0, st>>>(A);
 }
-const UpdateFn kUpdateFused[8] = {launch_update_fused<0, 0, 0>, launch_update_fused<0, 0, 1>,
-                                  launch_update_fused<0, 1, 0>, launch_update_fused<0, 1, 1>,
-                                  launch_update_fused<1, 0, 0>, launch_update_fused<1, 0, 1>,
-                                  launch_update_fused<1, 1, 0>, launch_update_fused<1, 1, 1>};
+const UpdateFn kUpdateFused[16] = {
+    launch_update_fused<0, 0, 0>, launch_update_fused<0, 0, 1>, launch_update_fused<0, 1, 0>,
+    launch_update_fused<0, 1, 1>, launch_update_fused<1, 0, 0>, launch_update_fused<1, 0, 1>,
+    launch_update_fused<1, 1, 0>, launch_update_fused<1, 1, 1>, launch_update_fused<0, 0, 0, 1>,
+    launch_update_fused<0, 0, 1, 1>, launch_update_fused<0, 1, 0, 1>, launch_update_fused<0, 1, 1, 1>,
+    launch_update_fused<1, 0, 0, 1>, launch_update_fused<1, 0, 1, 1>, launch_update_fused<1, 1, 0, 1>,
+    launch_update_fused<1, 1, 1, 1>};
 
 template <bool M, bool S>
 void launch_step_begin(const DevLevel& D, unsigned long long* key, const DevStatus* st, cudaStream_t stream) {
@@ -889,7 +929,8 @@ int enqueue_smooth(mgcfd_solver* s, int level) {
       // into the other buffer: k_step_begin fills rec32 for stage 0.
       A.rec32_in = (rk & 1) ? D.rec32b : D.rec32;
       A.rec32 = (rk & 1) ? D.rec32 : D.rec32b;
-      kUpdateFused[(last ? 4 : 0) | (seg ? 2 : 0) | (pair ? 1 : 0)](grid(D.n, kNodeThreads), s->stream, A);
+      kUpdateFused[(s->stage_ids ? 8 : 0) | (last ? 4 : 0) | (seg ? 2 : 0) | (pair ? 1 : 0)](grid(D.n, kNodeThreads),
+                                                                                        s->stream, A);
       if (time_this) {
         CK(cudaEventRecord(ev.second, s->stream));
         s->pending.push_back(ev);
@@ -1060,6 +1101,7 @@ int resolve_increment(mgcfd_solver* s) {
     return set_error(MGCFD_ERR_INVALID, "the fused increment needs mixed precision");
   s->fused = inc == MGCFD_INCREMENT_FUSED || (inc == MGCFD_INCREMENT_AUTO && mixed);
   s->gather = s->fused || inc == MGCFD_INCREMENT_GATHER;
+  s->stage_ids = s->fused && s->opt.stage_neighbour_ids != 0;
   return MGCFD_OK;
 }
 }  // namespace

@@ -120,6 +120,44 @@ def test_fused_stage_equals_gather_bitwise(n, nl, cycles, host_setup, accumulati
         np.testing.assert_array_equal(a, b)
 
 
+def _dense_levels(n=3000, per_node=20, seed=6):
+    """One level of random nodes with `per_node` random edges each: about ten
+    edges per node on each side, so a block of 128 nodes holds more a-side
+    and b-side edges than the staged id capacity (1,024) and the edge loop
+    falls back to global loads past it."""
+    rng = np.random.default_rng(seed)
+    coords = rng.random((n, 3))
+    a = np.repeat(np.arange(n), per_node)
+    b = (a + rng.integers(1, n, len(a))) % n
+    e = np.stack([a, b], 1)[rng.permutation(len(a))].astype(np.int32)
+    d = coords[e[:, 1]] - coords[e[:, 0]]
+    w = 1e-3 * d / np.linalg.norm(d, axis=1, keepdims=True)
+    bn = rng.choice(n, n // 10, replace=False).astype(np.int32)
+    return [mgcfd.Level(coords=coords, edge_to_nodes=np.ascontiguousarray(e), bnd_to_node=bn,
+                        bnd_group=rng.integers(0, 8, len(bn)).astype(np.int32),
+                        edge_weights=np.ascontiguousarray(w), bnd_weights=rng.normal(size=(len(bn), 3)) * 1e-3,
+                        node_to_mg=None)]
+
+
+@pytest.mark.parametrize("accumulation", ["fp64", "pair32"])
+@pytest.mark.parametrize("mesh_kind", ["lattice", "dense"])
+def test_staged_neighbour_ids_give_the_same_bits(mesh_kind, accumulation):
+    """stage_neighbour_ids only changes where the fused stage reads each
+    neighbour's id from (shared memory filled by cp.async, or global memory
+    past the staged capacity): the results are the unstaged stage's bits."""
+    levels = mgcfd.HostMesh.generate(20, 3, 8).levels() if mesh_kind == "lattice" else _dense_levels()
+    out = {}
+    for staged in (False, True):
+        s = mgcfd.Solver(levels, 0.6, 1.5, precision="mixed", increment="fused", accumulation=accumulation,
+                         stage_neighbour_ids=staged)
+        s.run(3)
+        assert s.synchronize() == 0
+        out[staged] = [s.fetch(l) for l in range(len(levels))]
+        s.close()
+    for a, b in zip(out[False], out[True]):
+        np.testing.assert_array_equal(a, b)
+
+
 def test_fused_needs_mixed_precision():
     mesh = mgcfd.HostMesh.generate(6, 1, 1)
     with pytest.raises(mgcfd._lib.MgcfdError):
