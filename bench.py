@@ -225,7 +225,8 @@ def run_gb300(args):
     N, E = L0.nnodes, L0.nedges
     inc = args.increment if args.increment != "auto" else ("fused" if args.precision == "mixed" else "atomic")
     variant = dict(precision=args.precision, increment=args.increment, renumber=args.renumber,
-                   accumulation=args.accumulation, stage_neighbour_ids=args.stage_ids)
+                   accumulation=args.accumulation, stage_neighbour_ids=args.stage_ids,
+                   edge_parallel_stage=args.edge_parallel)
     # The timed region: the production path, one CUDA graph per V-cycle on
     # the solver's stream, timed with CUDA events on that stream.
     stream = torch.cuda.Stream()
@@ -845,6 +846,8 @@ def main():
     ap.add_argument("--n", type=int, default=200)
     ap.add_argument("--stage-ids", action="store_true",
                     help="fused mixed stage: stage neighbour ids in shared memory with cp.async (measured slower)")
+    ap.add_argument("--edge-parallel", action="store_true",
+                    help="fused mixed stage: edge-parallel form (all edge ends of a block at once, then per-node sums)")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-cycles", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")

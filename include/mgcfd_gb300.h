@@ -310,7 +310,11 @@ typedef struct mgcfd_solver_options {
                                 shared memory with cp.async before the edge loop
                                 (same results; measured slower on GB300, off by
                                 default)                                           */
-  int32_t reserved[6];
+  int32_t edge_parallel_stage; /* FUSED only: each block computes all its nodes'
+                                edge ends at once into shared memory, then every
+                                node sums its own in the gather order (same
+                                results)                                           */
+  int32_t reserved[5];
 } mgcfd_solver_options;
 
 typedef struct mgcfd_solver_stats {

@@ -466,9 +466,29 @@ __device__ __forceinline__ void cp_async4(int32_t* smem_dst, const int32_t* gsrc
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
-template <bool GATHER, bool LAST, bool MIXED, bool SEG, bool PAIR = false, bool FUSED = false, bool STAGE = false>
+// Fused stage, edge-parallel (option edge_parallel_stage): the block's edge
+// ends -- each node's a-side edges then its b-side edges, nodes in order --
+// are processed in chunks of kEpChunk by all threads at once (each end's
+// flux depends on two loads, not on the node's previous edges), the signed
+// FP32 fluxes go to shared memory, and each thread then sums its own node's
+// ends in the gather order: the same operations on the same inputs in the
+// same order as the per-node loop, so the same bits.  Measured slower on
+// GB300 (8M nodes: 0.690 -> 0.876 ms with FP64 sums, 0.530 -> 0.785 ms with
+// pair sums): a warp of consecutive nodes in the per-node loop gathers
+// overlapping neighbour records together and hits in L1 (61%); spread over
+// the block's threads the ends lose that reuse (47%) and add barrier and
+// shared-memory stalls.  Off by default.
+constexpr int kEpChunk = 768;
+
+template <bool GATHER, bool LAST, bool MIXED, bool SEG, bool PAIR = false, bool FUSED = false, int FV = 0>
 __global__ void __launch_bounds__(kNodeThreads, (FUSED && PAIR) ? 10 : 0) k_update(UpdateArgs A) {
+  constexpr bool STAGE = FV == 1;  // neighbour ids staged by cp.async
+  constexpr bool EP = FV == 2;     // edge-parallel ends through shared memory
   __shared__ int32_t s_aid[STAGE ? kStageIds : 1], s_bid[STAGE ? kStageIds : 1];
+  __shared__ float s_x[EP ? 5 * kEpChunk : 1];
+  __shared__ float4 s_me[EP ? 2 * kNodeThreads : 1];
+  __shared__ int32_t s_ao[EP ? kNodeThreads + 1 : 1], s_bo[EP ? kNodeThreads + 1 : 1], s_na[EP ? kNodeThreads : 1];
+  __shared__ uint8_t s_owner[EP ? kEpChunk : 1];
   __shared__ double srms[LAST ? kNodeThreads : 1];
   __shared__ double srho[LAST ? kNodeThreads : 1];
   __shared__ int sbad[LAST ? kNodeThreads : 1];
@@ -517,6 +537,64 @@ __global__ void __launch_bounds__(kNodeThreads, (FUSED && PAIR) ? 10 : 0) k_upda
       return;
     }
   }
+  // Edge-parallel fused stage: every thread of the block takes part (the
+  // barriers are block-wide), whatever its own node's state.
+  float ep_hi[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, ep_lo[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  double ep_F[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  if (FUSED && EP) {
+    const int t = threadIdx.x;
+    const int64_t i0 = (int64_t)blockIdx.x * blockDim.x;
+    const int nloc = (int)(A.n - i0 < (int64_t)blockDim.x ? A.n - i0 : (int64_t)blockDim.x);
+    const int32_t A0 = A.a_off[i0], B0 = A.b_off[i0];
+    if (t < nloc) {
+      const int32_t ao = A.a_off[i] - A0, bo = A.b_off[i] - B0;
+      s_ao[t] = ao;
+      s_bo[t] = bo;
+      s_na[t] = A.a_off[i + 1] - A.a_off[i];
+      const float4* r = reinterpret_cast<const float4*>(A.rec32_in + 8 * i);
+      s_me[2 * t] = r[0];
+      s_me[2 * t + 1] = r[1];
+    }
+    if (t == 0) {
+      s_ao[nloc] = A.a_off[i0 + nloc] - A0;
+      s_bo[nloc] = A.b_off[i0 + nloc] - B0;
+    }
+    __syncthreads();
+    const int32_t total = s_ao[nloc] + s_bo[nloc];
+    const int32_t my0 = t < nloc ? s_ao[t] + s_bo[t] : 0, my1 = t < nloc ? s_ao[t + 1] + s_bo[t + 1] : 0;
+    for (int32_t c0 = 0; c0 < total; c0 += kEpChunk) {
+      const int32_t c1 = c0 + kEpChunk < total ? c0 + kEpChunk : total;
+      for (int32_t k = (my0 > c0 ? my0 : c0); k < (my1 < c1 ? my1 : c1); k++) s_owner[k - c0] = (uint8_t)t;
+      __syncthreads();
+#pragma unroll 2
+      for (int32_t k = c0 + t; k < c1; k += blockDim.x) {
+        const int u = s_owner[k - c0];
+        const int32_t j = k - (s_ao[u] + s_bo[u]);
+        const bool end_a = j < s_na[u];
+        const int32_t ja = end_a ? A0 + s_ao[u] + j : 0, jb = end_a ? 0 : B0 + s_bo[u] + (j - s_na[u]);
+        const NodePrimF o = load_rec32(A.rec32_in, end_a ? A.e2n[ja].y : A.b_nbr[jb]);
+        const float4 w = end_a ? A.w4f[ja] : A.b_w4f[jb];
+        const float4 m0 = s_me[2 * u], m1 = s_me[2 * u + 1];
+        const NodePrimF me{m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, m1.z, m1.w};
+        NodePrimF ea = me, eb = o;
+        if (!end_a) { ea = o; eb = me; }
+        float f[5];
+        edge_flux_f32(ea, eb, w, f);
+#pragma unroll
+        for (int v = 0; v < 5; v++) s_x[5 * (k - c0) + v] = end_a ? f[v] : -f[v];
+      }
+      __syncthreads();
+      for (int32_t k = (my0 > c0 ? my0 : c0); k < (my1 < c1 ? my1 : c1); k++) {
+#pragma unroll
+        for (int v = 0; v < 5; v++) {
+          const float x = s_x[5 * (k - c0) + v];
+          if (PAIR) two_sum_acc(ep_hi[v], ep_lo[v], x);
+          else ep_F[v] += f2d_bits(x);
+        }
+      }
+      __syncthreads();
+    }
+  }
   double r2 = 0.0, rr = 0.0;
   int bad = 0;
   bool active = i < A.n;
@@ -526,7 +604,10 @@ __global__ void __launch_bounds__(kNodeThreads, (FUSED && PAIR) ? 10 : 0) k_upda
   }
   if (active) {
     double F[5];
-    if (FUSED) {
+    if (FUSED && EP) {
+#pragma unroll
+      for (int k = 0; k < 5; k++) F[k] = PAIR ? f2d_bits(ep_hi[k]) + f2d_bits(ep_lo[k]) : ep_F[k];
+    } else if (FUSED) {
       // Node-centric stage: the flux of each edge of this node, computed from
       // the stage's input primitives exactly as k_flux_mixed computes it
       // (end a first), summed in k_update's gather order.
@@ -839,17 +920,21 @@ void launch_update_pair(int grid_n, cudaStream_t st, const UpdateArgs& A) {
 const UpdateFn kUpdatePair[4] = {launch_update_pair<0, 0>, launch_update_pair<0, 1>, launch_update_pair<1, 0>,
                                  launch_update_pair<1, 1>};
 
-template <bool L, bool S, bool P, bool G = false>
+template <bool L, bool S, bool P, int V = 0>
 void launch_update_fused(int grid_n, cudaStream_t st, const UpdateArgs& A) {
-  k_update<true, L, true, S, P, true, G><<<grid_n, kNodeThreads, 0, st>>>(A);
+  k_update<true, L, true, S, P, true, V><<<grid_n, kNodeThreads, 0, st>>>(A);
 }
-const UpdateFn kUpdateFused[16] = {
-    launch_update_fused<0, 0, 0>, launch_update_fused<0, 0, 1>, launch_update_fused<0, 1, 0>,
-    launch_update_fused<0, 1, 1>, launch_update_fused<1, 0, 0>, launch_update_fused<1, 0, 1>,
-    launch_update_fused<1, 1, 0>, launch_update_fused<1, 1, 1>, launch_update_fused<0, 0, 0, 1>,
+// Indexed by variant (0 per-node loop, 1 staged ids, 2 edge-parallel) * 8 +
+// last * 4 + seg * 2 + pair.
+const UpdateFn kUpdateFused[24] = {
+    launch_update_fused<0, 0, 0, 0>, launch_update_fused<0, 0, 1, 0>, launch_update_fused<0, 1, 0, 0>,
+    launch_update_fused<0, 1, 1, 0>, launch_update_fused<1, 0, 0, 0>, launch_update_fused<1, 0, 1, 0>,
+    launch_update_fused<1, 1, 0, 0>, launch_update_fused<1, 1, 1, 0>, launch_update_fused<0, 0, 0, 1>,
     launch_update_fused<0, 0, 1, 1>, launch_update_fused<0, 1, 0, 1>, launch_update_fused<0, 1, 1, 1>,
     launch_update_fused<1, 0, 0, 1>, launch_update_fused<1, 0, 1, 1>, launch_update_fused<1, 1, 0, 1>,
-    launch_update_fused<1, 1, 1, 1>};
+    launch_update_fused<1, 1, 1, 1>, launch_update_fused<0, 0, 0, 2>, launch_update_fused<0, 0, 1, 2>,
+    launch_update_fused<0, 1, 0, 2>, launch_update_fused<0, 1, 1, 2>, launch_update_fused<1, 0, 0, 2>,
+    launch_update_fused<1, 0, 1, 2>, launch_update_fused<1, 1, 0, 2>, launch_update_fused<1, 1, 1, 2>};
 
 template <bool M, bool S>
 void launch_step_begin(const DevLevel& D, unsigned long long* key, const DevStatus* st, cudaStream_t stream) {
@@ -929,8 +1014,8 @@ int enqueue_smooth(mgcfd_solver* s, int level) {
       // into the other buffer: k_step_begin fills rec32 for stage 0.
       A.rec32_in = (rk & 1) ? D.rec32b : D.rec32;
       A.rec32 = (rk & 1) ? D.rec32 : D.rec32b;
-      kUpdateFused[(s->stage_ids ? 8 : 0) | (last ? 4 : 0) | (seg ? 2 : 0) | (pair ? 1 : 0)](grid(D.n, kNodeThreads),
-                                                                                        s->stream, A);
+      kUpdateFused[8 * s->fused_variant + ((last ? 4 : 0) | (seg ? 2 : 0) | (pair ? 1 : 0))](grid(D.n, kNodeThreads),
+                                                                                           s->stream, A);
       if (time_this) {
         CK(cudaEventRecord(ev.second, s->stream));
         s->pending.push_back(ev);
@@ -1101,7 +1186,7 @@ int resolve_increment(mgcfd_solver* s) {
     return set_error(MGCFD_ERR_INVALID, "the fused increment needs mixed precision");
   s->fused = inc == MGCFD_INCREMENT_FUSED || (inc == MGCFD_INCREMENT_AUTO && mixed);
   s->gather = s->fused || inc == MGCFD_INCREMENT_GATHER;
-  s->stage_ids = s->fused && s->opt.stage_neighbour_ids != 0;
+  s->fused_variant = !s->fused ? 0 : s->opt.edge_parallel_stage ? 2 : s->opt.stage_neighbour_ids ? 1 : 0;
   return MGCFD_OK;
 }
 }  // namespace

@@ -103,7 +103,7 @@ struct mgcfd_solver {
   int64_t launches_per_cycle = 0;
   bool gather = false;  // node-side CSR tables exist (GATHER or FUSED)
   bool fused = false;   // FUSED: flux and update in one node-centric kernel
-  bool stage_ids = false;  // FUSED: neighbour ids staged in shared memory by cp.async
+  int fused_variant = 0;  // FUSED: 0 per-node edge loop, 1 neighbour ids staged by cp.async, 2 edge-parallel
   cudaGraphExec_t graph = nullptr;
   // Kernel timing.
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending, spare;

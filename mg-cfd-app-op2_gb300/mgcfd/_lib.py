@@ -34,7 +34,8 @@ class SolverOptions(C.Structure):
     _fields_ = [("precision", C.c_int32), ("increment", C.c_int32), ("renumber", C.c_int32),
                 ("use_graph", C.c_int32), ("measure_mem_bound", C.c_int32), ("block_size", C.c_int32),
                 ("time_kernels", C.c_int32), ("host_setup", C.c_int32), ("accumulation", C.c_int32),
-                ("stage_neighbour_ids", C.c_int32), ("reserved", C.c_int32 * 6)]
+                ("stage_neighbour_ids", C.c_int32), ("edge_parallel_stage", C.c_int32),
+                ("reserved", C.c_int32 * 5)]
 
 
 class SolverStats(C.Structure):

@@ -17,7 +17,7 @@ Q_VARIABLES, Q_FLUXES, Q_STEP_FACTORS, Q_VOLUMES, Q_RESIDUALS, Q_OLD_VARIABLES =
 
 def options(precision="fp64", increment="auto", renumber="spatial", use_graph=True, measure_mem_bound=False,
             block_size=0, time_kernels=False, host_setup=False, accumulation="fp64",
-            stage_neighbour_ids=False) -> _lib.SolverOptions:
+            stage_neighbour_ids=False, edge_parallel_stage=False) -> _lib.SolverOptions:
     o = _lib.SolverOptions()
     _lib.load().mgcfd_solver_default_options(C.byref(o))
     o.precision = PRECISION[precision]
@@ -30,6 +30,7 @@ def options(precision="fp64", increment="auto", renumber="spatial", use_graph=Tr
     o.host_setup = int(host_setup)
     o.accumulation = ACCUMULATION[accumulation]
     o.stage_neighbour_ids = int(stage_neighbour_ids)
+    o.edge_parallel_stage = int(edge_parallel_stage)
     return o
 
 

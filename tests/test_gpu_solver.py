@@ -139,23 +139,35 @@ def _dense_levels(n=3000, per_node=20, seed=6):
                         node_to_mg=None)]
 
 
+@pytest.mark.parametrize("variant", ["stage_neighbour_ids", "edge_parallel_stage"])
 @pytest.mark.parametrize("accumulation", ["fp64", "pair32"])
 @pytest.mark.parametrize("mesh_kind", ["lattice", "dense"])
-def test_staged_neighbour_ids_give_the_same_bits(mesh_kind, accumulation):
-    """stage_neighbour_ids only changes where the fused stage reads each
-    neighbour's id from (shared memory filled by cp.async, or global memory
-    past the staged capacity): the results are the unstaged stage's bits."""
+def test_fused_stage_variants_give_the_same_bits(mesh_kind, accumulation, variant):
+    """The fused stage's variants change only where values travel: neighbour
+    ids from shared memory filled by cp.async (global memory past the staged
+    capacity), or every edge end of a block computed at once into shared
+    memory and summed per node afterwards (in several chunks on the dense
+    mesh).  The results are the per-node loop's bits, alone and batched."""
     levels = mgcfd.HostMesh.generate(20, 3, 8).levels() if mesh_kind == "lattice" else _dense_levels()
     out = {}
-    for staged in (False, True):
+    for on in (False, True):
         s = mgcfd.Solver(levels, 0.6, 1.5, precision="mixed", increment="fused", accumulation=accumulation,
-                         stage_neighbour_ids=staged)
+                         **{variant: on})
         s.run(3)
         assert s.synchronize() == 0
-        out[staged] = [s.fetch(l) for l in range(len(levels))]
+        out[on] = [s.fetch(l) for l in range(len(levels))] + [s.fetch(0, mgcfd.Q_RESIDUALS)]
         s.close()
     for a, b in zip(out[False], out[True]):
         np.testing.assert_array_equal(a, b)
+    if mesh_kind == "lattice":
+        other = mgcfd.HostMesh.generate(9, 3, 4).levels()
+        b = mgcfd.Batch([levels, other], [0.6, 0.4], [1.5, 0.0], precision="mixed", increment="fused",
+                        accumulation=accumulation, **{variant: True})
+        b.run(3)
+        assert b.synchronize() == 0
+        for l in range(len(levels)):
+            np.testing.assert_array_equal(b.fetch_mesh(0, l), out[False][l])
+        b.close()
 
 
 def test_fused_needs_mixed_precision():
