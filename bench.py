@@ -408,10 +408,22 @@ def serve_specs(count, rng, seed0):
     return out
 
 
+# Served forms: slots=1 serves one request at a time; the others overlap up
+# to --serve-slots requests.  The *_cohorts forms also admit requests of at
+# most COHORT_NODES level-0 nodes that wait together as one batched solver
+# (up to 16 per cohort, one launch per stage).
+COHORT_NODES = 262144
 SERVE_FORMS = {"plain_fp64": dict(slots=1, precision="fp64"),
+               "serial_mixed": dict(slots=1, precision="mixed"),
                "served_fp64": dict(precision="fp64"),
                "served_mixed": dict(precision="mixed"),
-               "served_mixed_pair32": dict(precision="mixed", accumulation="pair32")}
+               "served_mixed_pair32": dict(precision="mixed", accumulation="pair32"),
+               "served_mixed_cohorts": dict(precision="mixed", batch_max_meshes=16, batch_max_nodes=COHORT_NODES),
+               "served_mixed_pair32_cohorts": dict(precision="mixed", accumulation="pair32", batch_max_meshes=16,
+                                                   batch_max_nodes=COHORT_NODES)}
+RATE_FORMS = ("plain_fp64", "served_mixed", "served_mixed_pair32", "served_mixed_cohorts",
+              "served_mixed_pair32_cohorts")
+ERROR_FORMS = ("served_mixed", "served_mixed_pair32", "served_mixed_cohorts", "served_mixed_pair32_cohorts")
 
 
 def serve_stream(pool, picks, machs, aoas, gaps, form, rate, slots, reuse, want_results=False):
@@ -460,7 +472,8 @@ def serve_stream(pool, picks, machs, aoas, gaps, form, rate, slots, reuse, want_
             "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 2), "ok": ok, "failed": len(res) - ok,
             "mean_cycles": round(float(np.mean([r["cycles"] for r in res])), 2),
             "peak_active": int(st["peak_active"]), "peak_budget_gb": round(st["peak_bytes"] / 2 ** 30, 2),
-            "resident_mesh_hits": int(st["cache_hits"])}, results
+            "resident_mesh_hits": int(st["cache_hits"]), "cohorts": int(st["cohorts"]),
+            "cohort_requests": int(st["cohort_requests"])}, results
 
 
 def served_section(args):
@@ -483,12 +496,12 @@ def served_section(args):
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as sampler:
         for f in SERVE_FORMS:
             cap[f], results[f] = serve_stream(pool, picks, machs, aoas, gaps, f, 0, args.serve_slots, False,
-                                              want_results=f != "served_fp64")
+                                              want_results=f == "plain_fp64" or f in ERROR_FORMS)
         rate = args.line_serve_rate * cap["plain_fp64"]["solves_per_s"]
         at_rate = {f: serve_stream(pool, picks, machs, aoas, gaps, f, rate, args.serve_slots, False)[0]
-                   for f in ("plain_fp64", "served_mixed", "served_mixed_pair32")}
+                   for f in RATE_FORMS}
     err = {}
-    for f in ("served_mixed", "served_mixed_pair32"):
+    for f in ERROR_FORMS:
         worst, same = 0.0, 0
         for k, (r, v) in results[f].items():
             rp, vp = results["plain_fp64"][k]
@@ -506,6 +519,11 @@ def served_section(args):
             "speedup_served_mixed_vs_plain_fp64": round(c["served_mixed"] / c["plain_fp64"], 3),
             "speedup_served_mixed_pair32_vs_plain_fp64": round(c["served_mixed_pair32"] / c["plain_fp64"], 3),
             "speedup_served_fp64_vs_plain_fp64": round(c["served_fp64"] / c["plain_fp64"], 3),
+            "speedup_served_mixed_cohorts_vs_plain_fp64": round(c["served_mixed_cohorts"] / c["plain_fp64"], 3),
+            "speedup_served_mixed_pair32_cohorts_vs_plain_fp64": round(c["served_mixed_pair32_cohorts"] /
+                                                                       c["plain_fp64"], 3),
+            "cohort_rule": f"requests of at most {COHORT_NODES} level-0 nodes waiting together share one batched "
+                           "solver (up to 16)",
             "poisson": {"rate_multiple_of_plain_capacity": args.line_serve_rate, "runs": at_rate},
             "final_state_error": err, "capacity_runs": cap, "clocks": sampler.summary()}
 
@@ -681,11 +699,11 @@ def run_serve(args):
         capacity = {f: serve_stream(pool, picks, machs, aoas, gaps, f, 0, args.serve_slots, False)[0]
                     for f in SERVE_FORMS}
         reuse = ({f"{f}_resident": serve_stream(pool, picks, machs, aoas, gaps, f, 0, args.serve_slots, True)[0]
-                  for f in SERVE_FORMS if f != "plain_fp64"} if args.serve_reuse else {})
+                  for f in ("served_fp64", "served_mixed", "served_mixed_pair32")} if args.serve_reuse else {})
         plain_cap = capacity["plain_fp64"]["solves_per_s"]
         rates = [f * plain_cap for f in args.serve_rate_multiples]
         sweep = {f: [serve_stream(pool, picks, machs, aoas, gaps, f, r, args.serve_slots, False)[0] for r in rates]
-                 for f in SERVE_FORMS}
+                 for f in RATE_FORMS}
     cap = {f: capacity[f]["solves_per_s"] for f in SERVE_FORMS}
     sizes = [L[0].nnodes for L in pool]
     line = {"metric": "served solves/s and p50/p99 latency (Poisson stream), vs the plain FP64 path",
@@ -700,6 +718,7 @@ def run_serve(args):
             "speedup_served_mixed_vs_plain_fp64": round(cap["served_mixed"] / cap["plain_fp64"], 3),
             "speedup_served_mixed_pair32_vs_plain_fp64": round(cap["served_mixed_pair32"] / cap["plain_fp64"], 3),
             "speedup_served_fp64_vs_plain_fp64": round(cap["served_fp64"] / cap["plain_fp64"], 3),
+            "speedup_served_mixed_cohorts_vs_plain_fp64": round(cap["served_mixed_cohorts"] / cap["plain_fp64"], 3),
             "capacity_runs": capacity, "resident_mesh_variant": reuse or None, "sweep": sweep,
             "clocks": sampler.summary()}
     print(json.dumps(line), flush=True)

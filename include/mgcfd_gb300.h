@@ -408,8 +408,16 @@ void mgcfd_solver_destroy(mgcfd_solver* s);
 /* time, and retires it when its level-0 density residual has dropped below */
 /* residual_drop times its first value, it fails (min_dt < 0, NaN/Inf), or  */
 /* max_cycles is reached.  A request's arithmetic is that of a solver       */
-/* running alone, so with MGCFD_INCREMENT_GATHER its result is identical    */
-/* alone and in any mix.                                                     */
+/* running alone, so with MGCFD_INCREMENT_GATHER or _FUSED its result is    */
+/* identical alone and in any mix.                                           */
+/* Cohorts (batch_max_meshes > 1): small requests -- at most                 */
+/* batch_max_nodes level-0 nodes -- that wait next to each other in the     */
+/* queue with the same number of levels are admitted together as one        */
+/* batched solver (mgcfd_batch_create: one launch per V-cycle stage for all */
+/* of them, one slot), each with its own stop rule: a request that meets it */
+/* or fails stops changing while the others go on; the cohort's results are */
+/* copied out when its last request has stopped.  Batched kernels do the    */
+/* arithmetic of the solver alone, so results stay identical.               */
 typedef struct mgcfd_server_options {
   int64_t hbm_budget_bytes;  /* admission budget for all active requests          */
   int32_t max_active;        /* concurrent requests (one stream each)              */
@@ -418,7 +426,9 @@ typedef struct mgcfd_server_options {
   int32_t max_cycles;        /* V-cycles per request at most                       */
   double residual_drop;      /* stop when rho_rms <= residual_drop * first rho_rms */
   int32_t accumulation;      /* MGCFD_ACCUM_* for mixed precision                 */
-  int32_t reserved[7];
+  int32_t batch_max_meshes;  /* requests per cohort (<= 64); 0 or 1: no cohorts    */
+  int32_t batch_max_nodes;   /* level-0 nodes of a request that may join a cohort  */
+  int32_t reserved[5];
 } mgcfd_server_options;
 
 typedef struct mgcfd_request_result {
@@ -436,7 +446,8 @@ typedef struct mgcfd_server_stats {
   int64_t used_bytes, peak_bytes, peak_active;  /* used_bytes includes idle cached solvers */
   int64_t cache_hits;                           /* requests that reused a resident mesh   */
   int64_t cached_solvers;                       /* idle solvers held for reuse            */
-  int64_t reserved[2];
+  int64_t cohorts;                              /* batched solvers admitted               */
+  int64_t cohort_requests;                      /* requests admitted inside them          */
 } mgcfd_server_stats;
 
 typedef struct mgcfd_server mgcfd_server;

@@ -8,11 +8,12 @@
 //     on its slot's stream (upload, device setup), installs the device-side
 //     stop rule and enqueues the first V-cycles.  Retirement copies the final
 //     level-0 state out, frees the solver and releases slot and budget.
-//   * the progress thread keeps every active request's stream fed.  Cycles
-//     are enqueued in chunks of kChunk V-cycles (CUDA graph launches), each
-//     followed by an asynchronous copy of the solver's status block to pinned
-//     memory and an event; up to kDepth chunks are in flight per request, so
-//     the stream never waits for the host between chunks.
+//   * the progress thread keeps every active job's stream fed (a job is one
+//     request's solver, or a cohort's batched solver).  Cycles are enqueued in
+//     chunks of kChunk V-cycles (CUDA graph launches), each followed by an
+//     asynchronous copy of the solver's status (per mesh for a cohort) to
+//     pinned memory and an event; up to kDepth chunks are in flight per job,
+//     so the stream never waits for the host between chunks.
 // The stop rule runs on the device at the end of every V-cycle (k_cycle_end):
 // it counts cycles, records the level-0 density residual norm and, once the
 // norm has dropped to residual_drop times the first cycle's or max_cycles is
@@ -27,11 +28,22 @@
 // (solver_retarget): no upload and no setup.  Idle solvers are evicted, least
 // recently used first, when a new mesh needs their budget.
 //
+// Cohorts: with batch_max_meshes > 1, small requests (at most batch_max_nodes
+// level-0 nodes) that wait next to each other at the front of the queue with
+// the same number of levels are admitted together into one slot as one
+// batched solver (mgcfd_batch_create): every V-cycle stage is one launch over
+// all of their meshes, which matters for meshes too small to fill the GPU on
+// their own.  The batched solver carries the stop rule per mesh
+// (k_cycle_end_seg): a request that meets it, or fails, stops changing while
+// the others go on, and its cycle count and residual norms are its own.  The
+// cohort retires when its last request has stopped; each request's record and
+// level-0 state are then published.
+//
 // Requests therefore join and leave at V-cycle boundaries and their kernels
 // overlap on the device (continuous batching at V-cycle granularity).  Each
-// request's arithmetic is exactly that of a solver running alone, so with the
-// deterministic gather increment a result is bit-identical alone and in any
-// mix.
+// request's arithmetic is exactly that of a solver running alone -- batched
+// kernels included -- so with a deterministic increment (gather or the fused
+// stage) a result is bit-identical alone, in the mix and in a cohort.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -51,8 +63,9 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
-constexpr int kChunk = 4;  // V-cycles per enqueued chunk
-constexpr int kDepth = 2;  // chunks in flight per request
+constexpr int kChunk = 4;       // V-cycles per enqueued chunk
+constexpr int kDepth = 2;       // chunks in flight per job
+constexpr int kMaxCohort = 64;  // requests per cohort at most
 
 struct Request {
   int64_t id = 0;
@@ -62,16 +75,34 @@ struct Request {
   double* out = nullptr;  // level-0 variables [N0][5] on completion, may be NULL
   int64_t estimate = 0;
   double t_submit = 0, t_admit = -1, t_finish = -1;
+  int cycles = 0;
+  double rho_first = -1, rho_last = -1;
+  int status = MGCFD_OK;
+};
+
+// What one slot runs: one request's own solver, or a cohort of requests in
+// one batched solver (request m is the batch's mesh m).
+struct Job {
+  std::vector<Request*> reqs;
   mgcfd_solver* solver = nullptr;
+  bool cohort = false;
   int slot = -1;
+  int64_t charged = 0;   // budget charged for this job (0: never admitted)
   int enqueued = 0;      // V-cycles enqueued so far
   int inflight = 0;      // chunks not yet seen complete
   int next_buf = 0;      // status buffer of the next chunk
   int oldest_buf = 0;    // status buffer of the oldest chunk in flight
   bool ending = false;   // no more chunks: waiting for the ones in flight
-  int cycles = 0;
-  double rho_first = -1, rho_last = -1;
-  int status = MGCFD_OK;
+  int status = MGCFD_OK; // failure of the job itself (set-up, CUDA)
+};
+
+// Copied to page-locked memory after every chunk: the solver's status block
+// and, for a cohort, every mesh's stop rule and failure flags.
+struct ChunkStatus {
+  DevStatus st;
+  SegStop seg[kMaxCohort];
+  int neg[kMaxCohort];
+  int bad[kMaxCohort];
 };
 
 }  // namespace
@@ -83,8 +114,8 @@ struct mgcfd_server {
   std::mutex mu;
   std::condition_variable cv;
   std::deque<Request*> pending;
-  std::vector<Request*> active;
-  std::deque<Request*> retiring;
+  std::vector<Job*> active;
+  std::deque<Job*> retiring;
   std::vector<mgcfd_request_result> done;
   struct Idle {
     int64_t key;
@@ -93,19 +124,23 @@ struct mgcfd_server {
   };
   std::list<Idle> idle_cache;  // front = most recently used
   bool stop = false;
-  int admitting = 0;  // requests between pending and active
-  int retiring_now = 0;  // requests taken for retirement whose record is not yet published
+  int admitting = 0;     // jobs between pending and active
+  int retiring_now = 0;  // jobs taken for retirement whose records are not yet published
+  int64_t active_requests = 0;
   int64_t next_id = 1;
   int64_t used = 0;
   std::vector<cudaEvent_t> events;  // [slot][kDepth]
   std::vector<int> slot_free;
-  DevStatus* pinned = nullptr;      // [slot][kDepth] status blocks
+  ChunkStatus* pinned = nullptr;    // [slot][kDepth]
   Clock::time_point t0;
   mgcfd_server_stats stats{};
 
   double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
   bool idle() const {
     return pending.empty() && active.empty() && retiring.empty() && admitting == 0 && retiring_now == 0;
+  }
+  bool batchable(const Request* r) const {
+    return opt.batch_max_meshes > 1 && r->levels[0].nnodes <= opt.batch_max_nodes;
   }
 };
 
@@ -130,59 +165,111 @@ int64_t estimate_bytes(const std::vector<mgcfd_level_view>& lv, int precision, i
   return b;
 }
 
-// Host-work thread: copy the result out, free the solver, publish the record.
-void retire(mgcfd_server* S, Request* r) {
+// Host-work thread: copy the results out, free or cache the solver, publish
+// one record per request.
+void retire(mgcfd_server* S, Job* job) {
   bool cached = false;
-  if (r->solver) {
-    if (r->out && r->status == MGCFD_OK) {
-      int st = mgcfd_solver_fetch(r->solver, 0, MGCFD_Q_VARIABLES, r->out);
-      if (st) r->status = st;
+  if (job->solver) {
+    if (job->status == MGCFD_OK) {
+      for (size_t m = 0; m < job->reqs.size(); m++) {
+        Request* r = job->reqs[m];
+        if (!r->out || r->status != MGCFD_OK) continue;
+        const int st = job->cohort ? mgcfd_solver_fetch_mesh(job->solver, (int32_t)m, 0, MGCFD_Q_VARIABLES, r->out)
+                                   : mgcfd_solver_fetch(job->solver, 0, MGCFD_Q_VARIABLES, r->out);
+        if (st) r->status = st;
+      }
     }
-    if (r->key != 0 && r->status == MGCFD_OK) {
+    Request* r0 = job->reqs[0];
+    if (!job->cohort && r0->key != 0 && job->status == MGCFD_OK && r0->status == MGCFD_OK) {
       std::lock_guard<std::mutex> lock(S->mu);
-      S->idle_cache.push_front({r->key, r->solver, r->estimate});
+      S->idle_cache.push_front({r0->key, job->solver, job->charged});
       cached = true;
     } else {
-      mgcfd_solver_destroy(r->solver);
+      mgcfd_solver_destroy(job->solver);
     }
-    r->solver = nullptr;
+    job->solver = nullptr;
   }
-  r->t_finish = S->now();
-  mgcfd_request_result res;
-  std::memset(&res, 0, sizeof(res));
-  res.id = r->id;
-  res.status = r->status;
-  res.cycles = r->cycles;
-  res.submit_s = r->t_submit;
-  res.admit_s = r->t_admit;
-  res.finish_s = r->t_finish;
-  res.rho_rms_first = r->rho_first;
-  res.rho_rms_last = r->rho_last;
+  const double t = S->now();
   std::lock_guard<std::mutex> lock(S->mu);
-  if (r->slot >= 0) S->slot_free[(size_t)r->slot] = 1;
-  if (!cached) S->used -= r->t_admit >= 0 ? r->estimate : 0;
-  S->done.push_back(res);
-  S->stats.completed++;
-  if (r->status != MGCFD_OK) S->stats.failed++;
+  for (Request* r : job->reqs) {
+    if (job->status != MGCFD_OK && r->status == MGCFD_OK) r->status = job->status;
+    r->t_finish = t;
+    mgcfd_request_result res;
+    std::memset(&res, 0, sizeof(res));
+    res.id = r->id;
+    res.status = r->status;
+    res.cycles = r->cycles;
+    res.submit_s = r->t_submit;
+    res.admit_s = r->t_admit;
+    res.finish_s = r->t_finish;
+    res.rho_rms_first = r->rho_first;
+    res.rho_rms_last = r->rho_last;
+    S->done.push_back(res);
+    S->stats.completed++;
+    if (r->status != MGCFD_OK) S->stats.failed++;
+    delete r;
+  }
+  if (job->slot >= 0) {
+    S->slot_free[(size_t)job->slot] = 1;
+    S->active_requests -= (int64_t)job->reqs.size();
+  }
+  if (!cached) S->used -= job->charged;
   S->retiring_now--;
   S->cv.notify_all();
-  delete r;
+  delete job;
 }
 
-// Enqueue the next chunk of V-cycles, then the status copy and its event.
-int enqueue_chunk(mgcfd_server* S, Request* r) {
-  const int n = std::min(kChunk, S->opt.max_cycles - r->enqueued);
-  int st = mgcfd_solver_run(r->solver, n);
+// Enqueue the next chunk of V-cycles, then the status copies and their event.
+int enqueue_chunk(mgcfd_server* S, Job* job) {
+  const int n = std::min(kChunk, S->opt.max_cycles - job->enqueued);
+  int st = mgcfd_solver_run(job->solver, n);
   if (st) return st;
-  r->enqueued += n;
-  const size_t k = (size_t)r->slot * kDepth + (size_t)r->next_buf;
-  const cudaStream_t s = r->solver->stream;
-  cudaError_t e = cudaMemcpyAsync(&S->pinned[k], r->solver->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);
+  job->enqueued += n;
+  const size_t k = (size_t)job->slot * kDepth + (size_t)job->next_buf;
+  mgcfd_solver* sv = job->solver;
+  const cudaStream_t s = sv->stream;
+  ChunkStatus* c = &S->pinned[k];
+  cudaError_t e = cudaMemcpyAsync(&c->st, sv->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);
+  if (job->cohort) {
+    const size_t m = job->reqs.size();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->seg, sv->seg_stop, sizeof(SegStop) * m, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->neg, sv->seg_neg, sizeof(int) * m, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->bad, sv->seg_bad, sizeof(int) * m, cudaMemcpyDeviceToHost, s);
+  }
   if (e == cudaSuccess) e = cudaEventRecord(S->events[k], s);
   if (e != cudaSuccess) return mgcfd::set_error(MGCFD_ERR_CUDA, std::string("server: ") + cudaGetErrorString(e));
-  r->next_buf = (r->next_buf + 1) % kDepth;
-  r->inflight++;
+  job->next_buf = (job->next_buf + 1) % kDepth;
+  job->inflight++;
   return MGCFD_OK;
+}
+
+// Builds the job's solver: a cached solver retargeted, a new solver, or one
+// batched solver for a cohort; every one with the server's stop rule.
+int start_job(mgcfd_server* S, Job* job, mgcfd_solver* reuse, const mgcfd_solver_options& so) {
+  Request* r0 = job->reqs[0];
+  int st;
+  if (reuse) {
+    job->solver = reuse;
+    return mgcfd::solver_retarget(reuse, r0->mach, r0->aoa);
+  }
+  if (job->cohort) {
+    const size_t m = job->reqs.size();
+    std::vector<const mgcfd_level_view*> lv(m);
+    std::vector<double> mach(m), aoa(m);
+    for (size_t i = 0; i < m; i++) {
+      lv[i] = job->reqs[i]->levels.data();
+      mach[i] = job->reqs[i]->mach;
+      aoa[i] = job->reqs[i]->aoa;
+    }
+    st = mgcfd_batch_create((int32_t)m, (int32_t)r0->levels.size(), lv.data(), mach.data(), aoa.data(), &so, nullptr,
+                            &job->solver);
+  } else {
+    st = mgcfd_solver_create((int32_t)r0->levels.size(), r0->levels.data(), r0->mach, r0->aoa, &so, nullptr,
+                             &job->solver);
+  }
+  if (st == MGCFD_OK) st = mgcfd::solver_set_stop_rule(job->solver, S->opt.max_cycles, S->opt.residual_drop);
+  (void)S;
+  return st;
 }
 
 // Host-work thread: admission and retirement.
@@ -194,7 +281,7 @@ void host_main(mgcfd_server* S) {
   so.increment = S->opt.increment;
   so.accumulation = S->opt.accumulation;
   for (;;) {
-    Request* r = nullptr;
+    Job* job = nullptr;
     bool admit = false;
     mgcfd_solver* reuse = nullptr;        // an idle solver of this request's mesh
     std::vector<mgcfd_solver*> victims;  // idle solvers evicted to make room
@@ -202,7 +289,7 @@ void host_main(mgcfd_server* S) {
       std::unique_lock<std::mutex> lock(S->mu);
       for (;;) {
         if (!S->retiring.empty()) {
-          r = S->retiring.front();
+          job = S->retiring.front();
           S->retiring.pop_front();
           S->retiring_now++;
           break;
@@ -212,43 +299,88 @@ void host_main(mgcfd_server* S) {
           if (f->estimate > S->opt.hbm_budget_bytes) {  // can never fit
             S->pending.pop_front();
             f->status = MGCFD_ERR_BUDGET;
+            job = new Job();
+            job->reqs.push_back(f);
             S->retiring_now++;
-            r = f;
             break;
           }
           int slot = -1;
           for (size_t k = 0; k < S->slot_free.size(); k++)
             if (S->slot_free[k]) { slot = (int)k; break; }
           if (slot >= 0) {
-            auto hit = S->idle_cache.end();
-            if (f->key != 0)
-              for (auto it = S->idle_cache.begin(); it != S->idle_cache.end(); ++it)
-                if (it->key == f->key) { hit = it; break; }
-            bool fits = hit != S->idle_cache.end();
-            if (fits) {  // already charged to the budget
-              reuse = hit->solver;
-              f->estimate = hit->estimate;
-              S->idle_cache.erase(hit);
-              S->stats.cache_hits++;
-            } else {
-              // Evict least recently used idle solvers until the new mesh fits.
-              while (S->used + f->estimate > S->opt.hbm_budget_bytes && !S->idle_cache.empty()) {
+            // A cohort: the run of batchable requests at the front of the
+            // queue with the first one's number of levels.
+            std::vector<Request*> co;
+            int64_t co_bytes = 0;
+            if (S->batchable(f)) {
+              for (Request* r : S->pending) {
+                if ((int)co.size() >= std::min(S->opt.batch_max_meshes, kMaxCohort) || !S->batchable(r) ||
+                    r->levels.size() != f->levels.size())
+                  break;
+                co.push_back(r);
+                co_bytes += r->estimate;
+              }
+            }
+            if (co.size() >= 2) {
+              while (S->used + co_bytes > S->opt.hbm_budget_bytes && !S->idle_cache.empty()) {
                 victims.push_back(S->idle_cache.back().solver);
                 S->used -= S->idle_cache.back().estimate;
                 S->idle_cache.pop_back();
               }
-              fits = S->used + f->estimate <= S->opt.hbm_budget_bytes;
-              if (fits) S->used += f->estimate;
+              while (co.size() > 1 && S->used + co_bytes > S->opt.hbm_budget_bytes) {
+                co_bytes -= co.back()->estimate;
+                co.pop_back();
+              }
             }
-            if (fits) {
-              S->pending.pop_front();
+            if (co.size() >= 2) {
+              job = new Job();
+              job->cohort = true;
+              job->reqs = co;
+              job->charged = co_bytes;
+              S->used += co_bytes;
+              for (size_t k = 0; k < co.size(); k++) S->pending.pop_front();
+              S->stats.cohorts++;
+              S->stats.cohort_requests += (int64_t)co.size();
+              admit = true;
+            } else {
+              auto hit = S->idle_cache.end();
+              if (f->key != 0)
+                for (auto it = S->idle_cache.begin(); it != S->idle_cache.end(); ++it)
+                  if (it->key == f->key) { hit = it; break; }
+              bool fits = hit != S->idle_cache.end();
+              int64_t charged = f->estimate;
+              if (fits) {  // already charged to the budget
+                reuse = hit->solver;
+                charged = hit->estimate;
+                S->idle_cache.erase(hit);
+                S->stats.cache_hits++;
+              } else {
+                // Evict least recently used idle solvers until the new mesh fits.
+                while (S->used + f->estimate > S->opt.hbm_budget_bytes && !S->idle_cache.empty()) {
+                  victims.push_back(S->idle_cache.back().solver);
+                  S->used -= S->idle_cache.back().estimate;
+                  S->idle_cache.pop_back();
+                }
+                fits = S->used + f->estimate <= S->opt.hbm_budget_bytes;
+                if (fits) S->used += f->estimate;
+              }
+              if (fits) {
+                S->pending.pop_front();
+                job = new Job();
+                job->reqs.push_back(f);
+                job->charged = charged;
+                admit = true;
+              }
+            }
+            if (admit) {
               S->slot_free[(size_t)slot] = 0;
               S->stats.peak_bytes = std::max(S->stats.peak_bytes, S->used);
-              f->slot = slot;
-              f->t_admit = S->now();
+              job->slot = slot;
+              const double t = S->now();
+              for (Request* r : job->reqs) r->t_admit = t;
+              S->active_requests += (int64_t)job->reqs.size();
+              S->stats.peak_active = std::max(S->stats.peak_active, S->active_requests);
               S->admitting++;
-              r = f;
-              admit = true;
               break;
             }
           }
@@ -263,41 +395,57 @@ void host_main(mgcfd_server* S) {
       }
     }
     for (mgcfd_solver* v : victims) mgcfd_solver_destroy(v);
-    if (!r) continue;
+    if (!job) continue;
     if (!admit) {
-      retire(S, r);
+      retire(S, job);
       continue;
     }
-    int st;
-    if (reuse) {
-      r->solver = reuse;
-      st = mgcfd::solver_retarget(reuse, r->mach, r->aoa);
-    } else {
-      st = mgcfd_solver_create((int32_t)r->levels.size(), r->levels.data(), r->mach, r->aoa, &so, nullptr, &r->solver);
-      if (st == MGCFD_OK) st = mgcfd::solver_set_stop_rule(r->solver, S->opt.max_cycles, S->opt.residual_drop);
-    }
-    for (int c = 0; st == MGCFD_OK && c < kDepth && r->enqueued < S->opt.max_cycles; c++) st = enqueue_chunk(S, r);
+    int st = start_job(S, job, reuse, so);
+    for (int c = 0; st == MGCFD_OK && c < kDepth && job->enqueued < S->opt.max_cycles; c++) st = enqueue_chunk(S, job);
     {
       std::lock_guard<std::mutex> lock(S->mu);
       S->admitting--;
       if (st == MGCFD_OK) {
-        S->active.push_back(r);
-        S->stats.peak_active = std::max<int64_t>(S->stats.peak_active, (int64_t)S->active.size());
+        S->active.push_back(job);
         S->cv.notify_all();
         continue;
       }
       S->retiring_now++;
     }
-    if (r->solver) cudaStreamSynchronize(r->solver->stream);
-    r->status = st;
-    retire(S, r);
+    if (job->solver) cudaStreamSynchronize(job->solver->stream);
+    job->status = st;
+    retire(S, job);
   }
+}
+
+// Reads one completed chunk's status into the job's requests; true when
+// every request of the job has stopped.
+bool read_chunk(Job* job, const ChunkStatus& c) {
+  if (!job->cohort) {
+    Request* r = job->reqs[0];
+    const DevStatus& h = c.st;
+    r->cycles = h.cycles_done;
+    if (h.cycles_done > 0) { r->rho_first = h.rho_first; r->rho_last = h.rho_last; }
+    if (h.halt && !h.stopped && r->status == MGCFD_OK) r->status = h.neg_dt ? MGCFD_ERR_NEGATIVE_DT : MGCFD_ERR_BAD_VALUES;
+    return h.halt != 0;
+  }
+  bool all = true;
+  for (size_t m = 0; m < job->reqs.size(); m++) {
+    Request* r = job->reqs[m];
+    const SegStop& g = c.seg[m];
+    r->cycles = g.cycles_done;
+    if (g.cycles_done > 0) { r->rho_first = g.rho_first; r->rho_last = g.rho_last; }
+    if (r->status == MGCFD_OK && (c.neg[m] || c.bad[m]))
+      r->status = c.neg[m] ? MGCFD_ERR_NEGATIVE_DT : MGCFD_ERR_BAD_VALUES;
+    all = all && g.halt != 0;
+  }
+  return all;
 }
 
 // Progress thread: completes chunks and enqueues the next ones.
 void progress_main(mgcfd_server* S) {
   cudaSetDevice(S->device);
-  std::vector<Request*> act;
+  std::vector<Job*> act;
   for (;;) {
     {
       std::unique_lock<std::mutex> lock(S->mu);
@@ -309,33 +457,27 @@ void progress_main(mgcfd_server* S) {
       act = S->active;
     }
     bool progressed = false;
-    for (Request* r : act) {
-      const size_t k = (size_t)r->slot * kDepth + (size_t)r->oldest_buf;
+    for (Job* job : act) {
+      const size_t k = (size_t)job->slot * kDepth + (size_t)job->oldest_buf;
       const cudaError_t q = cudaEventQuery(S->events[k]);
       if (q == cudaErrorNotReady) continue;
       progressed = true;
-      r->inflight--;
-      r->oldest_buf = (r->oldest_buf + 1) % kDepth;
+      job->inflight--;
+      job->oldest_buf = (job->oldest_buf + 1) % kDepth;
       if (q != cudaSuccess) {
-        r->status = mgcfd::set_error(MGCFD_ERR_CUDA, std::string("server: ") + cudaGetErrorString(q));
-        r->ending = true;
-      } else {
-        const DevStatus& h = S->pinned[k];
-        r->cycles = h.cycles_done;
-        if (h.cycles_done > 0) { r->rho_first = h.rho_first; r->rho_last = h.rho_last; }
-        if (h.halt) {
-          if (!h.stopped && r->status == MGCFD_OK) r->status = h.neg_dt ? MGCFD_ERR_NEGATIVE_DT : MGCFD_ERR_BAD_VALUES;
-          r->ending = true;
-        }
+        job->status = mgcfd::set_error(MGCFD_ERR_CUDA, std::string("server: ") + cudaGetErrorString(q));
+        job->ending = true;
+      } else if (read_chunk(job, S->pinned[k])) {
+        job->ending = true;
       }
-      if (!r->ending && r->enqueued < S->opt.max_cycles) {
-        const int st = enqueue_chunk(S, r);
-        if (st) { r->status = st; r->ending = true; }
+      if (!job->ending && job->enqueued < S->opt.max_cycles) {
+        const int st = enqueue_chunk(S, job);
+        if (st) { job->status = st; job->ending = true; }
       }
-      if (r->inflight == 0) {  // nothing left on the device for this request
+      if (job->inflight == 0) {  // nothing left on the device for this job
         std::lock_guard<std::mutex> lock(S->mu);
-        S->active.erase(std::find(S->active.begin(), S->active.end(), r));
-        S->retiring.push_back(r);
+        S->active.erase(std::find(S->active.begin(), S->active.end(), job));
+        S->retiring.push_back(job);
         S->cv.notify_all();
       }
     }
@@ -363,14 +505,15 @@ extern "C" int mgcfd_server_create(const mgcfd_server_options* opt, mgcfd_server
   if (!S) return mgcfd::set_error(MGCFD_ERR_NOMEM, "host allocation failed");
   if (opt) S->opt = *opt; else mgcfd_server_default_options(&S->opt);
   if (S->opt.max_active < 1 || S->opt.max_active > 1024 || S->opt.max_cycles < 1 || S->opt.hbm_budget_bytes <= 0 ||
-      (S->opt.precision != MGCFD_PRECISION_FP64 && S->opt.precision != MGCFD_PRECISION_MIXED))
+      (S->opt.precision != MGCFD_PRECISION_FP64 && S->opt.precision != MGCFD_PRECISION_MIXED) ||
+      S->opt.batch_max_meshes < 0 || S->opt.batch_max_meshes > kMaxCohort || S->opt.batch_max_nodes < 0)
     return mgcfd::set_error(MGCFD_ERR_INVALID, "mgcfd_server_create: bad options");
   CK(cudaGetDevice(&S->device));
   const int k = S->opt.max_active;
   S->events.resize((size_t)k * kDepth);
   S->slot_free.assign((size_t)k, 1);
   for (auto& ev : S->events) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-  CK(cudaMallocHost(reinterpret_cast<void**>(&S->pinned), sizeof(DevStatus) * (size_t)k * kDepth));
+  CK(cudaMallocHost(reinterpret_cast<void**>(&S->pinned), sizeof(ChunkStatus) * (size_t)k * kDepth));
   S->t0 = Clock::now();
   mgcfd_server* raw = S.get();
   S->host_worker = std::thread(host_main, raw);
@@ -434,7 +577,7 @@ extern "C" int mgcfd_server_get_stats(mgcfd_server* S, mgcfd_server_stats* out) 
   std::lock_guard<std::mutex> lock(S->mu);
   *out = S->stats;
   out->used_bytes = S->used;
-  out->active = (int64_t)S->active.size() + S->admitting;
+  out->active = S->active_requests;
   out->pending = (int64_t)S->pending.size();
   out->cached_solvers = (int64_t)S->idle_cache.size();
   return MGCFD_OK;

@@ -184,7 +184,8 @@ __global__ void __launch_bounds__(kNodeThreads) k_step_begin(int32_t n, double* 
                                                              const double* __restrict__ cbrt_vol,
                                                              unsigned long long* __restrict__ dt_key,
                                                              const DevStatus* __restrict__ st,
-                                                             const int32_t* __restrict__ mesh_id) {
+                                                             const int32_t* __restrict__ mesh_id,
+                                                             const SegStop* __restrict__ seg_stop) {
   __shared__ unsigned long long smin[kNodeThreads / 32];
   __shared__ unsigned int sest[kNodeThreads / 32];
   __shared__ int s_halt;
@@ -199,7 +200,9 @@ __global__ void __launch_bounds__(kNodeThreads) k_step_begin(int32_t n, double* 
   unsigned long long key = ~0ull;
   double cv = 0.0, sp = 1.0;  // FP64: cbrt(vol) and |u| + c of this node
   float est = 0.0f;
-  if (i < n) {
+  // Batched solvers under a stop rule: a stopped mesh's nodes change no more.
+  const bool live = i < n && !(SEG && seg_stop && seg_stop[mesh_id[i]].halt);
+  if (live) {
     const double4_32a* r = reinterpret_cast<const double4_32a*>(rec + 8 * i);
     const double4_32a x = r[0];
     const double e = r[1].x;
@@ -226,7 +229,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_step_begin(int32_t n, double* 
     // estimate -- and only they divide in FP64.  Estimates that are not
     // finite normal numbers always take the exact path.
     const uint32_t eb = __float_as_uint(est) & 0x7fffffffu;
-    const bool normal = i < n && eb - 0x00800000u < 0x7f000000u;
+    const bool normal = live && eb - 0x00800000u < 0x7f000000u;
     unsigned int ek = normal ? fkey(est) : 0xffffffffu;
     ek = __reduce_min_sync(0xffffffffu, ek);
     if ((threadIdx.x & 31) == 0) sest[threadIdx.x >> 5] = ek;
@@ -235,7 +238,7 @@ __global__ void __launch_bounds__(kNodeThreads) k_step_begin(int32_t n, double* 
 #pragma unroll
     for (int w = 1; w < kNodeThreads / 32; w++) bk = min(bk, sest[w]);
     const float m32 = bk == 0xffffffffu ? INFINITY : fkey_inv(bk);
-    if (i < n && (!normal || est <= m32 + fabsf(m32) * 4e-6f))
+    if (live && (!normal || est <= m32 + fabsf(m32) * 4e-6f))
       key = dt_candidate_key(0.5 * (cv / sp));  // time_stepping_kernels.h:31
   }
   if (SEG) {
@@ -377,6 +380,7 @@ struct UpdateArgs {
   int* seg_bad;
   double* seg_rms;
   double* seg_rho;
+  const SegStop* seg_stop;           // batched solvers under a stop rule, else null
 };
 
 // Boundary flux of one node (flux.h:14-39 summed over the node's entries).
@@ -598,6 +602,7 @@ __global__ void __launch_bounds__(kNodeThreads, (FUSED && PAIR) ? 10 : 0) k_upda
   double r2 = 0.0, rr = 0.0;
   int bad = 0;
   bool active = i < A.n;
+  if (SEG && active && A.seg_stop && A.seg_stop[mid].halt) active = false;  // a stopped mesh
   if (SEG && active && min_dt < 0.0) {
     atomicOr(A.seg_neg + mid, 1);
     active = false;
@@ -762,7 +767,9 @@ template <bool NORMS>
 __global__ void __launch_bounds__(kNodeThreads) k_restrict(int32_t nc, const int32_t* __restrict__ ch_off,
                                                            const int32_t* __restrict__ ch_list,
                                                            const double* __restrict__ frec, double* __restrict__ crec,
-                                                           const double* __restrict__ fres, DevStatus* st) {
+                                                           const double* __restrict__ fres, DevStatus* st,
+                                                           const int32_t* __restrict__ mesh_id,
+                                                           const SegStop* __restrict__ seg_stop) {
   __shared__ double srms[NORMS ? kNodeThreads : 1], srho[NORMS ? kNodeThreads : 1];
   __shared__ int sbad[NORMS ? kNodeThreads : 1];
   __shared__ int s_halt;
@@ -777,7 +784,8 @@ __global__ void __launch_bounds__(kNodeThreads) k_restrict(int32_t nc, const int
   double q[5] = {0.0, 0.0, 0.0, 0.0, 0.0};  // sums of squared residuals, one chain per variable
   int bad = 0;
   const int32_t lo = c < nc ? ch_off[c] : 0, hi = c < nc ? ch_off[c + 1] : 0;
-  if (hi > lo) {  // no children: state unchanged (avg = 1 on untouched values)
+  const bool halted = c < nc && seg_stop && seg_stop[mesh_id[c]].halt;  // a stopped mesh of a batch
+  if (hi > lo && !halted) {  // no children: state unchanged (avg = 1 on untouched values)
     double s[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
     for (int32_t j = lo; j < hi; j++) {
       const int64_t f = ch_list[j];
@@ -806,10 +814,12 @@ __global__ void __launch_bounds__(kNodeThreads) k_restrict(int32_t nc, const int
 // down_kernel (mg.h:66-88) with the parent offsets precomputed.
 __global__ void k_prolong(int32_t nf, const int32_t* __restrict__ n2mg, const double4_32a* __restrict__ dvec,
                           double* __restrict__ frec, const double* __restrict__ fres,
-                          const double* __restrict__ cres, const DevStatus* __restrict__ st) {
+                          const double* __restrict__ cres, const DevStatus* __restrict__ st,
+                          const int32_t* __restrict__ mesh_id, const SegStop* __restrict__ seg_stop) {
   if (st->halt) return;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nf) return;
+  if (seg_stop && seg_stop[mesh_id[i]].halt) return;  // a stopped mesh of a batch
   const int64_t c = n2mg[i];
   const double4_32a d = dvec[i];
   // The record's first four values as one 32-byte access, the fifth alone.
@@ -865,6 +875,27 @@ __global__ void k_cycle_end(DevStatus* st, double n0, int32_t max_cycles, double
   if (c >= max_cycles || (drop > 0.0 && c > 1 && rho <= drop * st->rho_first)) {
     st->stopped = 1;
     st->halt = 1;
+  }
+}
+
+// The same per mesh of a batched solver, one thread per mesh: a mesh that
+// met the rule, or failed (min_dt < 0, NaN/Inf), stops changing.
+__global__ void k_cycle_end_seg(int32_t nseg, SegStop* __restrict__ ss, const double* __restrict__ seg_rho,
+                                const double* __restrict__ n0, const int* __restrict__ seg_neg,
+                                const int* __restrict__ seg_bad, int32_t max_cycles, double drop) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= nseg || ss[m].halt) return;
+  if (seg_neg[m] || seg_bad[m]) {
+    ss[m].halt = 1;
+    return;
+  }
+  const int c = ++ss[m].cycles_done;
+  const double rho = sqrt(seg_rho[m] / n0[m]);
+  if (c == 1) ss[m].rho_first = rho;
+  ss[m].rho_last = rho;
+  if (c >= max_cycles || (drop > 0.0 && c > 1 && rho <= drop * ss[m].rho_first)) {
+    ss[m].stopped = 1;
+    ss[m].halt = 1;
   }
 }
 
@@ -937,11 +968,12 @@ const UpdateFn kUpdateFused[24] = {
     launch_update_fused<1, 0, 1, 2>, launch_update_fused<1, 1, 0, 2>, launch_update_fused<1, 1, 1, 2>};
 
 template <bool M, bool S>
-void launch_step_begin(const DevLevel& D, unsigned long long* key, const DevStatus* st, cudaStream_t stream) {
+void launch_step_begin(const DevLevel& D, unsigned long long* key, const DevStatus* st, const SegStop* ss,
+                       cudaStream_t stream) {
   k_step_begin<M, S><<<grid(D.n, kNodeThreads), kNodeThreads, 0, stream>>>(D.n, D.rec, D.rec32, D.old, D.cbrt_vol,
-                                                                            key, st, D.mesh_id);
+                                                                            key, st, D.mesh_id, ss);
 }
-using StepFn = void (*)(const DevLevel&, unsigned long long*, const DevStatus*, cudaStream_t);
+using StepFn = void (*)(const DevLevel&, unsigned long long*, const DevStatus*, const SegStop*, cudaStream_t);
 const StepFn kStepBegin[4] = {launch_step_begin<0, 0>, launch_step_begin<0, 1>, launch_step_begin<1, 0>,
                               launch_step_begin<1, 1>};
 
@@ -968,7 +1000,7 @@ int enqueue_smooth(mgcfd_solver* s, int level) {
       CK(cudaMemsetAsync(s->seg_rho, 0, sizeof(double) * (size_t)s->nseg, s->stream));
     }
   }
-  kStepBegin[(mixed ? 2 : 0) | (seg ? 1 : 0)](D, key, s->st, s->stream);
+  kStepBegin[(mixed ? 2 : 0) | (seg ? 1 : 0)](D, key, s->st, seg ? s->seg_stop : nullptr, s->stream);
   s->launches++;
   const int et = edge_threads(s);
   const bool pair = mixed && s->opt.accumulation == MGCFD_ACCUM_PAIR32;
@@ -1008,6 +1040,7 @@ int enqueue_smooth(mgcfd_solver* s, int level) {
     A.bdata = D.bdata; A.res = D.res; A.dt_key = key; A.st = s->st;
     A.mesh_id = D.mesh_id; A.seg_neg = s->seg_neg; A.seg_bad = s->seg_bad; A.seg_rms = s->seg_rms;
     A.seg_rho = s->seg_rho;
+    A.seg_stop = seg ? s->seg_stop : nullptr;
     A.e2n = D.e2n; A.w4f = D.w4f; A.b_nbr = D.b_nbr; A.b_w4f = D.b_w4f;
     if (s->fused) {
       // Stage rk reads the primitives of stage rk and writes those of rk + 1
@@ -1050,19 +1083,21 @@ int enqueue_iteration(mgcfd_solver* s) {
     s->level++;
     DevLevel& F = s->L[(size_t)s->level - 1];
     DevLevel& Cl = s->L[(size_t)s->level];
+    const SegStop* ss = s->nseg > 1 ? s->seg_stop : nullptr;
     if (s->level == 1 && norms_in_restrict(s))  // level-0 norms of the step just smoothed
       k_restrict<true><<<grid(Cl.n, kNodeThreads), kNodeThreads, 0, s->stream>>>(Cl.n, Cl.ch_off, Cl.ch_list, F.rec,
-                                                                                 Cl.rec, F.res, s->st);
+                                                                                 Cl.rec, F.res, s->st, Cl.mesh_id, ss);
     else
       k_restrict<false><<<grid(Cl.n, kNodeThreads), kNodeThreads, 0, s->stream>>>(Cl.n, Cl.ch_off, Cl.ch_list, F.rec,
-                                                                                  Cl.rec, nullptr, s->st);
+                                                                                  Cl.rec, nullptr, s->st, Cl.mesh_id, ss);
     s->launches++;
     if (s->level == levels - 1) s->up = false;
   } else {
     s->level--;
     DevLevel& F = s->L[(size_t)s->level];
     DevLevel& Cl = s->L[(size_t)s->level + 1];
-    k_prolong<<<grid(F.n, kNodeThreads), kNodeThreads, 0, s->stream>>>(F.n, F.n2mg, F.dvec, F.rec, F.res, Cl.res, s->st);
+    k_prolong<<<grid(F.n, kNodeThreads), kNodeThreads, 0, s->stream>>>(F.n, F.n2mg, F.dvec, F.rec, F.res, Cl.res, s->st,
+                                                                       F.mesh_id, s->nseg > 1 ? s->seg_stop : nullptr);
     s->launches++;
     if (s->level == 0) {
       s->up = true;
@@ -1070,7 +1105,11 @@ int enqueue_iteration(mgcfd_solver* s) {
     }
   }
   if (s->cycle != cycle0 && s->stop_max_cycles > 0) {  // a V-cycle just ended
-    k_cycle_end<<<1, 1, 0, s->stream>>>(s->st, (double)s->L[0].n, s->stop_max_cycles, s->stop_drop);
+    if (s->nseg > 1)
+      k_cycle_end_seg<<<(unsigned)((s->nseg + 127) / 128), 128, 0, s->stream>>>(
+          s->nseg, s->seg_stop, s->seg_rho, s->seg_n0, s->seg_neg, s->seg_bad, s->stop_max_cycles, s->stop_drop);
+    else
+      k_cycle_end<<<1, 1, 0, s->stream>>>(s->st, (double)s->L[0].n, s->stop_max_cycles, s->stop_drop);
     s->launches++;
   }
   CK(cudaGetLastError());
@@ -1150,6 +1189,7 @@ int init_state(mgcfd_solver* s) {
     CK(cudaMemsetAsync(s->seg_bad, 0, sizeof(int) * ns, s->stream));
     CK(cudaMemsetAsync(s->seg_rms, 0, sizeof(double) * ns, s->stream));
     CK(cudaMemsetAsync(s->seg_rho, 0, sizeof(double) * ns, s->stream));
+    if (s->seg_stop) CK(cudaMemsetAsync(s->seg_stop, 0, sizeof(SegStop) * ns, s->stream));
   }
   s->seg_status.assign((size_t)s->nseg, MGCFD_OK);
   CK(cudaGetLastError());
@@ -1423,8 +1463,17 @@ int mgcfd::solver_retarget(mgcfd_solver* s, double mach, double aoa_deg) {
 }
 
 int mgcfd::solver_set_stop_rule(mgcfd_solver* s, int32_t max_cycles, double residual_drop) {
-  if (!s || s->nseg > 1 || max_cycles < 1 || s->graph || s->cycle > 0)
-    return set_error(MGCFD_ERR_INVALID, "stop rule: plain solver before its first cycle only");
+  if (!s || max_cycles < 1 || s->graph || s->cycle > 0)
+    return set_error(MGCFD_ERR_INVALID, "stop rule: before the solver's first cycle only");
+  if (s->nseg > 1 && !s->seg_stop) {
+    const size_t ns = (size_t)s->nseg;
+    std::vector<double> n0(ns);
+    for (size_t m = 0; m < ns; m++) n0[m] = (double)(s->seg_noff[0][m + 1] - s->seg_noff[0][m]);
+    int r;
+    if ((r = s->alloc(&s->seg_stop, ns)) || (r = s->upload(&s->seg_n0, n0.data(), ns))) return r;
+    CK(cudaMemsetAsync(s->seg_stop, 0, sizeof(SegStop) * ns, s->stream));
+    CK(cudaStreamSynchronize(s->stream));  // n0's host buffer
+  }
   s->stop_max_cycles = max_cycles;
   s->stop_drop = residual_drop;
   return MGCFD_OK;

@@ -38,6 +38,18 @@ struct DevStatus {
   double rho_last;
 };
 
+// Per-mesh stop rule of a batched solver (the serving loop's cohorts): like
+// DevStatus's cycles_done / rho_first / rho_last / stopped, one per mesh, and
+// `halt`, which every batched node kernel checks for its node's mesh.
+struct SegStop {
+  int halt;         // non-zero: this mesh's state no longer changes
+  int stopped;      // the stop rule ended this mesh's solve (not an error)
+  int cycles_done;
+  int pad;
+  double rho_first;
+  double rho_last;
+};
+
 struct DevLevel {
   int32_t n = 0, ne = 0, nb = 0;
   int32_t nbrows = 0;  // folded boundary rows in bdata
@@ -93,6 +105,8 @@ struct mgcfd_solver {
   double* seg_rms = nullptr;                     // [nseg] sum of residual^2, last level-0 step
   double* seg_rho = nullptr;                     // [nseg] its density part
   double* seg_ffvar = nullptr;                   // [nseg][5] freestream states
+  SegStop* seg_stop = nullptr;                   // [nseg] per-mesh stop rule (when installed)
+  double* seg_n0 = nullptr;                      // [nseg] level-0 node counts, for the norms
   std::vector<int> seg_status;                   // host copy after synchronize
   // V-cycle state (euler3d.cpp:452-457).
   int64_t cycle = 0;
@@ -158,7 +172,9 @@ int build_fused_tables(mgcfd_solver* s, DevLevel& D);
 // on the same mesh would have them.  Stream-ordered.
 int solver_retarget(mgcfd_solver* s, double mach, double aoa_deg);
 
-// Installs the device-side stop rule on a plain solver before its first run
-// (the V-cycle graph is captured with it).
+// Installs the device-side stop rule before the solver's first run (the
+// V-cycle graph is captured with it).  On a batched solver it applies to
+// every mesh separately: a mesh that meets it (or fails) stops changing
+// while the others go on.
 int solver_set_stop_rule(mgcfd_solver* s, int32_t max_cycles, double residual_drop);
 }  // namespace mgcfd

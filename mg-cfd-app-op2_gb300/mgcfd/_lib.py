@@ -47,7 +47,8 @@ class SolverStats(C.Structure):
 class ServerOptions(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_int64), ("max_active", C.c_int32), ("precision", C.c_int32),
                 ("increment", C.c_int32), ("max_cycles", C.c_int32), ("residual_drop", C.c_double),
-                ("accumulation", C.c_int32), ("reserved", C.c_int32 * 7)]
+                ("accumulation", C.c_int32), ("batch_max_meshes", C.c_int32), ("batch_max_nodes", C.c_int32),
+                ("reserved", C.c_int32 * 5)]
 
 
 class RequestResult(C.Structure):
@@ -60,7 +61,7 @@ class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("failed", C.c_int64), ("active", C.c_int64),
                 ("pending", C.c_int64), ("used_bytes", C.c_int64), ("peak_bytes", C.c_int64),
                 ("peak_active", C.c_int64), ("cache_hits", C.c_int64), ("cached_solvers", C.c_int64),
-                ("reserved", C.c_int64 * 2)]
+                ("cohorts", C.c_int64), ("cohort_requests", C.c_int64)]
 
 
 OK = 0

@@ -22,11 +22,13 @@ def estimate_bytes(mesh, precision: str = "fp64", increment: str = "auto") -> in
 
 
 class Server:
-    """Continuous-batching solve server on one GPU."""
+    """Continuous-batching solve server on one GPU.  batch_max_meshes > 1
+    admits small requests (at most batch_max_nodes level-0 nodes) that wait
+    next to each other as cohorts solved in shared launches."""
 
     def __init__(self, hbm_budget_gb: float = 150.0, max_active: int = 16, precision: str = "fp64",
                  increment: str = "auto", max_cycles: int = 50, residual_drop: float = 1e-6,
-                 accumulation: str = "fp64"):
+                 accumulation: str = "fp64", batch_max_meshes: int = 0, batch_max_nodes: int = 0):
         self._lib = _lib.load()
         o = _lib.ServerOptions()
         self._lib.mgcfd_server_default_options(C.byref(o))
@@ -37,6 +39,8 @@ class Server:
         o.max_cycles = max_cycles
         o.residual_drop = residual_drop
         o.accumulation = ACCUMULATION[accumulation]
+        o.batch_max_meshes = batch_max_meshes
+        o.batch_max_nodes = batch_max_nodes
         h = C.c_void_p()
         _lib.check(self._lib.mgcfd_server_create(C.byref(o), C.byref(h)))
         self._h = h

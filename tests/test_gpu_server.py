@@ -195,3 +195,88 @@ def test_idle_meshes_are_evicted_for_new_ones(meshes):
     srv.close()
     assert [r["status"] for r in res] == [0, 0, 0]
     assert st["cache_hits"] == 0 and st["cached_solvers"] == 1 and st["used_bytes"] <= budget
+
+
+# Cohorts: small requests that wait together are solved as one batched solver.
+COHORT = [(30, 3, 21, 0.5, 2.0), (12, 3, 22, 0.7, 1.0), (9, 3, 23, 0.35, 4.0), (16, 3, 24, 0.8, 0.5),
+          (11, 3, 25, 0.6, 3.0), (14, 3, 26, 0.45, 6.0)]
+
+
+@pytest.fixture(scope="module")
+def cohort_meshes():
+    return [mgcfd.HostMesh.generate(n, nl, seed) for n, nl, seed, _, _ in COHORT]
+
+
+def run_cohort_stream(meshes, cases, **opts):
+    """One slot, every request queued at once: the first is admitted alone
+    and the rest wait behind it, so they are admitted as a cohort."""
+    srv = mgcfd.Server(max_active=1, batch_max_meshes=16, batch_max_nodes=10 ** 7, **opts)
+    ids = {srv.submit(m, c[3], c[4], want_result=True): i for i, (m, c) in enumerate(zip(meshes, cases))}
+    srv.drain(300)
+    out = {ids[r["id"]]: (r, v) for r, v in srv.poll()}
+    st = srv.stats()
+    srv.close()
+    return out, st
+
+
+@pytest.mark.parametrize("opts", [dict(precision="mixed", increment="fused", accumulation="fp64"),
+                                  dict(precision="mixed", increment="fused", accumulation="pair32"),
+                                  dict(precision="fp64", increment="gather")])
+def test_cohort_results_equal_requests_alone_bitwise(cohort_meshes, opts):
+    cycles = 4
+    mix, st = run_cohort_stream(cohort_meshes, COHORT, max_cycles=cycles, **opts)
+    assert st["cohorts"] >= 1 and st["cohort_requests"] >= 2 and st["failed"] == 0
+    for i, (m, c) in enumerate(zip(cohort_meshes, COHORT)):
+        srv = mgcfd.Server(max_active=1, max_cycles=cycles, **opts)
+        rid = srv.submit(m, c[3], c[4], want_result=True)
+        srv.drain(300)
+        (ra, va), = [(r, v) for r, v in srv.poll() if r["id"] == rid]
+        srv.close()
+        rm, vm = mix[i]
+        assert ra["status"] == rm["status"] == 0 and ra["cycles"] == rm["cycles"] == cycles
+        # The norms are sums over blocks with FP64 atomics (order not fixed,
+        # alone or batched); the states are compared bit for bit.
+        assert ra["rho_rms_first"] == pytest.approx(rm["rho_rms_first"], rel=1e-12)
+        assert ra["rho_rms_last"] == pytest.approx(rm["rho_rms_last"], rel=1e-12)
+        np.testing.assert_array_equal(va, vm)
+        if opts["precision"] == "mixed":
+            ref = O.OracleRun(m.levels())
+            assert ref.run(c[3], c[4], cycles)[0] == 0
+            mx, l2 = per_variable_errors(vm, ref.get(0, O.Q_VARIABLES))
+            assert mx.max() <= MIXED_TOL and l2.max() <= MIXED_TOL
+
+
+def test_cohort_stop_rule_is_per_request(cohort_meshes):
+    """residual_drop = 10 is met at every request's second cycle: each stops
+    there although the cohort has more cycles enqueued, and its result is a
+    plain 2-cycle solve's, bit for bit."""
+    mix, st = run_cohort_stream(cohort_meshes, COHORT, increment="gather", max_cycles=50, residual_drop=10.0)
+    assert st["cohort_requests"] >= 2
+    for i, (m, c) in enumerate(zip(cohort_meshes, COHORT)):
+        r, v = mix[i]
+        assert r["status"] == 0 and r["cycles"] == 2 and r["rho_rms_first"] > 0
+        s = mgcfd.Solver(m, c[3], c[4], increment="gather")
+        s.run(2)
+        assert s.synchronize() == 0
+        np.testing.assert_array_equal(v, s.fetch(0))
+        s.close()
+
+
+def test_failing_request_in_a_cohort_stops_alone(cohort_meshes):
+    levels = cohort_meshes[2].levels()
+    bad = [mgcfd.Level(**{k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in L.__dict__.items()
+                          if k != "owner"}) for L in levels]
+    bad[0].edge_weights[5, :] = np.nan
+    meshes = list(cohort_meshes)
+    meshes[2] = bad
+    mix, st = run_cohort_stream(meshes, COHORT, precision="mixed", increment="fused", max_cycles=3)
+    assert st["cohort_requests"] >= 2 and st["failed"] == 1
+    assert mix[2][0]["status"] == mgcfd._lib.ERR_BAD_VALUES
+    for i in (1, 3, 4, 5):
+        r, v = mix[i]
+        assert r["status"] == 0 and r["cycles"] == 3
+        s = mgcfd.Solver(cohort_meshes[i], COHORT[i][3], COHORT[i][4], precision="mixed", increment="fused")
+        s.run(3)
+        assert s.synchronize() == 0
+        np.testing.assert_array_equal(v, s.fetch(0))
+        s.close()
