@@ -437,7 +437,10 @@ typedef struct mgcfd_request_result {
   int32_t cycles;            /* V-cycles run                                       */
   double submit_s, admit_s, finish_s;  /* seconds since the server started       */
   double rho_rms_first, rho_rms_last;  /* level-0 density residual norms         */
-  int64_t reserved[2];
+  double device_begin_s, device_end_s; /* GPU timestamps (CUDA events, seconds since
+                                          the server started) of the request's first
+                                          V-cycle chunk starting and its last one
+                                          ending; -1 if it never ran               */
 } mgcfd_request_result;
 
 typedef struct mgcfd_server_stats {

@@ -94,6 +94,9 @@ struct Job {
   int oldest_buf = 0;    // status buffer of the oldest chunk in flight
   bool ending = false;   // no more chunks: waiting for the ones in flight
   int status = MGCFD_OK; // failure of the job itself (set-up, CUDA)
+  // GPU timestamps: recorded before the first chunk, and again after every
+  // chunk, so at retirement ev_end holds the end of the last one.
+  cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
 };
 
 // Copied to page-locked memory after every chunk: the solver's status block
@@ -132,6 +135,7 @@ struct mgcfd_server {
   std::vector<cudaEvent_t> events;  // [slot][kDepth]
   std::vector<int> slot_free;
   ChunkStatus* pinned = nullptr;    // [slot][kDepth]
+  cudaEvent_t t0_ev = nullptr;      // GPU time zero of the device timestamps
   Clock::time_point t0;
   mgcfd_server_stats stats{};
 
@@ -189,6 +193,18 @@ void retire(mgcfd_server* S, Job* job) {
     }
     job->solver = nullptr;
   }
+  double dev_begin = -1.0, dev_end = -1.0;
+  if (job->ev_begin && job->ev_end) {  // the stream is idle: every chunk has completed
+    float b = 0.f, e = 0.f;
+    if (cudaEventElapsedTime(&b, S->t0_ev, job->ev_begin) == cudaSuccess &&
+        cudaEventElapsedTime(&e, S->t0_ev, job->ev_end) == cudaSuccess) {
+      dev_begin = 1e-3 * b;
+      dev_end = 1e-3 * e;
+    }
+    cudaGetLastError();
+  }
+  if (job->ev_begin) cudaEventDestroy(job->ev_begin);
+  if (job->ev_end) cudaEventDestroy(job->ev_end);
   const double t = S->now();
   std::lock_guard<std::mutex> lock(S->mu);
   for (Request* r : job->reqs) {
@@ -204,6 +220,8 @@ void retire(mgcfd_server* S, Job* job) {
     res.finish_s = r->t_finish;
     res.rho_rms_first = r->rho_first;
     res.rho_rms_last = r->rho_last;
+    res.device_begin_s = dev_begin;
+    res.device_end_s = dev_end;
     S->done.push_back(res);
     S->stats.completed++;
     if (r->status != MGCFD_OK) S->stats.failed++;
@@ -222,14 +240,22 @@ void retire(mgcfd_server* S, Job* job) {
 // Enqueue the next chunk of V-cycles, then the status copies and their event.
 int enqueue_chunk(mgcfd_server* S, Job* job) {
   const int n = std::min(kChunk, S->opt.max_cycles - job->enqueued);
-  int st = mgcfd_solver_run(job->solver, n);
+  mgcfd_solver* sv = job->solver;
+  const cudaStream_t s = sv->stream;
+  cudaError_t e = cudaSuccess;
+  if (!job->ev_begin) {
+    e = cudaEventCreate(&job->ev_begin);
+    if (e == cudaSuccess) e = cudaEventCreate(&job->ev_end);
+    if (e == cudaSuccess) e = cudaEventRecord(job->ev_begin, s);
+    if (e != cudaSuccess) return mgcfd::set_error(MGCFD_ERR_CUDA, std::string("server: ") + cudaGetErrorString(e));
+  }
+  int st = mgcfd_solver_run(sv, n);
   if (st) return st;
   job->enqueued += n;
   const size_t k = (size_t)job->slot * kDepth + (size_t)job->next_buf;
-  mgcfd_solver* sv = job->solver;
-  const cudaStream_t s = sv->stream;
   ChunkStatus* c = &S->pinned[k];
-  cudaError_t e = cudaMemcpyAsync(&c->st, sv->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);
+  e = cudaEventRecord(job->ev_end, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&c->st, sv->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);
   if (job->cohort) {
     const size_t m = job->reqs.size();
     if (e == cudaSuccess) e = cudaMemcpyAsync(c->seg, sv->seg_stop, sizeof(SegStop) * m, cudaMemcpyDeviceToHost, s);
@@ -513,6 +539,9 @@ extern "C" int mgcfd_server_create(const mgcfd_server_options* opt, mgcfd_server
   S->events.resize((size_t)k * kDepth);
   S->slot_free.assign((size_t)k, 1);
   for (auto& ev : S->events) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  CK(cudaEventCreate(&S->t0_ev));
+  CK(cudaEventRecord(S->t0_ev, nullptr));
+  CK(cudaEventSynchronize(S->t0_ev));
   CK(cudaMallocHost(reinterpret_cast<void**>(&S->pinned), sizeof(ChunkStatus) * (size_t)k * kDepth));
   S->t0 = Clock::now();
   mgcfd_server* raw = S.get();
@@ -593,6 +622,7 @@ extern "C" void mgcfd_server_destroy(mgcfd_server* S) {
   if (S->host_worker.joinable()) S->host_worker.join();
   if (S->progress_worker.joinable()) S->progress_worker.join();
   for (auto ev : S->events) cudaEventDestroy(ev);
+  if (S->t0_ev) cudaEventDestroy(S->t0_ev);
   if (S->pinned) cudaFreeHost(S->pinned);
   delete S;
 }

@@ -54,7 +54,7 @@ class ServerOptions(C.Structure):
 class RequestResult(C.Structure):
     _fields_ = [("id", C.c_int64), ("status", C.c_int32), ("cycles", C.c_int32), ("submit_s", C.c_double),
                 ("admit_s", C.c_double), ("finish_s", C.c_double), ("rho_rms_first", C.c_double),
-                ("rho_rms_last", C.c_double), ("reserved", C.c_int64 * 2)]
+                ("rho_rms_last", C.c_double), ("device_begin_s", C.c_double), ("device_end_s", C.c_double)]
 
 
 class ServerStats(C.Structure):

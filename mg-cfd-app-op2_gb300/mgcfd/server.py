@@ -75,7 +75,8 @@ class Server:
                 keep = self._keep.pop(r.id, None)
                 done.append(({"id": r.id, "status": r.status, "cycles": r.cycles, "submit_s": r.submit_s,
                               "admit_s": r.admit_s, "finish_s": r.finish_s, "rho_rms_first": r.rho_rms_first,
-                              "rho_rms_last": r.rho_rms_last}, keep[3] if keep else None))
+                              "rho_rms_last": r.rho_rms_last, "device_begin_s": r.device_begin_s,
+                              "device_end_s": r.device_end_s}, keep[3] if keep else None))
             if n.value < 256:
                 return done
 

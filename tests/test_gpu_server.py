@@ -123,6 +123,12 @@ def test_later_arrival_overlaps_running_request(meshes):
     srv.close()
     assert res[first]["status"] == res[second]["status"] == 0
     assert res[second]["admit_s"] < res[first]["finish_s"]  # joined while the first was running
+    # and its V-cycles ran on the GPU while the first one's did (CUDA-event
+    # timestamps of both requests' first chunk start and last chunk end)
+    b1, e1 = res[first]["device_begin_s"], res[first]["device_end_s"]
+    b2, e2 = res[second]["device_begin_s"], res[second]["device_end_s"]
+    assert 0 <= b1 < e1 and 0 <= b2 < e2
+    assert b2 < e1 and b1 < e2
 
 
 def test_failing_request_does_not_disturb_others(meshes):
