@@ -7,15 +7,28 @@
 //                 [--mach M] [--aoa DEG] [--precision fp64|mixed]
 //                 [--increment auto|atomic|gather|fused] [--accumulation fp64|pair32]
 //
+// Two ways to run the V-cycle:
+//   * default: the device-resident solver (mgcfd_solver_*: renumbered, fused
+//     kernels, one CUDA graph per V-cycle);
+//   * --per-loop: the reference's main loop itself (euler3d.cpp:413-641) with
+//     every op_par_loop replaced by the mgcfd_op_* entry point that binds it,
+//     on device dats in OP2's layout and the mesh file's numbering -- what an
+//     OP2 application bound to this library runs.  Like the reference it reads
+//     its OP_MIN / OP_INC globals back after each loop that produces one, and
+//     stops where the reference stops (min_dt < 0, NaN/Inf at level 0).
+//
 // Differences from the reference, all forced by running on one GPU:
 //   * -m/-r (partitioner) and -p (PAPI) are accepted and ignored;
-//   * -n selects reverse Cuthill-McKee renumbering instead of Scotch;
+//   * -n selects reverse Cuthill-McKee renumbering instead of Scotch (with
+//     --per-loop it has no effect: the loops' plans order the nodes);
 //   * Mach and angle of attack are run-time options (defaults 1.2 and 0.0,
 //     the values const.h:32-33 fixes at compile time).
+#include <cuda_runtime.h>
 #include <getopt.h>
 #include <sys/time.h>
 #include <unistd.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -36,6 +49,7 @@ struct Config {
   int flow_interval = 0;
   double mach = 1.2, aoa = 0.0;
   int precision = MGCFD_PRECISION_FP64, increment = MGCFD_INCREMENT_AUTO, accumulation = MGCFD_ACCUM_FP64;
+  bool per_loop = false;
 };
 
 std::string trim(const std::string& s) {
@@ -98,6 +112,7 @@ void usage() {
                "--output-variables | --output-fluxes | --output-step-factors\n"
                "--mach=FLOAT (1.2)  --aoa=DEGREES (0.0)  --precision=fp64|mixed\n"
                "--increment=auto|atomic|gather|fused  --accumulation=fp64|pair32\n"
+               "--per-loop   run the reference's loop sequence through the per-loop entry points\n"
                "-m, -r, -p are accepted for compatibility and ignored (one GPU, no PAPI).\n");
 }
 
@@ -126,6 +141,7 @@ bool parse(int argc, char** argv, Config& c) {
       {"precision", required_argument, nullptr, 1003},
       {"increment", required_argument, nullptr, 1004},
       {"accumulation", required_argument, nullptr, 1005},
+      {"per-loop", no_argument, nullptr, 1006},
       {nullptr, 0, nullptr, 0}};
   int o;
   while ((o = getopt_long(argc, argv, "hc:li:d:p:o:g:m:r:vbnI:", opts, nullptr)) != -1) {
@@ -154,6 +170,7 @@ bool parse(int argc, char** argv, Config& c) {
       case 1005:
         c.accumulation = std::strcmp(optarg, "pair32") == 0 ? MGCFD_ACCUM_PAIR32 : MGCFD_ACCUM_FP64;
         break;
+      case 1006: c.per_loop = true; break;
       case 0: break;
       default: std::printf("Unknown command line parameter '%c'\n", o);
     }
@@ -177,38 +194,196 @@ int fail(int st) {
 
 std::string dir_join(const std::string& dir, const std::string& name) { return dir.empty() ? name : dir + "/" + name; }
 
-}  // namespace
+// The run's results in the mesh file's numbering, per level.
+struct Results {
+  std::vector<std::vector<double>> vars, step_factors, fluxes;
+};
 
-int main(int argc, char** argv) {
-  Config c;
-  if (!parse(argc, argv, c)) return 1;
-  if (c.input_file.empty()) {
-    std::printf("ERROR: input_file not set\n");
-    return 1;
+// --per-loop: device dats of one level in OP2 layout ([set size][dim]).
+struct LoopLevel {
+  int32_t n = 0, ne = 0, nb = 0;
+  bool legacy = false;
+  double *coords = nullptr, *ewt = nullptr, *bwt = nullptr, *vol = nullptr, *var = nullptr, *old = nullptr;
+  double *flux = nullptr, *res = nullptr, *sf = nullptr, *dummy = nullptr;
+  int32_t *e2n = nullptr, *b2n = nullptr, *grp = nullptr, *n2mg = nullptr, *scratch = nullptr;
+};
+
+// Every device buffer of a --per-loop run, freed together (the role of
+// OP2's own allocator for dats and maps).
+class DeviceArena {
+ public:
+  ~DeviceArena() {
+    for (void* q : ptrs_) cudaFree(q);
   }
-  std::printf("-----------------------------------------------------\nLoading from HDF5 files ...\n");
-  mgcfd_host_mesh* mesh = nullptr;
-  int st = mgcfd_host_mesh_load(c.input_file.c_str(), c.input_dir.c_str(), c.legacy ? 1 : 0, &mesh);
-  if (st) {
-    std::fprintf(stderr, "Error: %s\n", mgcfd_last_error());
-    return 1;
+  template <class T>
+  bool alloc(T** out, size_t n) {
+    void* q = nullptr;
+    if (cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) return false;
+    ptrs_.push_back(q);
+    *out = static_cast<T*>(q);
+    return true;
   }
-  const int levels = mgcfd_host_mesh_num_levels(mesh);
-  std::vector<mgcfd_level_view> lv((size_t)levels);
-  for (int l = 0; l < levels; l++) {
-    mgcfd_host_mesh_level(mesh, l, &lv[(size_t)l]);
-    std::printf("Loading level %d / %d\n", l + 1, levels);
+  template <class T>
+  bool upload(T** out, const T* src, size_t n) {
+    if (!alloc(out, n)) return false;
+    return n == 0 || cudaMemcpy(*out, src, n * sizeof(T), cudaMemcpyHostToDevice) == cudaSuccess;
   }
-  // Solutions for -v (euler3d.cpp:314-335).
-  std::vector<std::string> solution((size_t)levels);
-  if (c.validate)
-    for (int l = 0; l < levels; l++) {
-      std::string p = dir_join(c.input_dir, "solution.variables.L" + std::to_string(l) + ".cycles=" +
-                                                std::to_string(c.cycles) + ".h5");
-      if (access(p.c_str(), R_OK) != -1) solution[(size_t)l] = p;
-      else std::printf("Cannot find level %d solution file: %s\n", l, p.c_str());
+  template <class T>
+  static bool download(std::vector<double>* out, const T* src, size_t n) {
+    out->resize(n);
+    return cudaMemcpy(out->data(), src, n * sizeof(T), cudaMemcpyDeviceToHost) == cudaSuccess;
+  }
+
+ private:
+  std::vector<void*> ptrs_;
+};
+
+#define OPCALL(call)                    \
+  do {                                  \
+    const int st_ = (call);             \
+    if (st_) return fail(st_);          \
+  } while (0)
+
+// The reference's main loop (euler3d.cpp:413-641), each op_par_loop one
+// mgcfd_op_* call.  Returns 0, or 1 where the reference exits with an error.
+int run_per_loop(const Config& c, const std::vector<mgcfd_level_view>& lv, Results* out) {
+  const int levels = (int)lv.size();
+  DeviceArena arena;
+  std::vector<LoopLevel> L((size_t)levels);
+  // The plans built for these maps go before the maps' memory does, on every
+  // way out (declared after the arena, so destroyed before it).
+  struct PlanRelease {
+    const std::vector<LoopLevel>& L;
+    ~PlanRelease() {
+      for (const auto& d : L) {
+        if (d.e2n) mgcfd_op_plan_release(d.e2n);
+        if (d.n2mg) mgcfd_op_plan_release(d.n2mg);
+      }
     }
+  } release_plans{L};
+  for (int l = 0; l < levels; l++) {
+    const mgcfd_level_view& v = lv[(size_t)l];
+    LoopLevel& d = L[(size_t)l];
+    d.n = v.nnodes; d.ne = v.nedges; d.nb = v.nbnd;
+    d.legacy = v.volumes != nullptr;
+    const size_t n = (size_t)v.nnodes, ne = (size_t)v.nedges, nb = (size_t)v.nbnd;
+    bool ok = arena.upload(&d.coords, v.coords, 3 * n) && arena.upload(&d.e2n, v.edge_to_nodes, 2 * ne) &&
+              arena.upload(&d.b2n, v.bnd_to_node, nb) && arena.upload(&d.grp, v.bnd_group, nb) &&
+              arena.upload(&d.ewt, v.edge_weights, 3 * ne) && arena.upload(&d.bwt, v.bnd_weights, 3 * nb) &&
+              arena.alloc(&d.var, 5 * n) && arena.alloc(&d.old, 5 * n) && arena.alloc(&d.flux, 5 * n) &&
+              arena.alloc(&d.res, 5 * n) && arena.alloc(&d.sf, n) && arena.alloc(&d.scratch, n) &&
+              (d.legacy ? arena.upload(&d.vol, v.volumes, n) : arena.alloc(&d.vol, n)) &&
+              (!v.node_to_mg || arena.upload(&d.n2mg, v.node_to_mg, n)) && (!c.mem_bound || arena.alloc(&d.dummy, 5 * n));
+    if (!ok) {
+      std::printf("Device allocation or upload failed: %s\n", cudaGetErrorString(cudaGetLastError()));
+      return 1;
+    }
+  }
+  double* d_min_dt = nullptr;
+  double* d_rms = nullptr;
+  int32_t* d_bad = nullptr;
+  if (!arena.alloc(&d_min_dt, 1) || !arena.alloc(&d_rms, 1) || !arena.alloc(&d_bad, 1)) return fail(MGCFD_ERR_NOMEM);
+  mgcfd_freestream ff;
+  OPCALL(mgcfd_freestream_init(c.mach, c.aoa, &ff));
 
+  // Initialise variables and geometry (euler3d.cpp:413-441).
+  for (auto& d : L) {
+    OPCALL(mgcfd_op_initialize_variables(d.n, &ff, d.var, nullptr));
+    OPCALL(mgcfd_op_zero(d.n, 5, d.flux, nullptr));
+    if (c.mem_bound) OPCALL(mgcfd_op_zero(d.n, 5, d.dummy, nullptr));
+    if (!d.legacy) {
+      OPCALL(mgcfd_op_zero(d.n, 1, d.vol, nullptr));
+      OPCALL(mgcfd_op_calculate_cell_volumes(d.ne, d.n, d.e2n, d.coords, d.ewt, d.vol, nullptr));
+    }
+  }
+  for (auto& d : L) {
+    OPCALL(mgcfd_op_dampen_ewt(d.ne, d.ewt, nullptr));
+    OPCALL(mgcfd_op_dampen_ewt(d.nb, d.bwt, nullptr));
+  }
+
+  std::printf("-----------------------------------------------------\nCompute beginning\n");
+  const double t0 = wall();
+  int level = 0, i = 0;
+  bool up = true;
+  while (i < c.cycles) {
+    LoopLevel& d = L[(size_t)level];
+    if (level == 0) std::printf("Performing MG cycle %d / %d\n", i + 1, c.cycles);
+    OPCALL(mgcfd_op_copy_double(d.n, d.var, d.old, nullptr));
+    OPCALL(mgcfd_op_calculate_dt(d.n, d.var, d.vol, d.sf, nullptr));
+    OPCALL(mgcfd_op_get_min_dt(d.n, d.sf, d_min_dt, nullptr));
+    double min_dt = 0.0;  // OP_MIN global, read back as OP2 returns it
+    if (cudaMemcpy(&min_dt, d_min_dt, sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) return fail(MGCFD_ERR_CUDA);
+    if (min_dt < 0.0) {
+      std::printf("Fatal error during 'step factor' calculation, min_dt = %.5e\n", min_dt);
+      return 1;
+    }
+    OPCALL(mgcfd_op_compute_step_factor(d.n, d.var, d.vol, d_min_dt, d.sf, nullptr));
+    for (int rk = 0; rk < 3; rk++) {
+      OPCALL(mgcfd_op_compute_flux_edge(d.ne, d.n, d.e2n, d.var, d.ewt, ff.smoothing_coefficient, d.flux, nullptr));
+      OPCALL(mgcfd_op_compute_bnd_node_flux(d.nb, d.n, d.b2n, d.grp, d.bwt, d.var, &ff, d.flux, nullptr));
+      OPCALL(mgcfd_op_time_step(d.n, rk, d.sf, d.flux, d.old, d.var, nullptr));
+      if (c.mem_bound) OPCALL(mgcfd_op_unstructured_stream(d.ne, d.n, d.e2n, d.var, d.ewt, d.dummy, nullptr));
+    }
+    OPCALL(mgcfd_op_residual(d.n, d.old, d.var, d.res, nullptr));
+    if (level == 0) {  // euler3d.cpp:533-548
+      if (cudaMemset(d_rms, 0, sizeof(double)) != cudaSuccess || cudaMemset(d_bad, 0, sizeof(int32_t)) != cudaSuccess)
+        return fail(MGCFD_ERR_CUDA);
+      OPCALL(mgcfd_op_calc_rms(d.n, d.res, d_rms, nullptr));
+      OPCALL(mgcfd_op_count_bad_vals(d.n, d.var, d_bad, nullptr));
+      int32_t bad = 0;
+      if (cudaMemcpy(&bad, d_bad, sizeof(bad), cudaMemcpyDeviceToHost) != cudaSuccess) return fail(MGCFD_ERR_CUDA);
+      if (bad > 0) {
+        std::printf("Bad variable values detected, aborting\n");
+        return 1;
+      }
+      if (c.flow_interval > 0 && ((i + 1) % c.flow_interval) == 0) {  // euler3d.cpp:552-571
+        std::vector<double> v;
+        if (!DeviceArena::download(&v, d.var, 5 * (size_t)d.n)) return fail(MGCFD_ERR_CUDA);
+        const std::string f = c.prefix + "variables.L0.cycle=" + std::to_string(i + 1) + ".h5";
+        OPCALL(mgcfd_h5_write_f64(f.c_str(), "p_variables", v.data(), d.n, 5));
+      }
+    }
+    if (levels <= 1) {
+      i++;
+    } else if (up) {  // euler3d.cpp:579-597
+      level++;
+      LoopLevel& f = L[(size_t)level - 1];
+      LoopLevel& cl = L[(size_t)level];
+      OPCALL(mgcfd_op_up_pre(f.n, cl.n, f.n2mg, cl.var, cl.scratch, nullptr));
+      OPCALL(mgcfd_op_up(f.n, cl.n, f.n2mg, f.var, cl.var, cl.scratch, nullptr));
+      OPCALL(mgcfd_op_up_post(cl.n, cl.var, cl.scratch, nullptr));
+      if (level == levels - 1) up = false;
+    } else {  // euler3d.cpp:598-639 (down_kernel: p_edge_to_mg_nodes is always NULL)
+      level--;
+      LoopLevel& f = L[(size_t)level];
+      LoopLevel& cl = L[(size_t)level + 1];
+      OPCALL(mgcfd_op_down(f.n, cl.n, f.n2mg, f.var, f.res, f.coords, cl.res, cl.coords, nullptr));
+      if (level == 0) {
+        up = true;
+        i++;
+      }
+    }
+  }
+  if (cudaDeviceSynchronize() != cudaSuccess) return fail(MGCFD_ERR_CUDA);
+  std::printf("\nCompute complete\n");
+  std::printf("Max total runtime = %f\n", wall() - t0);
+
+  out->vars.resize((size_t)levels);
+  out->step_factors.resize((size_t)levels);
+  out->fluxes.resize((size_t)levels);
+  for (int l = 0; l < levels; l++) {
+    const LoopLevel& d = L[(size_t)l];
+    if (!DeviceArena::download(&out->vars[(size_t)l], d.var, 5 * (size_t)d.n) ||
+        (c.out_step_factors && !DeviceArena::download(&out->step_factors[(size_t)l], d.sf, (size_t)d.n)) ||
+        (c.out_fluxes && !DeviceArena::download(&out->fluxes[(size_t)l], d.flux, 5 * (size_t)d.n)))
+      return fail(MGCFD_ERR_CUDA);
+  }
+  return 0;
+}
+
+// The default run: the device-resident solver.
+int run_solver(const Config& c, const std::vector<mgcfd_level_view>& lv, Results* out) {
+  const int levels = (int)lv.size();
   mgcfd_solver_options opt;
   mgcfd_solver_default_options(&opt);
   opt.precision = c.precision;
@@ -217,6 +392,7 @@ int main(int argc, char** argv) {
   opt.renumber = c.renumber ? MGCFD_RENUMBER_RCM : MGCFD_RENUMBER_SPATIAL;
   opt.measure_mem_bound = c.mem_bound ? 1 : 0;
   mgcfd_solver* s = nullptr;
+  int st;
   if ((st = mgcfd_solver_create(levels, lv.data(), c.mach, c.aoa, &opt, nullptr, &s))) return fail(st);
 
   std::printf("-----------------------------------------------------\nCompute beginning\n");
@@ -250,18 +426,77 @@ int main(int argc, char** argv) {
   if (st == MGCFD_ERR_NEGATIVE_DT || st == MGCFD_ERR_BAD_VALUES) {
     std::printf("%s\n", mgcfd_last_error());
     mgcfd_solver_destroy(s);
-    mgcfd_host_mesh_destroy(mesh);
     return 1;
   }
   if (st) return fail(st);
   std::printf("\nCompute complete\n");
   std::printf("Max total runtime = %f\n", wall() - t0);
 
-  std::vector<std::vector<double>> vars((size_t)levels);
+  out->vars.resize((size_t)levels);
+  out->step_factors.resize((size_t)levels);
+  out->fluxes.resize((size_t)levels);
   for (int l = 0; l < levels; l++) {
-    vars[(size_t)l].resize((size_t)lv[(size_t)l].nnodes * 5);
-    if ((st = mgcfd_solver_fetch(s, l, MGCFD_Q_VARIABLES, vars[(size_t)l].data()))) return fail(st);
+    const size_t n = (size_t)lv[(size_t)l].nnodes;
+    out->vars[(size_t)l].resize(n * 5);
+    if ((st = mgcfd_solver_fetch(s, l, MGCFD_Q_VARIABLES, out->vars[(size_t)l].data()))) return fail(st);
+    if (c.out_step_factors) {
+      out->step_factors[(size_t)l].resize(n);
+      if ((st = mgcfd_solver_fetch(s, l, MGCFD_Q_STEP_FACTORS, out->step_factors[(size_t)l].data()))) return fail(st);
+    }
+    if (c.out_fluxes) {
+      out->fluxes[(size_t)l].resize(n * 5);
+      if ((st = mgcfd_solver_fetch(s, l, MGCFD_Q_FLUXES, out->fluxes[(size_t)l].data()))) return fail(st);
+    }
   }
+  mgcfd_solver_destroy(s);
+  return 0;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  Config c;
+  if (!parse(argc, argv, c)) return 1;
+  if (c.input_file.empty()) {
+    std::printf("ERROR: input_file not set\n");
+    return 1;
+  }
+  std::printf("-----------------------------------------------------\nLoading from HDF5 files ...\n");
+  mgcfd_host_mesh* mesh = nullptr;
+  int st = mgcfd_host_mesh_load(c.input_file.c_str(), c.input_dir.c_str(), c.legacy ? 1 : 0, &mesh);
+  if (st) {
+    std::fprintf(stderr, "Error: %s\n", mgcfd_last_error());
+    return 1;
+  }
+  const int levels = mgcfd_host_mesh_num_levels(mesh);
+  std::vector<mgcfd_level_view> lv((size_t)levels);
+  for (int l = 0; l < levels; l++) {
+    mgcfd_host_mesh_level(mesh, l, &lv[(size_t)l]);
+    std::printf("Loading level %d / %d\n", l + 1, levels);
+  }
+  // Solutions for -v (euler3d.cpp:314-335).
+  std::vector<std::string> solution((size_t)levels);
+  if (c.validate)
+    for (int l = 0; l < levels; l++) {
+      std::string p = dir_join(c.input_dir, "solution.variables.L" + std::to_string(l) + ".cycles=" +
+                                                std::to_string(c.cycles) + ".h5");
+      if (access(p.c_str(), R_OK) != -1) solution[(size_t)l] = p;
+      else std::printf("Cannot find level %d solution file: %s\n", l, p.c_str());
+    }
+
+  if (c.per_loop && c.precision != MGCFD_PRECISION_FP64) {
+    std::printf("ERROR: --per-loop runs the reference's FP64 loops; --precision mixed needs the solver\n");
+    mgcfd_host_mesh_destroy(mesh);
+    return 1;
+  }
+  if (c.per_loop && c.renumber) std::printf("Note: -n has no effect with --per-loop (the loops' plans order the nodes)\n");
+  Results res;
+  st = c.per_loop ? run_per_loop(c, lv, &res) : run_solver(c, lv, &res);
+  if (st) {
+    mgcfd_host_mesh_destroy(mesh);
+    return 1;
+  }
+  std::vector<std::vector<double>>& vars = res.vars;
 
   if (c.validate) {  // euler3d.cpp:658-718, validation.h:46-115
     std::printf("-----------------------------------------------------\n");
@@ -314,20 +549,16 @@ int main(int argc, char** argv) {
     for (int l = 0; l < levels; l++) {
       const std::string sfx = ".L" + std::to_string(l) + ".cycles=" + std::to_string(c.cycles) + ".h5";
       const int32_t n = lv[(size_t)l].nnodes;
-      if (c.out_step_factors) {
-        std::vector<double> sf((size_t)n);
-        if ((st = mgcfd_solver_fetch(s, l, MGCFD_Q_STEP_FACTORS, sf.data())) ||
-            (st = mgcfd_h5_write_f64((c.prefix + "step_factors" + sfx).c_str(),
-                                     ("p_step_factors_result_L" + std::to_string(l)).c_str(), sf.data(), n, 1)))
-          return fail(st);
-      }
-      if (c.out_fluxes) {
-        std::vector<double> fx((size_t)n * 5);
-        if ((st = mgcfd_solver_fetch(s, l, MGCFD_Q_FLUXES, fx.data())) ||
-            (st = mgcfd_h5_write_f64((c.prefix + "fluxes" + sfx).c_str(),
-                                     ("p_fluxes_result_L" + std::to_string(l)).c_str(), fx.data(), n, 5)))
-          return fail(st);
-      }
+      if (c.out_step_factors &&
+          (st = mgcfd_h5_write_f64((c.prefix + "step_factors" + sfx).c_str(),
+                                   ("p_step_factors_result_L" + std::to_string(l)).c_str(),
+                                   res.step_factors[(size_t)l].data(), n, 1)))
+        return fail(st);
+      if (c.out_fluxes &&
+          (st = mgcfd_h5_write_f64((c.prefix + "fluxes" + sfx).c_str(),
+                                   ("p_fluxes_result_L" + std::to_string(l)).c_str(), res.fluxes[(size_t)l].data(),
+                                   n, 5)))
+        return fail(st);
       if (c.out_variables &&
           (st = mgcfd_h5_write_f64((c.prefix + "variables" + sfx).c_str(),
                                    ("p_variables_result_L" + std::to_string(l)).c_str(), vars[(size_t)l].data(), n, 5)))
@@ -335,7 +566,6 @@ int main(int argc, char** argv) {
     }
   }
   std::printf("-----------------------------------------------------\n");
-  mgcfd_solver_destroy(s);
   mgcfd_host_mesh_destroy(mesh);
   return 0;
 }

@@ -101,12 +101,14 @@ def build_library(force: bool = False, jobs: int | None = None) -> Path:
                 f.result()
     if force or jobs_list or _stale(LIB, objs):
         _run([nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lpthread"])
+    cuda = Path(nvcc).resolve().parent.parent  # the toolkit: the CLI allocates its --per-loop dats itself
     for name, exe in TOOLS.items():
         src = CSRC / name
         if src.exists() and (force or _stale(exe, [src, LIB] + hdrs)):
             exe.parent.mkdir(parents=True, exist_ok=True)
-            _run(["g++", *CXX_FLAGS, str(src), "-o", str(exe), f"-L{LIB.parent}", "-lmgcfd_gb300",
-                  f"-Wl,-rpath,{LIB.parent}", "-Wl,-rpath,$ORIGIN/../lib"])
+            _run(["g++", *CXX_FLAGS, f"-I{cuda / 'include'}", str(src), "-o", str(exe), f"-L{LIB.parent}",
+                  "-lmgcfd_gb300", f"-L{cuda / 'lib64'}", "-lcudart", f"-Wl,-rpath,{LIB.parent}",
+                  "-Wl,-rpath,$ORIGIN/../lib"])
     _write_stamp(OBJ)
     return LIB
 

@@ -109,3 +109,55 @@ def test_mixed_precision_flags(tmp_path, extra):
         mx, l2 = per_variable_errors(b, a)
         assert mx.max() <= MIXED_TOL and l2.max() <= MIXED_TOL
         assert not np.array_equal(a, b)  # the flag took effect
+
+
+@pytest.mark.gpu
+def test_per_loop_run_matches_reference_fixture(tmp_path):
+    """--per-loop runs the reference's loop sequence through the mgcfd_op_*
+    entry points on OP2-layout dats: its solution files match the reference's
+    (golden fixture) and -v accepts them."""
+    z = np.load(GOLDEN / "lattice9_l3_c3.npz")
+    meta = json.loads(str(z["meta"]))
+    mesh = mgcfd.HostMesh.generate(meta["n"], meta["levels"], meta["seed"])
+    mesh.write(str(tmp_path), "m_")
+    args = ["-i", "input.dat", "-d", tmp_path, "-g", meta["cycles"], "--mach", meta["mach"], "--aoa", meta["aoa"],
+            "--per-loop"]
+    r = cli(*args, "--output-variables", "--output-step-factors", "--output-fluxes", "-o", f"{tmp_path}/solution.")
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.count("Performing MG cycle") == meta["cycles"] and "Max total runtime" in r.stdout
+    for l in range(meta["levels"]):
+        got = mgcfd.h5_read(tmp_path / f"solution.variables.L{l}.cycles={meta['cycles']}.h5",
+                            f"p_variables_result_L{l}")
+        assert state_error(got, z[f"variables_L{l}"]) <= STATE_TOL
+        sf = mgcfd.h5_read(tmp_path / f"solution.step_factors.L{l}.cycles={meta['cycles']}.h5",
+                           f"p_step_factors_result_L{l}")
+        np.testing.assert_allclose(sf.reshape(-1), z[f"step_factors_L{l}"], rtol=1e-12)
+        fx = mgcfd.h5_read(tmp_path / f"solution.fluxes.L{l}.cycles={meta['cycles']}.h5", f"p_fluxes_result_L{l}")
+        assert not fx.any()  # time_step_kernel leaves the fluxes at zero (time_stepping_kernels.h:84)
+    r = cli(*args, "-v")
+    assert r.returncode == 0 and "Validation passed" in r.stdout, r.stdout
+
+
+@pytest.mark.gpu
+def test_per_loop_flags_match_the_solver(tmp_path):
+    """-l (legacy datasets), -b (unstructured_stream each stage) and -I
+    (level-0 snapshots) through the per-loop entry points give the device
+    solver's results; --precision mixed is refused with --per-loop."""
+    mesh = mgcfd.HostMesh.generate(8, 2, 21)
+    mesh.write(str(tmp_path), "m_", legacy_datasets=True)
+    base = ["-i", "input.dat", "-d", tmp_path, "-g", 4, "--mach", 0.5, "--aoa", 3.0, "--output-variables"]
+    for extra in ([], ["-l"], ["-b"], ["-I", 2]):
+        outs = []
+        for mode in ([], ["--per-loop"]):
+            pre = f"{tmp_path}/{'p' if mode else 's'}{len(extra)}{''.join(map(str, extra))}."
+            r = cli(*base, "-o", pre, *extra, *mode)
+            assert r.returncode == 0, r.stdout + r.stderr
+            outs.append([mgcfd.h5_read(f"{pre}variables.L{l}.cycles=4.h5", f"p_variables_result_L{l}")
+                         for l in range(2)])
+            if extra == ["-I", 2]:
+                snap = mgcfd.h5_read(f"{pre}variables.L0.cycle=2.h5", "p_variables")
+                outs[-1].append(snap)
+        for a, b in zip(outs[0], outs[1]):
+            assert state_error(b, a) <= STATE_TOL, extra
+    r = cli(*base, "-o", f"{tmp_path}/x.", "--per-loop", "--precision", "mixed")
+    assert r.returncode == 1 and "--per-loop" in r.stdout
