@@ -90,6 +90,11 @@ namespace {
 
 constexpr int kT = 256;
 constexpr int kMaxComponents = 64;  // breadth-first searches before the rest is appended in id order
+// Breadth-first levels at most (each reads its size on the host): a mesh
+// whose graph is a long chain stops there and the rest follows in id order,
+// so the first call never takes more than a fraction of a second per level
+// cap; results do not depend on the order, only locality does.
+constexpr int kMaxBfsLevels = 16384;
 
 int grid(int64_t n, int t = kT) { return (int)((n + t - 1) / t); }
 
@@ -497,7 +502,8 @@ int cm_order(const int32_t* e2n, int32_t ne, int32_t nn, cudaStream_t s, Scratch
   } hf{&ncand_h, &best_h};
   CK(cudaMallocHost(&ncand_h, sizeof(int32_t)));
   CK(cudaMallocHost(&best_h, sizeof(unsigned long long)));
-  for (int comp = 0; comp < kMaxComponents && placed < nn; comp++) {
+  int bfs_levels = 0;
+  for (int comp = 0; comp < kMaxComponents && placed < nn && bfs_levels < kMaxBfsLevels; comp++) {
     k_fill_u64<<<1, 1, 0, s>>>(1, ~0ull, best);
     k_pick_start<<<grid(nn), kT, 0, s>>>(nn, pos, off, best);
     CK(cudaMemcpyAsync(best_h, best, sizeof(*best_h), cudaMemcpyDeviceToHost, s));
@@ -506,7 +512,7 @@ int cm_order(const int32_t* e2n, int32_t ne, int32_t nn, cudaStream_t s, Scratch
     k_place_one<<<1, 1, 0, s>>>(best, placed, pos, order);
     int32_t lb = placed, le = placed + 1;
     placed = le;
-    while (lb < le) {
+    while (lb < le && ++bfs_levels <= kMaxBfsLevels) {
       CK(cudaMemsetAsync(ncand, 0, sizeof(int32_t), s));
       k_expand<<<grid(le - lb), kT, 0, s>>>(lb, le, order, off, adj, pos, parent, cand, ncand);
       CK(cudaMemcpyAsync(ncand_h, ncand, sizeof(int32_t), cudaMemcpyDeviceToHost, s));

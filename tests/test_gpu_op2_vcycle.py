@@ -186,3 +186,23 @@ def test_restriction_plan_is_a_deterministic_gather():
     assert ops.plans_info()["child_plans"] == 1
     ops.plan_release(m.data_ptr())
     assert ops.plans_info()["child_plans"] == 0
+
+
+def test_plan_on_a_chain_longer_than_the_search_cap():
+    """A chain of 20,000 nodes has as many breadth-first levels; the search
+    stops at its cap (16,384 levels) and the rest follows in id order, with
+    the same fluxes."""
+    rng = np.random.default_rng(21)
+    nn = 20000
+    relabel = rng.permutation(nn).astype(np.int32)
+    e = np.ascontiguousarray(relabel[np.stack([np.arange(nn - 1), np.arange(1, nn)], 1)].astype(np.int32))
+    var, w = _flux_case(rng, nn, e)
+    exp, _ = _oracle_flux(e, var, w, 0.2, nn)
+    ops.plans_mode("reorder")
+    d_e, d_v, d_w = (torch.from_numpy(x).cuda() for x in (e, var, w))
+    flux = torch.zeros((nn, 5), dtype=torch.float64, device="cuda")
+    ops.compute_flux_edge(len(e), nn, d_e.data_ptr(), d_v.data_ptr(), d_w.data_ptr(), 0.2, flux.data_ptr())
+    torch.cuda.synchronize()
+    assert state_error(flux.cpu().numpy(), exp) <= STATE_TOL
+    assert ops.plans_info()["reordered"] == 1
+    ops.plan_release(d_e.data_ptr())
