@@ -857,7 +857,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
-    ap.add_argument("--increment", default="auto", choices=["auto", "atomic", "gather", "fused"],
+    ap.add_argument("--increment", default="auto", choices=["auto", "atomic", "gather", "fused", "coloured"],
                     help="auto: FP64 atomics for fp64, the fused node-centric stage for mixed")
     ap.add_argument("--renumber", default="spatial", choices=["none", "spatial", "rcm"])
     ap.add_argument("--accumulation", default="fp64", choices=["fp64", "pair32"],

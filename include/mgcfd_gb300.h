@@ -275,7 +275,19 @@ enum { MGCFD_PRECISION_FP64 = 0, MGCFD_PRECISION_MIXED = 1 };
  * edge at both of its end nodes from the same inputs in the same order, sums
  * them exactly as GATHER does and applies the time step -- GATHER's results
  * bit for bit, with no per-edge flux array and one launch per stage. */
-enum { MGCFD_INCREMENT_AUTO = 0, MGCFD_INCREMENT_ATOMIC = 1, MGCFD_INCREMENT_GATHER = 2, MGCFD_INCREMENT_FUSED = 3 };
+/* COLOURED (FP64, single-mesh solvers): each level's edges are split at set-up
+ * into colour classes in which no two edges share a node (greedy, at most 64
+ * classes); each class is one launch whose edges add +f / -f to their end
+ * nodes with plain loads and stores -- no atomics, and the same sums in the
+ * same order on every run.  Measured slower than ATOMIC on GB300 (each class
+ * streams the node records and flux rows again), so AUTO does not pick it. */
+enum {
+  MGCFD_INCREMENT_AUTO = 0,
+  MGCFD_INCREMENT_ATOMIC = 1,
+  MGCFD_INCREMENT_GATHER = 2,
+  MGCFD_INCREMENT_FUSED = 3,
+  MGCFD_INCREMENT_COLOURED = 4
+};
 enum { MGCFD_RENUMBER_NONE = 0, MGCFD_RENUMBER_SPATIAL = 1, MGCFD_RENUMBER_RCM = 2 };
 /* Node-residual accumulation in mixed precision.  FP64: every FP32 edge flux
  * is widened exactly and added in FP64.  PAIR32: the fluxes enter an

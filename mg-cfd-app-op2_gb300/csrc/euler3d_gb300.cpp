@@ -5,7 +5,7 @@
 //                 [-I interval] [-n] [-c config] [--output-variables]
 //                 [--output-fluxes] [--output-step-factors]
 //                 [--mach M] [--aoa DEG] [--precision fp64|mixed]
-//                 [--increment auto|atomic|gather|fused] [--accumulation fp64|pair32]
+//                 [--increment auto|atomic|gather|fused|coloured] [--accumulation fp64|pair32]
 //
 // Two ways to run the V-cycle:
 //   * default: the device-resident solver (mgcfd_solver_*: renumbered, fused
@@ -111,7 +111,7 @@ void usage() {
                "-I, --output-flow-interval=INT   cycles between writes of the level-0 flow\n"
                "--output-variables | --output-fluxes | --output-step-factors\n"
                "--mach=FLOAT (1.2)  --aoa=DEGREES (0.0)  --precision=fp64|mixed\n"
-               "--increment=auto|atomic|gather|fused  --accumulation=fp64|pair32\n"
+               "--increment=auto|atomic|gather|fused|coloured  --accumulation=fp64|pair32\n"
                "--per-loop   run the reference's loop sequence through the per-loop entry points\n"
                "-m, -r, -p are accepted for compatibility and ignored (one GPU, no PAPI).\n");
 }
@@ -165,6 +165,7 @@ bool parse(int argc, char** argv, Config& c) {
         c.increment = std::strcmp(optarg, "gather") == 0   ? MGCFD_INCREMENT_GATHER
                       : std::strcmp(optarg, "atomic") == 0 ? MGCFD_INCREMENT_ATOMIC
                       : std::strcmp(optarg, "fused") == 0  ? MGCFD_INCREMENT_FUSED
+                      : std::strcmp(optarg, "coloured") == 0 ? MGCFD_INCREMENT_COLOURED
                                                            : MGCFD_INCREMENT_AUTO;
         break;
       case 1005:

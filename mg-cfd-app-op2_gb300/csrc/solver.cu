@@ -291,6 +291,39 @@ __global__ void k_flux_f64(int32_t ne, const int2* __restrict__ e2n, const doubl
   }
 }
 
+// compute_flux_edge_kernel over one colour class: no two of these edges share
+// a node, so each adds +f / -f to its end nodes with plain loads and stores.
+// (A loop edge a == b is one thread's two updates of one row, in order.)
+__global__ void k_flux_f64_coloured(int32_t ne, const int2* __restrict__ e2n, const double4_32a* __restrict__ w4,
+                                    const double* __restrict__ rec, double* flux, const DevStatus* __restrict__ st) {
+  if (st->halt) return;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  const int2 ab = e2n[e];
+  const double4_32a w = w4[e];
+  const NodePrim a = load_rec(rec, ab.x);
+  const NodePrim b = load_rec(rec, ab.y);
+  double f[5];
+  edge_flux(a, b, w.x, w.y, w.z, w.w, f);
+  double* fa = flux + 5 * (int64_t)ab.x;
+#pragma unroll
+  for (int k = 0; k < 5; k++) fa[k] += f[k];
+  double* fb = flux + 5 * (int64_t)ab.y;
+#pragma unroll
+  for (int k = 0; k < 5; k++) fb[k] += negate(f[k]);
+}
+
+// Edges of a level into colour order (idx[k] = old position of edge k).
+__global__ void k_gather_edges(int32_t ne, const int32_t* __restrict__ idx, const int2* __restrict__ e2n_in,
+                               const double4_32a* __restrict__ w4_in, int2* __restrict__ e2n_out,
+                               double4_32a* __restrict__ w4_out) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= ne) return;
+  const int32_t e = idx[k];
+  e2n_out[k] = e2n_in[e];
+  w4_out[k] = w4_in[e];
+}
+
 // Mixed precision edge flux: FP32 arithmetic, FP64 accumulation.  The
 // gather strategy stores the FP32 fluxes (widened exactly, on the integer
 // pipe, where the node sums them in FP64); the atomic strategy widens them
@@ -1018,7 +1051,18 @@ int enqueue_smooth(mgcfd_solver* s, int level) {
       }
       CK(cudaEventRecord(ev.first, s->stream));
     }
-    if (D.ne > 0 && !s->fused) {
+    if (D.ne > 0 && s->coloured) {
+      for (size_t c = 0; c + 1 < D.colour_off.size(); c++) {
+        const int32_t lo = D.colour_off[c], cnt = D.colour_off[c + 1] - lo;
+        if (cnt == 0) continue;
+        k_flux_f64_coloured<<<grid(cnt, et), et, 0, s->stream>>>(cnt, D.e2n + lo, D.w4 + lo, D.rec, D.flux, s->st);
+        s->launches++;
+      }
+      if (time_this) {
+        CK(cudaEventRecord(ev.second, s->stream));
+        s->pending.push_back(ev);
+      }
+    } else if (D.ne > 0 && !s->fused) {
       const int g = grid(D.ne, et);
       if (mixed) {
         if (s->gather) k_flux_mixed<true><<<g, et, 0, s->stream>>>(D.ne, D.e2n, D.w4f, D.rec32, D.flux, D.fe32, s->st);
@@ -1215,15 +1259,65 @@ void free_solver(mgcfd_solver* s) {
 }  // namespace
 
 namespace {
+// COLOURED increment: greedy edge colouring of one level on the host (each
+// edge takes the smallest colour that neither end node has used yet, in the
+// level's sorted edge order), then the level's edges and weights reordered on
+// the device into colour classes.  At most 64 classes (a node with more edges
+// than that fails the set-up with MGCFD_ERR_INVALID); a lattice needs 7.
+int colour_edges(mgcfd_solver* s, DevLevel& D) {
+  D.colour_off.assign(1, 0);
+  if (D.ne == 0) return MGCFD_OK;
+  std::vector<int2> e2n((size_t)D.ne);
+  CK(cudaMemcpyAsync(e2n.data(), D.e2n, sizeof(int2) * e2n.size(), cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  std::vector<uint64_t> used((size_t)D.n, 0);
+  std::vector<uint8_t> col((size_t)D.ne);
+  int ncol = 0;
+  for (size_t e = 0; e < e2n.size(); e++) {
+    const uint64_t free_mask = ~(used[(size_t)e2n[e].x] | used[(size_t)e2n[e].y]);
+    if (!free_mask) return set_error(MGCFD_ERR_INVALID, "coloured increment: a node has more than 64 edges");
+    const int c = __builtin_ctzll(free_mask);
+    col[e] = (uint8_t)c;
+    used[(size_t)e2n[e].x] |= 1ull << c;
+    used[(size_t)e2n[e].y] |= 1ull << c;
+    ncol = std::max(ncol, c + 1);
+  }
+  std::vector<int32_t> off((size_t)ncol + 1, 0), idx((size_t)D.ne);
+  for (uint8_t c : col) off[(size_t)c + 1]++;
+  for (int c = 0; c < ncol; c++) off[(size_t)c + 1] += off[(size_t)c];
+  std::vector<int32_t> fill(off.begin(), off.end() - 1);
+  for (size_t e = 0; e < col.size(); e++) idx[(size_t)fill[col[e]]++] = (int32_t)e;  // stable within a colour
+  int32_t* d_idx = nullptr;
+  int2* e2n_tmp = nullptr;
+  double4_32a* w4_tmp = nullptr;
+  CK(cudaMallocAsync(reinterpret_cast<void**>(&d_idx), sizeof(int32_t) * idx.size(), s->stream));
+  CK(cudaMallocAsync(reinterpret_cast<void**>(&e2n_tmp), sizeof(int2) * idx.size(), s->stream));
+  CK(cudaMallocAsync(reinterpret_cast<void**>(&w4_tmp), sizeof(double4_32a) * idx.size(), s->stream));
+  CK(cudaMemcpyAsync(d_idx, idx.data(), sizeof(int32_t) * idx.size(), cudaMemcpyHostToDevice, s->stream));
+  k_gather_edges<<<grid(D.ne, 256), 256, 0, s->stream>>>(D.ne, d_idx, D.e2n, D.w4, e2n_tmp, w4_tmp);
+  CK(cudaMemcpyAsync(D.e2n, e2n_tmp, sizeof(int2) * idx.size(), cudaMemcpyDeviceToDevice, s->stream));
+  CK(cudaMemcpyAsync(D.w4, w4_tmp, sizeof(double4_32a) * idx.size(), cudaMemcpyDeviceToDevice, s->stream));
+  CK(cudaFreeAsync(d_idx, s->stream));
+  CK(cudaFreeAsync(e2n_tmp, s->stream));
+  CK(cudaFreeAsync(w4_tmp, s->stream));
+  CK(cudaStreamSynchronize(s->stream));  // idx's host buffer
+  CK(cudaGetLastError());
+  D.colour_off = off;
+  return MGCFD_OK;
+}
+
 // Increment strategy: AUTO is FP64 atomics for FP64 and the fused
 // node-centric stage for mixed precision (the fastest of each, measured).
 int resolve_increment(mgcfd_solver* s) {
   const int inc = s->opt.increment;
   const bool mixed = s->opt.precision == MGCFD_PRECISION_MIXED;
-  if (inc < MGCFD_INCREMENT_AUTO || inc > MGCFD_INCREMENT_FUSED)
+  if (inc < MGCFD_INCREMENT_AUTO || inc > MGCFD_INCREMENT_COLOURED)
     return set_error(MGCFD_ERR_INVALID, "unknown increment strategy");
   if (inc == MGCFD_INCREMENT_FUSED && !mixed)
     return set_error(MGCFD_ERR_INVALID, "the fused increment needs mixed precision");
+  if (inc == MGCFD_INCREMENT_COLOURED && mixed)
+    return set_error(MGCFD_ERR_INVALID, "the coloured increment is an FP64 strategy");
+  s->coloured = inc == MGCFD_INCREMENT_COLOURED;
   s->fused = inc == MGCFD_INCREMENT_FUSED || (inc == MGCFD_INCREMENT_AUTO && mixed);
   s->gather = s->fused || inc == MGCFD_INCREMENT_GATHER;
   s->fused_variant = !s->fused ? 0 : s->opt.edge_parallel_stage ? 2 : s->opt.stage_neighbour_ids ? 1 : 0;
@@ -1333,6 +1427,8 @@ extern "C" int mgcfd_solver_create(int32_t nlevels, const mgcfd_level_view* leve
     // The host vectors of this level die at the end of create: finish the copies first.
     CK(cudaStreamSynchronize(s->stream));
   }
+  for (auto& D : s->L)
+    if (s->coloured && (r = colour_edges(s.get(), D))) return r;
   if ((r = s->alloc(&s->st, 1)) || (r = s->alloc(&s->fetch_buf, 5 * max_n))) return r;
   if ((r = init_state(s.get()))) return r;
   CK(cudaStreamSynchronize(s->stream));
@@ -1360,6 +1456,7 @@ extern "C" int mgcfd_batch_create(int32_t nmeshes, int32_t nlevels, const mgcfd_
   if (s->opt.renumber == MGCFD_RENUMBER_RCM || s->opt.host_setup)
     return set_error(MGCFD_ERR_INVALID, "batched solvers are set up on the device (renumber none or spatial)");
   if ((r0 = resolve_increment(s.get()))) return r0;
+  if (s->coloured) return set_error(MGCFD_ERR_INVALID, "the coloured increment is for single-mesh solvers");
   s->stream = static_cast<cudaStream_t>(stream);
   CK(cudaGetDevice(&s->device));
   if (!s->stream) {

@@ -82,6 +82,7 @@ struct DevLevel {
   int32_t* ch_list = nullptr;
   int32_t* perm = nullptr;
   int32_t* mesh_id = nullptr;  // [n] mesh of each node (batched solvers only)
+  std::vector<int32_t> colour_off;  // COLOURED: edges [colour_off[c], colour_off[c+1]) share no node
 };
 
 struct mgcfd_solver {
@@ -117,6 +118,7 @@ struct mgcfd_solver {
   int64_t launches_per_cycle = 0;
   bool gather = false;  // node-side CSR tables exist (GATHER or FUSED)
   bool fused = false;   // FUSED: flux and update in one node-centric kernel
+  bool coloured = false;  // COLOURED: one flux launch per colour class, plain increments
   int fused_variant = 0;  // FUSED: 0 per-node edge loop, 1 neighbour ids staged by cp.async, 2 edge-parallel
   cudaGraphExec_t graph = nullptr;
   // Kernel timing.

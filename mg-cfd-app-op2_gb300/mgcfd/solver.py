@@ -9,7 +9,7 @@ from . import _lib
 from .mesh import HostMesh, level_views_from_arrays
 
 PRECISION = {"fp64": 0, "mixed": 1}
-INCREMENT = {"auto": 0, "atomic": 1, "gather": 2, "fused": 3}
+INCREMENT = {"auto": 0, "atomic": 1, "gather": 2, "fused": 3, "coloured": 4}
 RENUMBER = {"none": 0, "spatial": 1, "rcm": 2}
 ACCUMULATION = {"fp64": 0, "pair32": 1}
 Q_VARIABLES, Q_FLUXES, Q_STEP_FACTORS, Q_VOLUMES, Q_RESIDUALS, Q_OLD_VARIABLES = range(6)

@@ -170,6 +170,51 @@ def test_fused_stage_variants_give_the_same_bits(mesh_kind, accumulation, varian
         b.close()
 
 
+@pytest.mark.parametrize("host_setup", [False, True])
+@pytest.mark.parametrize("kind", ["lattice", "irregular", "dense"])
+def test_coloured_increment_matches_oracle_and_repeats_bitwise(kind, host_setup):
+    """The coloured FP64 increment (one launch per colour class, plain
+    increments): within the FP64 bar of the oracle on every level, and the
+    same bits on a second run (no atomics, a fixed order per node)."""
+    from irregular import irregular_levels
+    levels = {"lattice": lambda: mgcfd.HostMesh.generate(14, 3, 61).levels(),
+              "irregular": lambda: irregular_levels(1500, 3, 9),
+              "dense": lambda: _dense_levels(per_node=8)}[kind]()
+    mach, aoa, cycles = 0.7, 2.0, 3
+    runs = []
+    for _ in range(2):
+        s = mgcfd.Solver(levels, mach, aoa, increment="coloured", host_setup=host_setup)
+        s.run(cycles)
+        assert s.synchronize() == 0
+        runs.append([s.fetch(l) for l in range(len(levels))])
+        s.close()
+    ref = _oracle(levels, mach, aoa, cycles)
+    x0 = _ff(mach, aoa)
+    for l in range(len(levels)):
+        np.testing.assert_array_equal(runs[0][l], runs[1][l])
+        r = ref.get(l, O.Q_VARIABLES)
+        assert state_error(runs[0][l], r) <= STATE_TOL, (l, state_error(runs[0][l], r))
+        assert delta_error(runs[0][l], r, x0) <= DELTA_TOL
+
+
+def test_coloured_increment_is_fp64_and_single_mesh():
+    mesh = mgcfd.HostMesh.generate(6, 2, 1)
+    with pytest.raises(mgcfd._lib.MgcfdError):
+        mgcfd.Solver(mesh, 0.5, 0.0, precision="mixed", increment="coloured")
+    with pytest.raises(mgcfd._lib.MgcfdError):
+        mgcfd.Batch([mesh, mesh], [0.5, 0.6], [0.0, 1.0], increment="coloured")
+    # A node with 70 edges needs more colour classes than the 64 the set-up keeps.
+    star = _dense_levels(n=200, per_node=1)[0]
+    e = np.concatenate([star.edge_to_nodes, np.stack([np.zeros(70), np.arange(1, 71)], 1).astype(np.int32)])
+    star.edge_to_nodes = np.ascontiguousarray(e.astype(np.int32))
+    d = star.coords[e[:, 1]] - star.coords[e[:, 0]]
+    star.edge_weights = np.ascontiguousarray(1e-3 * d / np.linalg.norm(d, axis=1, keepdims=True))
+    with pytest.raises(mgcfd._lib.MgcfdError, match="64"):
+        mgcfd.Solver([star], 0.5, 0.0, increment="coloured")
+    s = mgcfd.Solver([star], 0.5, 0.0, increment="atomic")  # the same mesh is fine otherwise
+    s.close()
+
+
 def test_fused_needs_mixed_precision():
     mesh = mgcfd.HostMesh.generate(6, 1, 1)
     with pytest.raises(mgcfd._lib.MgcfdError):
