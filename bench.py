@@ -54,7 +54,17 @@ def algorithmic_flux_bytes(nnodes: int, nedges: int, precision: str = "fp64", in
     Mixed, fused stage (flux and time step in one node kernel): per edge the
     a-side weights + map (24 B) and the b-side copies (20 B); per node the
     FP32 primitives read (32 B), old state (40 B), 1/vol, boundary index and
-    CSR offsets (20 B), state written (40 B) and next primitives written (32 B)."""
+    CSR offsets (20 B), state written (40 B) and next primitives written (32 B).
+    DW (double-word flux): 32 B weights as pair words + 8 B map per edge; 64 B
+    primitives as pair words read, 40 B flux read and 40 B written per node.
+    DW, fused stage: per edge both ends' table entries (neighbour id and
+    weight pair words, 2 x 36 B); per node the primitives read (64 B), old
+    state (40 B), 1/vol, boundary index and table offset (16 B), state written
+    (40 B) and next primitives written (64 B)."""
+    if precision == "dw" and increment == "fused":
+        return 72 * nedges + 224 * nnodes
+    if precision == "dw":
+        return 40 * nedges + 144 * nnodes
     if precision == "mixed" and increment == "fused":
         return 44 * nedges + 164 * nnodes
     if precision == "mixed":
@@ -300,7 +310,7 @@ def run_gb300(args):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64" if args.precision == "fp64" else "f32-flux/f64-accumulate",
+        "dtype": {"fp64": "f64", "mixed": "f32-flux/f64-accumulate", "dw": "f32x2-flux/f64"}[args.precision],
         "data": "synthetic: seeded jittered 200^3 lattice, permuted ids",
         "config": line_config(args, N, E),
         "variant": {"increment": inc, "renumber": args.renumber,
@@ -856,7 +866,7 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "dw"])
     ap.add_argument("--increment", default="auto", choices=["auto", "atomic", "gather", "fused", "coloured"],
                     help="auto: FP64 atomics for fp64, the fused node-centric stage for mixed")
     ap.add_argument("--renumber", default="spatial", choices=["none", "spatial", "rcm"])

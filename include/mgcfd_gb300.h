@@ -267,7 +267,16 @@ int mgcfd_op_count_differences(int32_t nnodes, const double* test, const double*
 
 /* ------------------------------------------------------------------------ */
 /* Device-resident multigrid solver.                                        */
-enum { MGCFD_PRECISION_FP64 = 0, MGCFD_PRECISION_MIXED = 1 };
+/* FP64: every operation in binary64.  MIXED: FP32 edge-flux arithmetic and
+ * geometry, FP64 node sums, time step and norms.  DW: the state, node sums,
+ * time step, norms and node primitives computed in binary64 as for FP64; the
+ * edge flux evaluated on the FP32 pipes in double-word arithmetic (each input
+ * held as an unevaluated pair of binary32 numbers, 48 significand bits,
+ * error-free TwoSum / TwoProd steps), with its inputs -- the primitives and
+ * the edge weights -- stored as such pairs.  Within the same 1e-10 relative
+ * bar of the FP64 reference as FP64; the exponent range of the flux inputs is
+ * binary32's.  DW takes the ATOMIC (AUTO) or GATHER increment. */
+enum { MGCFD_PRECISION_FP64 = 0, MGCFD_PRECISION_MIXED = 1, MGCFD_PRECISION_DW = 2 };
 /* How the edge fluxes reach the nodes.  ATOMIC: each edge adds +f / -f to its
  * end nodes with FP64 atomics.  GATHER: each edge stores f, then each node
  * sums its edges' f in a fixed order (deterministic).  FUSED (mixed precision

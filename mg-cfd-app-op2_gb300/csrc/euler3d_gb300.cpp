@@ -4,7 +4,7 @@
 //   euler3d_gb300 -i input.dat [-d dir] [-g cycles] [-o prefix] [-v] [-l] [-b]
 //                 [-I interval] [-n] [-c config] [--output-variables]
 //                 [--output-fluxes] [--output-step-factors]
-//                 [--mach M] [--aoa DEG] [--precision fp64|mixed]
+//                 [--mach M] [--aoa DEG] [--precision fp64|mixed|dw]
 //                 [--increment auto|atomic|gather|fused|coloured] [--accumulation fp64|pair32]
 //
 // Two ways to run the V-cycle:
@@ -110,7 +110,7 @@ void usage() {
                "-v, --validate-result            check final state against pre-calculated solution\n"
                "-I, --output-flow-interval=INT   cycles between writes of the level-0 flow\n"
                "--output-variables | --output-fluxes | --output-step-factors\n"
-               "--mach=FLOAT (1.2)  --aoa=DEGREES (0.0)  --precision=fp64|mixed\n"
+               "--mach=FLOAT (1.2)  --aoa=DEGREES (0.0)  --precision=fp64|mixed|dw\n"
                "--increment=auto|atomic|gather|fused|coloured  --accumulation=fp64|pair32\n"
                "--per-loop   run the reference's loop sequence through the per-loop entry points\n"
                "-m, -r, -p are accepted for compatibility and ignored (one GPU, no PAPI).\n");
@@ -160,7 +160,11 @@ bool parse(int argc, char** argv, Config& c) {
       case 'm': case 'r': case 'p': break;
       case 1001: c.mach = std::atof(optarg); break;
       case 1002: c.aoa = std::atof(optarg); break;
-      case 1003: c.precision = std::strcmp(optarg, "mixed") == 0 ? MGCFD_PRECISION_MIXED : MGCFD_PRECISION_FP64; break;
+      case 1003:
+        c.precision = std::strcmp(optarg, "mixed") == 0 ? MGCFD_PRECISION_MIXED
+                      : std::strcmp(optarg, "dw") == 0  ? MGCFD_PRECISION_DW
+                                                        : MGCFD_PRECISION_FP64;
+        break;
       case 1004:
         c.increment = std::strcmp(optarg, "gather") == 0   ? MGCFD_INCREMENT_GATHER
                       : std::strcmp(optarg, "atomic") == 0 ? MGCFD_INCREMENT_ATOMIC
@@ -486,7 +490,7 @@ int main(int argc, char** argv) {
     }
 
   if (c.per_loop && c.precision != MGCFD_PRECISION_FP64) {
-    std::printf("ERROR: --per-loop runs the reference's FP64 loops; --precision mixed needs the solver\n");
+    std::printf("ERROR: --per-loop runs the reference's FP64 loops; --precision mixed or dw needs the solver\n");
     mgcfd_host_mesh_destroy(mesh);
     return 1;
   }

@@ -161,6 +161,10 @@ int64_t estimate_bytes(const std::vector<mgcfd_level_view>& lv, int precision, i
     int64_t node = 8 * 8 + 5 * 8 * 3 + 8 * 3 + 4 * 4 + 32;   // rec, old/res/flux, vol constants, maps, dvec
     int64_t edge = 8 + 32;                                    // e2n, w4
     if (mixed) { node += fused ? 64 : 32; edge += 16; }
+    if (precision == MGCFD_PRECISION_DW) {  // rec2, w4dw; fused: rec2b, off2, nb2, w2
+      node += 64 + (increment == MGCFD_INCREMENT_FUSED ? 68 : 0);
+      edge += 32 + (increment == MGCFD_INCREMENT_FUSED ? 72 : 0);
+    }
     if (fused) edge += 4 + 4 + 16;                 // b_list, b_nbr, b_w4f
     else if (gather) edge += (mixed ? 20 : 40) + 4;  // per-edge fluxes, b_list
     b += n * node + e * edge + nb * 96;
@@ -531,7 +535,7 @@ extern "C" int mgcfd_server_create(const mgcfd_server_options* opt, mgcfd_server
   if (!S) return mgcfd::set_error(MGCFD_ERR_NOMEM, "host allocation failed");
   if (opt) S->opt = *opt; else mgcfd_server_default_options(&S->opt);
   if (S->opt.max_active < 1 || S->opt.max_active > 1024 || S->opt.max_cycles < 1 || S->opt.hbm_budget_bytes <= 0 ||
-      (S->opt.precision != MGCFD_PRECISION_FP64 && S->opt.precision != MGCFD_PRECISION_MIXED) ||
+      S->opt.precision < MGCFD_PRECISION_FP64 || S->opt.precision > MGCFD_PRECISION_DW ||
       S->opt.batch_max_meshes < 0 || S->opt.batch_max_meshes > kMaxCohort || S->opt.batch_max_nodes < 0)
     return mgcfd::set_error(MGCFD_ERR_INVALID, "mgcfd_server_create: bad options");
   CK(cudaGetDevice(&S->device));

@@ -49,6 +49,7 @@
 
 #include "common.h"
 #include "device_math.cuh"
+#include "dw_math.cuh"
 #include "setup.h"
 #include "solver_internal.h"
 
@@ -178,8 +179,11 @@ __global__ void k_init_state(int32_t n, double* __restrict__ rec, double v0, dou
 // one shared slot and one global atomic.
 
 // copy_double_kernel + calculate_dt_kernel + get_min_dt_kernel (block part).
-template <bool MIXED, bool SEG>
+// DW: the primitives go to rec2 as pairs (the edge flux's inputs); rec keeps
+// the state only.
+template <bool MIXED, bool SEG, bool DW = false>
 __global__ void __launch_bounds__(kNodeThreads) k_step_begin(int32_t n, double* __restrict__ rec,
+                                                             double* __restrict__ rec2,
                                                              float* __restrict__ rec32, double* __restrict__ old,
                                                              const double* __restrict__ cbrt_vol,
                                                              unsigned long long* __restrict__ dt_key,
@@ -214,10 +218,16 @@ __global__ void __launch_bounds__(kNodeThreads) k_step_begin(int32_t n, double* 
       const NodePrimF q = store_rec32_from_var(rec32, i, x.x, x.y, x.z, x.w, e);
       key = dt_candidate_key(f2d_bits(0.5f * (d2f_bits(cbrt_vol[i]) / q.s)));  // time_stepping_kernels.h:31
     } else {
-      const NodePrim p = node_prim(x.x, x.y, x.z, x.w, e);
-      store_rec(rec, i, p);
+      if (DW) {  // the primitives in double-word arithmetic, no FP64 instruction
+        const NodePrimDW q = node_prim_dw(x.x, x.y, x.z, x.w, e);
+        store_prim_dw(rec2, i, q);
+        sp = dw_to_double(q.s);
+      } else {
+        const NodePrim p = node_prim(x.x, x.y, x.z, x.w, e);
+        store_rec(rec, i, p);
+        sp = p.s;
+      }
       cv = cbrt_vol[i];
-      sp = p.s;
       if (SEG) key = dt_candidate_key(0.5 * (cv / sp));  // time_stepping_kernels.h:31
       else est = 0.5f * __fdividef(d2f_bits(cv), d2f_bits(sp));
     }
@@ -289,6 +299,82 @@ __global__ void k_flux_f64(int32_t ne, const int2* __restrict__ e2n, const doubl
       atomicAdd(fb + k, negate(f[k]));
     }
   }
+}
+
+// compute_flux_edge_kernel (flux.h:41-208) in double-word arithmetic on the
+// FP32 pipes (dw_math.cuh): the primitives and weights as pairs, the
+// increments in binary64, by FP64 atomics or stored per edge as k_flux_f64.
+template <bool GATHER>
+__global__ void k_flux_dw(int32_t ne, const int2* __restrict__ e2n, const double4_32a* __restrict__ w2,
+                          const double* __restrict__ rec2, double* __restrict__ flux, double* __restrict__ fe,
+                          const DevStatus* __restrict__ st) {
+  if (st->halt) return;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  const int2 ab = e2n[e];
+  const double4_32a w = w2[e];
+  const NodePrimDW a = load_prim_dw(rec2, ab.x);
+  const NodePrimDW b = load_prim_dw(rec2, ab.y);
+  double f[5];
+  edge_flux_dw(a, b, dw_unpack(w.x), dw_unpack(w.y), dw_unpack(w.z), dw_unpack(w.w), f);
+  if (GATHER) {
+    double* o = fe + 5 * e;
+#pragma unroll
+    for (int k = 0; k < 5; k++) o[k] = f[k];
+  } else {
+    double* fa = flux + 5 * (int64_t)ab.x;
+    double* fb = flux + 5 * (int64_t)ab.y;
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+      atomicAdd(fa + k, f[k]);
+      atomicAdd(fb + k, negate(f[k]));
+    }
+  }
+}
+
+// The per-node neighbour table of the fused DW stage: node i's entries start
+// at a_off[i] + b_off[i] (its a-side edges, then its b-side edges).
+__global__ void k_dw_offsets(int32_t n, const int32_t* __restrict__ a_off, const int32_t* __restrict__ b_off,
+                             int32_t* __restrict__ off2) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i <= n) off2[i] = a_off[i] + b_off[i];
+}
+
+__global__ void k_dw_table_a(int32_t ne, const int2* __restrict__ e2n, const double4_32a* __restrict__ w4dw,
+                             const int32_t* __restrict__ a_off, const int32_t* __restrict__ off2,
+                             int32_t* __restrict__ nb2, double4_32a* __restrict__ w2) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  const int2 ab = e2n[e];
+  const int64_t k = off2[ab.x] + (e - a_off[ab.x]);
+  nb2[k] = ab.y;
+  w2[k] = w4dw[e];
+}
+
+// b side: the edge seen from its end b, with h = -w/2 negated (both words'
+// sign bits), so the stage evaluates it with its own node as end a.
+__global__ void k_dw_table_b(int32_t ne, const int2* __restrict__ e2n, const double4_32a* __restrict__ w4dw,
+                             const int32_t* __restrict__ b_list, const int32_t* __restrict__ a_off,
+                             const int32_t* __restrict__ b_off, const int32_t* __restrict__ off2,
+                             int32_t* __restrict__ nb2, double4_32a* __restrict__ w2) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= ne) return;
+  const int32_t e = b_list[j];
+  const int2 ab = e2n[e];
+  const int32_t b = ab.y;
+  const int64_t k = off2[b] + (a_off[b + 1] - a_off[b]) + (j - b_off[b]);
+  const double4_32a w = w4dw[e];
+  const long long flip = (long long)0x8000000080000000ull;
+  nb2[k] = ab.x;
+  w2[k] = make_double4_32a(__longlong_as_double(__double_as_longlong(w.x) ^ flip),
+                           __longlong_as_double(__double_as_longlong(w.y) ^ flip),
+                           __longlong_as_double(__double_as_longlong(w.z) ^ flip), w.w);
+}
+
+// The edge weights as pair words (DW precision), once at set-up.
+__global__ void k_split_weights(int64_t n, const double* __restrict__ w, double* __restrict__ w2) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) w2[k] = dw_pack(dw_split(w[k]));
 }
 
 // compute_flux_edge_kernel over one colour class: no two of these edges share
@@ -389,6 +475,11 @@ struct UpdateArgs {
   int32_t level0;
   double inv_div;  // 1 / (RK + 1 - rk)
   double* rec;
+  double* rec2;            // DW: the next stage's primitives as pairs
+  const double* rec2_in;   // DW fused: the stage's input primitives
+  const int32_t* off2;     // DW fused: per-node neighbour table
+  const int32_t* nb2;
+  const double4_32a* w2;
   float* rec32;
   const double* old;
   double* flux;
@@ -517,7 +608,9 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // shared-memory stalls.  Off by default.
 constexpr int kEpChunk = 768;
 
-template <bool GATHER, bool LAST, bool MIXED, bool SEG, bool PAIR = false, bool FUSED = false, int FV = 0>
+// DW: the state goes to rec and the next stage's primitives to rec2 as pairs.
+template <bool GATHER, bool LAST, bool MIXED, bool SEG, bool PAIR = false, bool FUSED = false, int FV = 0,
+          bool DW = false>
 __global__ void __launch_bounds__(kNodeThreads, (FUSED && PAIR) ? 10 : 0) k_update(UpdateArgs A) {
   constexpr bool STAGE = FV == 1;  // neighbour ids staged by cp.async
   constexpr bool EP = FV == 2;     // edge-parallel ends through shared memory
@@ -645,6 +738,26 @@ __global__ void __launch_bounds__(kNodeThreads, (FUSED && PAIR) ? 10 : 0) k_upda
     if (FUSED && EP) {
 #pragma unroll
       for (int k = 0; k < 5; k++) F[k] = PAIR ? f2d_bits(ep_hi[k]) + f2d_bits(ep_lo[k]) : ep_F[k];
+    } else if (FUSED && DW) {
+      // Node-centric stage in double-word arithmetic: every edge of this node
+      // evaluated with the node as end a (f(b, a; -h) = -f(a, b; h), so the
+      // b-side entries carry -h and need no negation), summed in pairs, and
+      // one FP64 addition per variable at the end.
+      const NodePrimDW me = load_prim_dw(A.rec2_in, i);
+      dwacc S[5];
+#pragma unroll
+      for (int k = 0; k < 5; k++) S[k] = dwacc{0.0f, 0.0f};
+      const int32_t k0 = A.off2[i], k1 = A.off2[i + 1];
+      for (int32_t j = k0; j < k1; j++) {
+        const NodePrimDW o = load_prim_dw(A.rec2_in, A.nb2[j]);
+        const double4_32a w = A.w2[j];
+        dwacc f[5];
+        edge_flux_dw_acc(me, o, dw_unpack(w.x), dw_unpack(w.y), dw_unpack(w.z), dw_unpack(w.w), f);
+#pragma unroll
+        for (int k = 0; k < 5; k++) acc_add_acc(S[k], f[k], false);
+      }
+#pragma unroll
+      for (int k = 0; k < 5; k++) F[k] = acc_to_double(S[k]);
     } else if (FUSED) {
       // Node-centric stage: the flux of each edge of this node, computed from
       // the stage's input primitives exactly as k_flux_mixed computes it
@@ -728,7 +841,7 @@ __global__ void __launch_bounds__(kNodeThreads, (FUSED && PAIR) ? 10 : 0) k_upda
     }
     if (bi >= 0) {
       NodePrim p;
-      if (MIXED) {
+      if (MIXED || DW) {
         const double4_32a* r = reinterpret_cast<const double4_32a*>(A.rec + 8 * i);
         const double4_32a x = r[0];
         p = node_prim(x.x, x.y, x.z, x.w, r[1].x);
@@ -765,6 +878,11 @@ __global__ void __launch_bounds__(kNodeThreads, (FUSED && PAIR) ? 10 : 0) k_upda
       r[0] = make_double4_32a(v[0], v[1], v[2], v[3]);
       A.rec[8 * i + 4] = v[4];
       store_rec32_from_var(A.rec32, i, v[0], v[1], v[2], v[3], v[4]);
+    } else if (DW) {
+      double4_32a* r = reinterpret_cast<double4_32a*>(A.rec + 8 * i);
+      r[0] = make_double4_32a(v[0], v[1], v[2], v[3]);
+      A.rec[8 * i + 4] = v[4];
+      store_prim_dw(A.rec2, i, node_prim_dw(v[0], v[1], v[2], v[3], v[4]));
     } else {
       store_rec(A.rec, i, node_prim(v[0], v[1], v[2], v[3], v[4]));
     }
@@ -977,6 +1095,21 @@ const UpdateFn kUpdate[16] = {
     launch_update<1, 0, 0, 0>, launch_update<1, 0, 0, 1>, launch_update<1, 0, 1, 0>, launch_update<1, 0, 1, 1>,
     launch_update<1, 1, 0, 0>, launch_update<1, 1, 0, 1>, launch_update<1, 1, 1, 0>, launch_update<1, 1, 1, 1>};
 
+template <bool G, bool L, bool S>
+void launch_update_dw(int grid_n, cudaStream_t st, const UpdateArgs& A) {
+  k_update<G, L, false, S, false, false, 0, true><<<grid_n, kNodeThreads, 0, st>>>(A);
+}
+const UpdateFn kUpdateDW[8] = {launch_update_dw<0, 0, 0>, launch_update_dw<0, 0, 1>, launch_update_dw<0, 1, 0>,
+                               launch_update_dw<0, 1, 1>, launch_update_dw<1, 0, 0>, launch_update_dw<1, 0, 1>,
+                               launch_update_dw<1, 1, 0>, launch_update_dw<1, 1, 1>};
+
+template <bool L, bool S>
+void launch_update_dw_fused(int grid_n, cudaStream_t st, const UpdateArgs& A) {
+  k_update<true, L, false, S, false, true, 0, true><<<grid_n, kNodeThreads, 0, st>>>(A);
+}
+const UpdateFn kUpdateDWFused[4] = {launch_update_dw_fused<0, 0>, launch_update_dw_fused<0, 1>,
+                                    launch_update_dw_fused<1, 0>, launch_update_dw_fused<1, 1>};
+
 template <bool L, bool S>
 void launch_update_pair(int grid_n, cudaStream_t st, const UpdateArgs& A) {
   k_update<true, L, true, S, true><<<grid_n, kNodeThreads, 0, st>>>(A);
@@ -1000,15 +1133,16 @@ const UpdateFn kUpdateFused[24] = {
     launch_update_fused<0, 1, 0, 2>, launch_update_fused<0, 1, 1, 2>, launch_update_fused<1, 0, 0, 2>,
     launch_update_fused<1, 0, 1, 2>, launch_update_fused<1, 1, 0, 2>, launch_update_fused<1, 1, 1, 2>};
 
-template <bool M, bool S>
+template <bool M, bool S, bool W = false>
 void launch_step_begin(const DevLevel& D, unsigned long long* key, const DevStatus* st, const SegStop* ss,
                        cudaStream_t stream) {
-  k_step_begin<M, S><<<grid(D.n, kNodeThreads), kNodeThreads, 0, stream>>>(D.n, D.rec, D.rec32, D.old, D.cbrt_vol,
-                                                                            key, st, D.mesh_id, ss);
+  k_step_begin<M, S, W><<<grid(D.n, kNodeThreads), kNodeThreads, 0, stream>>>(D.n, D.rec, D.rec2, D.rec32, D.old,
+                                                                               D.cbrt_vol, key, st, D.mesh_id, ss);
 }
 using StepFn = void (*)(const DevLevel&, unsigned long long*, const DevStatus*, const SegStop*, cudaStream_t);
-const StepFn kStepBegin[4] = {launch_step_begin<0, 0>, launch_step_begin<0, 1>, launch_step_begin<1, 0>,
-                              launch_step_begin<1, 1>};
+// Indexed by precision (FP64, MIXED, DW) * 2 + seg.
+const StepFn kStepBegin[6] = {launch_step_begin<0, 0>, launch_step_begin<0, 1>, launch_step_begin<1, 0>,
+                              launch_step_begin<1, 1>, launch_step_begin<0, 0, 1>, launch_step_begin<0, 1, 1>};
 
 // Where the level-0 norms (calc_rms_kernel, count_bad_vals) are taken: in
 // the last RK stage, or -- for plain multi-level solvers with the fused
@@ -1022,6 +1156,7 @@ bool norms_in_restrict(const mgcfd_solver* s) { return s->fused && s->nseg == 1 
 int enqueue_smooth(mgcfd_solver* s, int level) {
   DevLevel& D = s->L[(size_t)level];
   const bool mixed = s->opt.precision == MGCFD_PRECISION_MIXED;
+  const bool dw = s->opt.precision == MGCFD_PRECISION_DW;
   const bool timing = s->opt.time_kernels && level == 0;
   const bool seg = s->nseg > 1;
   unsigned long long* key = seg ? s->seg_keys + (size_t)level * s->nseg : &s->st->dt_key[level];
@@ -1033,7 +1168,7 @@ int enqueue_smooth(mgcfd_solver* s, int level) {
       CK(cudaMemsetAsync(s->seg_rho, 0, sizeof(double) * (size_t)s->nseg, s->stream));
     }
   }
-  kStepBegin[(mixed ? 2 : 0) | (seg ? 1 : 0)](D, key, s->st, seg ? s->seg_stop : nullptr, s->stream);
+  kStepBegin[(dw ? 4 : mixed ? 2 : 0) | (seg ? 1 : 0)](D, key, s->st, seg ? s->seg_stop : nullptr, s->stream);
   s->launches++;
   const int et = edge_threads(s);
   const bool pair = mixed && s->opt.accumulation == MGCFD_ACCUM_PAIR32;
@@ -1064,7 +1199,10 @@ int enqueue_smooth(mgcfd_solver* s, int level) {
       }
     } else if (D.ne > 0 && !s->fused) {
       const int g = grid(D.ne, et);
-      if (mixed) {
+      if (dw) {
+        if (s->gather) k_flux_dw<true><<<g, et, 0, s->stream>>>(D.ne, D.e2n, D.w4dw, D.rec2, D.flux, D.fe, s->st);
+        else k_flux_dw<false><<<g, et, 0, s->stream>>>(D.ne, D.e2n, D.w4dw, D.rec2, D.flux, D.fe, s->st);
+      } else if (mixed) {
         if (s->gather) k_flux_mixed<true><<<g, et, 0, s->stream>>>(D.ne, D.e2n, D.w4f, D.rec32, D.flux, D.fe32, s->st);
         else k_flux_mixed<false><<<g, et, 0, s->stream>>>(D.ne, D.e2n, D.w4f, D.rec32, D.flux, D.fe32, s->st);
       } else {
@@ -1079,14 +1217,26 @@ int enqueue_smooth(mgcfd_solver* s, int level) {
     }
     UpdateArgs A;
     A.n = D.n; A.level0 = level == 0 && !norms_in_restrict(s); A.inv_div = 1.0 / (double)(kRK + 1 - rk);
-    A.rec = D.rec; A.rec32 = D.rec32; A.old = D.old; A.flux = D.flux; A.fe = D.fe; A.fe32 = D.fe32;
+    A.rec = D.rec; A.rec2 = D.rec2; A.rec32 = D.rec32; A.old = D.old; A.flux = D.flux; A.fe = D.fe; A.fe32 = D.fe32;
     A.a_off = D.a_off; A.b_off = D.b_off; A.b_list = D.b_list; A.inv_vol = D.inv_vol; A.bidx = D.bidx;
     A.bdata = D.bdata; A.res = D.res; A.dt_key = key; A.st = s->st;
     A.mesh_id = D.mesh_id; A.seg_neg = s->seg_neg; A.seg_bad = s->seg_bad; A.seg_rms = s->seg_rms;
     A.seg_rho = s->seg_rho;
     A.seg_stop = seg ? s->seg_stop : nullptr;
     A.e2n = D.e2n; A.w4f = D.w4f; A.b_nbr = D.b_nbr; A.b_w4f = D.b_w4f;
-    if (s->fused) {
+    A.rec2_in = nullptr; A.off2 = D.off2; A.nb2 = D.nb2; A.w2 = D.w2;
+    if (s->fused && dw) {
+      // Stage rk reads the primitives of stage rk and writes those of rk + 1
+      // into the other buffer: k_step_begin fills rec2 for stage 0.
+      A.rec2_in = (rk & 1) ? D.rec2b : D.rec2;
+      A.rec2 = (rk & 1) ? D.rec2 : D.rec2b;
+      A.rec32_in = nullptr;
+      kUpdateDWFused[(last ? 2 : 0) | (seg ? 1 : 0)](grid(D.n, kNodeThreads), s->stream, A);
+      if (time_this) {
+        CK(cudaEventRecord(ev.second, s->stream));
+        s->pending.push_back(ev);
+      }
+    } else if (s->fused) {
       // Stage rk reads the primitives of stage rk and writes those of rk + 1
       // into the other buffer: k_step_begin fills rec32 for stage 0.
       A.rec32_in = (rk & 1) ? D.rec32b : D.rec32;
@@ -1100,6 +1250,9 @@ int enqueue_smooth(mgcfd_solver* s, int level) {
     } else if (mixed && s->gather && pair) {
       A.rec32_in = nullptr;
       kUpdatePair[(last ? 2 : 0) | (seg ? 1 : 0)](grid(D.n, kNodeThreads), s->stream, A);
+    } else if (dw) {
+      A.rec32_in = nullptr;
+      kUpdateDW[(s->gather ? 4 : 0) | (last ? 2 : 0) | (seg ? 1 : 0)](grid(D.n, kNodeThreads), s->stream, A);
     } else {
       A.rec32_in = nullptr;
       kUpdate[(s->gather ? 8 : 0) | (last ? 4 : 0) | (mixed ? 2 : 0) | (seg ? 1 : 0)](grid(D.n, kNodeThreads), s->stream, A);
@@ -1306,16 +1459,44 @@ int colour_edges(mgcfd_solver* s, DevLevel& D) {
   return MGCFD_OK;
 }
 
-// Increment strategy: AUTO is FP64 atomics for FP64 and the fused
+// DW precision: one level's primitives as pair words (written by the node
+// kernels) and its edge weights split into pairs, from the FP64 weights.
+// FUSED: also the second primitive buffer and the per-node neighbour table
+// (nb2, w2 from off2), from the CSR tables a_off, b_off and b_list.
+int build_dw_tables(mgcfd_solver* s, DevLevel& D) {
+  int r;
+  if ((r = s->alloc(&D.rec2, 8 * (size_t)D.n)) || (r = s->alloc(&D.w4dw, (size_t)D.ne))) return r;
+  const int64_t nw = 4 * (int64_t)D.ne;
+  if (nw) k_split_weights<<<grid(nw, 256), 256, 0, s->stream>>>(nw, reinterpret_cast<const double*>(D.w4),
+                                                                reinterpret_cast<double*>(D.w4dw));
+  if (s->fused) {
+    if ((r = s->alloc(&D.rec2b, 8 * (size_t)D.n)) || (r = s->alloc(&D.off2, (size_t)D.n + 1)) ||
+        (r = s->alloc(&D.nb2, 2 * (size_t)D.ne)) || (r = s->alloc(&D.w2, 2 * (size_t)D.ne)))
+      return r;
+    k_dw_offsets<<<grid((int64_t)D.n + 1, 256), 256, 0, s->stream>>>(D.n, D.a_off, D.b_off, D.off2);
+    if (D.ne) {
+      k_dw_table_a<<<grid(D.ne, 256), 256, 0, s->stream>>>(D.ne, D.e2n, D.w4dw, D.a_off, D.off2, D.nb2, D.w2);
+      k_dw_table_b<<<grid(D.ne, 256), 256, 0, s->stream>>>(D.ne, D.e2n, D.w4dw, D.b_list, D.a_off, D.b_off, D.off2,
+                                                           D.nb2, D.w2);
+    }
+  }
+  CK(cudaGetLastError());
+  return MGCFD_OK;
+}
+
+// Increment strategy: AUTO is FP64 atomics for FP64 and DW, and the fused
 // node-centric stage for mixed precision (the fastest of each, measured).
 int resolve_increment(mgcfd_solver* s) {
   const int inc = s->opt.increment;
   const bool mixed = s->opt.precision == MGCFD_PRECISION_MIXED;
   if (inc < MGCFD_INCREMENT_AUTO || inc > MGCFD_INCREMENT_COLOURED)
     return set_error(MGCFD_ERR_INVALID, "unknown increment strategy");
-  if (inc == MGCFD_INCREMENT_FUSED && !mixed)
-    return set_error(MGCFD_ERR_INVALID, "the fused increment needs mixed precision");
-  if (inc == MGCFD_INCREMENT_COLOURED && mixed)
+  const bool dw = s->opt.precision == MGCFD_PRECISION_DW;
+  if (inc == MGCFD_INCREMENT_FUSED && !mixed && !dw)
+    return set_error(MGCFD_ERR_INVALID, "the fused increment needs mixed or DW precision");
+  if (dw && (s->opt.stage_neighbour_ids || s->opt.edge_parallel_stage))
+    return set_error(MGCFD_ERR_INVALID, "the staged and edge-parallel fused variants are mixed-precision forms");
+  if (inc == MGCFD_INCREMENT_COLOURED && s->opt.precision != MGCFD_PRECISION_FP64)
     return set_error(MGCFD_ERR_INVALID, "the coloured increment is an FP64 strategy");
   s->coloured = inc == MGCFD_INCREMENT_COLOURED;
   s->fused = inc == MGCFD_INCREMENT_FUSED || (inc == MGCFD_INCREMENT_AUTO && mixed);
@@ -1343,7 +1524,7 @@ extern "C" int mgcfd_solver_create(int32_t nlevels, const mgcfd_level_view* leve
   if (!s) return set_error(MGCFD_ERR_NOMEM, "host allocation failed");
   int r0;
   if (opt) s->opt = *opt; else mgcfd_solver_default_options(&s->opt);
-  if (s->opt.precision != MGCFD_PRECISION_FP64 && s->opt.precision != MGCFD_PRECISION_MIXED)
+  if (s->opt.precision < MGCFD_PRECISION_FP64 || s->opt.precision > MGCFD_PRECISION_DW)
     return set_error(MGCFD_ERR_INVALID, "unknown precision");
   if (s->opt.accumulation != MGCFD_ACCUM_FP64 && s->opt.accumulation != MGCFD_ACCUM_PAIR32)
     return set_error(MGCFD_ERR_INVALID, "unknown accumulation");
@@ -1427,8 +1608,10 @@ extern "C" int mgcfd_solver_create(int32_t nlevels, const mgcfd_level_view* leve
     // The host vectors of this level die at the end of create: finish the copies first.
     CK(cudaStreamSynchronize(s->stream));
   }
-  for (auto& D : s->L)
+  for (auto& D : s->L) {
     if (s->coloured && (r = colour_edges(s.get(), D))) return r;
+    if (s->opt.precision == MGCFD_PRECISION_DW && (r = build_dw_tables(s.get(), D))) return r;
+  }
   if ((r = s->alloc(&s->st, 1)) || (r = s->alloc(&s->fetch_buf, 5 * max_n))) return r;
   if ((r = init_state(s.get()))) return r;
   CK(cudaStreamSynchronize(s->stream));
@@ -1447,7 +1630,7 @@ extern "C" int mgcfd_batch_create(int32_t nmeshes, int32_t nlevels, const mgcfd_
   if (!s) return set_error(MGCFD_ERR_NOMEM, "host allocation failed");
   int r0;
   if (opt) s->opt = *opt; else mgcfd_solver_default_options(&s->opt);
-  if (s->opt.precision != MGCFD_PRECISION_FP64 && s->opt.precision != MGCFD_PRECISION_MIXED)
+  if (s->opt.precision < MGCFD_PRECISION_FP64 || s->opt.precision > MGCFD_PRECISION_DW)
     return set_error(MGCFD_ERR_INVALID, "unknown precision");
   if (s->opt.accumulation != MGCFD_ACCUM_FP64 && s->opt.accumulation != MGCFD_ACCUM_PAIR32)
     return set_error(MGCFD_ERR_INVALID, "unknown accumulation");
@@ -1481,6 +1664,8 @@ extern "C" int mgcfd_batch_create(int32_t nmeshes, int32_t nlevels, const mgcfd_
   s->nseg = nmeshes;
   s->L.resize((size_t)nlevels);
   if ((r = device_prepare(s.get(), meshes))) return r;
+  for (auto& D : s->L)
+    if (s->opt.precision == MGCFD_PRECISION_DW && (r = build_dw_tables(s.get(), D))) return r;
   size_t max_n = 0;
   for (auto& D : s->L) max_n = std::max(max_n, (size_t)D.n);
   const size_t ns = (size_t)nmeshes;
@@ -1538,6 +1723,7 @@ extern "C" int mgcfd_solver_run(mgcfd_solver* s, int32_t ncycles) {
 }
 
 int mgcfd::build_fused_tables(mgcfd_solver* s, DevLevel& D) {
+  if (s->opt.precision == MGCFD_PRECISION_DW) return MGCFD_OK;  // its own tables: build_dw_tables
   int r;
   if ((r = s->alloc(&D.rec32b, 8 * (size_t)D.n)) || (r = s->alloc(&D.b_nbr, (size_t)D.ne)) ||
       (r = s->alloc(&D.b_w4f, (size_t)D.ne)))

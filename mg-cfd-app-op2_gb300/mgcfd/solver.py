@@ -8,7 +8,7 @@ import numpy as np
 from . import _lib
 from .mesh import HostMesh, level_views_from_arrays
 
-PRECISION = {"fp64": 0, "mixed": 1}
+PRECISION = {"fp64": 0, "mixed": 1, "dw": 2}
 INCREMENT = {"auto": 0, "atomic": 1, "gather": 2, "fused": 3, "coloured": 4}
 RENUMBER = {"none": 0, "spatial": 1, "rcm": 2}
 ACCUMULATION = {"fp64": 0, "pair32": 1}
