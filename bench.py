@@ -7,7 +7,7 @@ Mach 0.8, angle of attack 3 degrees, FP64.  One step = one V-cycle
 (euler3d.cpp:458-641: 6 smoothing steps, 18 edge-flux sweeps).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                  [--precision fp64|mixed] [--increment atomic|gather] [--n 200]
+                  [--precision fp64|mixed|dw] [--increment atomic|gather|fused] [--n 200]
   python bench.py --mode batch     # 64 uneven meshes in one launch per stage
   python bench.py --mode serve     # Poisson request stream, p50/p99 latency
   python bench.py --mode loops     # the V-cycle through the per-loop entry points
@@ -17,8 +17,10 @@ Prints one JSON line.  `value` is V-cycles/s with the mesh resident in HBM
 `e2e` is V-cycles/s through the host-buffer entry point mgcfd_solve (mesh
 upload, setup, 25 V-cycles, download of every level's state), and `roofline`
 describes the level-0 edge-flux kernel.  The same line carries the
-mixed-precision workload on the same mesh (`mixed`) and served solves on a
-fresh-mesh request stream against the plain FP64 path (`served`).  --impl reference times the CPU
+double-word form (FP64 state, float-float edge flux and primitives, held to
+the FP64 bar: `dw`) and the mixed-precision workload (`mixed`) on the same
+mesh, and served solves on a fresh-mesh request stream against the plain
+FP64 path (`served`).  --impl reference times the CPU
 restatement of the reference path (OpenMP, all host threads) on the same
 mesh.  Under torchrun each rank runs an independent replica (the solve does
 not shard across GPUs); value is the sum over ranks.
@@ -288,9 +290,12 @@ def run_gb300(args):
     e2e_value, e2e_elapsed = replicas.job_throughput(e2e_steps * E2E_CYCLES, te1 - te0, dist, device="cuda")
     del pinned, hl, outs
 
-    mixed = served = cpu = None
+    mixed = dw = served = cpu = None
     if rank == 0 and not args.no_extra_forms:
-        mixed = mixed_section(mesh, args, N, E, stream, value if args.precision == "fp64" else None)
+        want = fp64_reference(mesh, stream, MIXED_CYCLES)
+        fp64_value = value if args.precision == "fp64" else None
+        dw = dw_section(mesh, args, N, E, stream, fp64_value, want)
+        mixed = mixed_section(mesh, args, N, E, stream, fp64_value, want)
         served = served_section(args)
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(levels, args.cpu_cycles)
@@ -327,6 +332,7 @@ def run_gb300(args):
                 "steps": e2e_steps},
         "gpu_launches": launches,
         "clocks": clocks.summary(),
+        "dw": dw,
         "mixed": mixed,
         "served": served,
         "cpu_baseline": cpu,
@@ -344,49 +350,85 @@ def line_config(args, N, E):
             "l2": "inputs larger than L2 (level-0 state and edges ~2.4 GB), no flush"}
 
 
-def mixed_section(mesh, args, N, E, stream, fp64_value):
-    """The mixed-precision workload on the same mesh: edge-flux arithmetic and
-    geometry in FP32, node sums, time step and norms in FP64 (FP64 node sums,
-    or compensated FP32-pair sums).  V-cycles/s on the CUDA-graph path, the
-    fused stage's roofline, and each variable's max and L2 relative error of
-    the final state after 25 V-cycles against the FP64 solve."""
-    import numpy as np
-
+def fp64_reference(mesh, stream, cycles):
+    """Every level's state after `cycles` V-cycles of the FP64 solver."""
     import mgcfd
     from mgcfd import _lib
-    cycles = MIXED_CYCLES
     ref = mgcfd.Solver(mesh, MACH, AOA, stream=stream.cuda_stream)
     ref.run(cycles)
     if ref.synchronize() != 0:
         raise RuntimeError(_lib.load().mgcfd_last_error().decode())
     want = [ref.fetch(l) for l in range(NLEVELS)]
     ref.close()
+    return want
+
+
+def timed_form(mesh, args, stream, cycles, want, **opts):
+    """V-cycles/s of one solver form on the CUDA-graph path, then its final
+    state after `cycles` V-cycles from the start against `want`: each
+    variable's max and L2 relative error at level 0, the worst max relative
+    error over all levels, and the FP64 parity metric (largest error relative
+    to each value, or to a thousandth of its variable's scale)."""
+    import numpy as np
+
+    import mgcfd
+    from mgcfd import _lib
+    sys.path.insert(0, str(ROOT / "tests"))
+    from parity import state_error
+    s = mgcfd.Solver(mesh, MACH, AOA, stream=stream.cuda_stream, **opts)
+    s.run(args.warmup)
+    if s.synchronize() != 0:
+        raise RuntimeError(_lib.load().mgcfd_last_error().decode())
+    secs, st = timed_cycles(s, stream, args.steps)
+    if st != 0:
+        raise RuntimeError(_lib.load().mgcfd_last_error().decode())
+    s.reset()
+    s.run(cycles)
+    if s.synchronize() != 0:
+        raise RuntimeError(_lib.load().mgcfd_last_error().decode())
+    got = [s.fetch(l) for l in range(NLEVELS)]
+    s.close()
+    mx = np.abs(got[0] - want[0]).max(axis=0) / np.abs(want[0]).max(axis=0)
+    l2 = np.linalg.norm(got[0] - want[0], axis=0) / np.linalg.norm(want[0], axis=0)
+    worst = max(float((np.abs(g - w).max(axis=0) / np.abs(w).max(axis=0)).max()) for g, w in zip(got, want))
+    parity = max(state_error(g, w) for g, w in zip(got, want))
+    return args.steps / secs, {"max_rel_l0": [float(f"{x:.3e}") for x in mx],
+                               "l2_rel_l0": [float(f"{x:.3e}") for x in l2],
+                               "max_rel_all_levels": float(f"{worst:.3e}"),
+                               "state_error_all_levels": float(f"{parity:.3e}")}
+
+
+def dw_section(mesh, args, N, E, stream, fp64_value, want):
+    """The double-word form on the same mesh: state, node sums, time step and
+    norms in FP64, edge fluxes and node primitives in float-float arithmetic on
+    the FP32 pipes, fused node-centric stage.  Held to the FP64 path's 1e-10
+    bar; its state after 25 V-cycles is compared with the FP64 solve's."""
+    opts = dict(precision="dw", increment="fused", renumber=args.renumber)
+    rate, err = timed_form(mesh, args, stream, MIXED_CYCLES, want, **opts)
+    return {"workload": f"{args.n}^3 lattice, {NLEVELS} levels, Mach {MACH}, AoA {AOA} deg, fused node-centric stage",
+            "dtype": "f32x2-flux/f64", "value": round(rate, 3), "unit": "cycles/s",
+            "speedup_vs_fp64_value": round(rate / fp64_value, 3) if fp64_value else None,
+            "error_against": f"FP64 solve of the same mesh after {MIXED_CYCLES} V-cycles",
+            "variables": ["rho", "rho_u", "rho_v", "rho_w", "rho_E"], **err,
+            "roofline": flux_roofline("dw", "fused", args.n, N, E, kernel_times(mesh, args.kernel_cycles, **opts))}
+
+
+def mixed_section(mesh, args, N, E, stream, fp64_value, want):
+    """The mixed-precision workload on the same mesh: edge-flux arithmetic and
+    geometry in FP32, node sums, time step and norms in FP64 (FP64 node sums,
+    or compensated FP32-pair sums).  V-cycles/s on the CUDA-graph path, the
+    fused stage's roofline, and each variable's max and L2 relative error of
+    the final state after 25 V-cycles against the FP64 solve."""
+    cycles = MIXED_CYCLES
     out = {"workload": f"{args.n}^3 lattice, {NLEVELS} levels, Mach {MACH}, AoA {AOA} deg, fused node-centric stage",
            "error_against": f"FP64 solve of the same mesh after {cycles} V-cycles",
            "variables": ["rho", "rho_u", "rho_v", "rho_w", "rho_E"]}
     for acc in ("fp64", "pair32"):
         opts = dict(precision="mixed", increment="fused", renumber=args.renumber, accumulation=acc)
-        s = mgcfd.Solver(mesh, MACH, AOA, stream=stream.cuda_stream, **opts)
-        s.run(args.warmup)
-        if s.synchronize() != 0:
-            raise RuntimeError(_lib.load().mgcfd_last_error().decode())
-        secs, st = timed_cycles(s, stream, args.steps)
-        if st != 0:
-            raise RuntimeError(_lib.load().mgcfd_last_error().decode())
-        s.reset()
-        s.run(cycles)
-        if s.synchronize() != 0:
-            raise RuntimeError(_lib.load().mgcfd_last_error().decode())
-        got = [s.fetch(l) for l in range(NLEVELS)]
-        s.close()
-        mx = np.abs(got[0] - want[0]).max(axis=0) / np.abs(want[0]).max(axis=0)
-        l2 = np.linalg.norm(got[0] - want[0], axis=0) / np.linalg.norm(want[0], axis=0)
-        worst = max(float((np.abs(g - w).max(axis=0) / np.abs(w).max(axis=0)).max()) for g, w in zip(got, want))
+        rate, err = timed_form(mesh, args, stream, cycles, want, **opts)
         out[f"accumulation_{acc}"] = {
-            "value": round(args.steps / secs, 3), "unit": "cycles/s",
-            "speedup_vs_fp64_value": round(args.steps / secs / fp64_value, 3) if fp64_value else None,
-            "max_rel_l0": [float(f"{x:.3e}") for x in mx], "l2_rel_l0": [float(f"{x:.3e}") for x in l2],
-            "max_rel_all_levels": float(f"{worst:.3e}"),
+            "value": round(rate, 3), "unit": "cycles/s",
+            "speedup_vs_fp64_value": round(rate / fp64_value, 3) if fp64_value else None, **err,
             "roofline": flux_roofline("mixed", "fused", args.n, N, E, kernel_times(mesh, args.kernel_cycles, **opts))}
     return out
 
@@ -430,10 +472,13 @@ SERVE_FORMS = {"plain_fp64": dict(slots=1, precision="fp64"),
                "served_mixed_pair32": dict(precision="mixed", accumulation="pair32"),
                "served_mixed_cohorts": dict(precision="mixed", batch_max_meshes=16, batch_max_nodes=COHORT_NODES),
                "served_mixed_pair32_cohorts": dict(precision="mixed", accumulation="pair32", batch_max_meshes=16,
-                                                   batch_max_nodes=COHORT_NODES)}
+                                                   batch_max_nodes=COHORT_NODES),
+               "served_dw": dict(precision="dw"),
+               "served_dw_cohorts": dict(precision="dw", batch_max_meshes=16, batch_max_nodes=COHORT_NODES)}
 RATE_FORMS = ("plain_fp64", "served_mixed", "served_mixed_pair32", "served_mixed_cohorts",
-              "served_mixed_pair32_cohorts")
-ERROR_FORMS = ("served_mixed", "served_mixed_pair32", "served_mixed_cohorts", "served_mixed_pair32_cohorts")
+              "served_mixed_pair32_cohorts", "served_dw")
+ERROR_FORMS = ("served_mixed", "served_mixed_pair32", "served_mixed_cohorts", "served_mixed_pair32_cohorts",
+               "served_dw", "served_dw_cohorts")
 
 
 def serve_stream(pool, picks, machs, aoas, gaps, form, rate, slots, reuse, want_results=False):
@@ -532,6 +577,8 @@ def served_section(args):
             "speedup_served_mixed_cohorts_vs_plain_fp64": round(c["served_mixed_cohorts"] / c["plain_fp64"], 3),
             "speedup_served_mixed_pair32_cohorts_vs_plain_fp64": round(c["served_mixed_pair32_cohorts"] /
                                                                        c["plain_fp64"], 3),
+            "speedup_served_dw_vs_plain_fp64": round(c["served_dw"] / c["plain_fp64"], 3),
+            "speedup_served_dw_cohorts_vs_plain_fp64": round(c["served_dw_cohorts"] / c["plain_fp64"], 3),
             "cohort_rule": f"requests of at most {COHORT_NODES} level-0 nodes waiting together share one batched "
                            "solver (up to 16)",
             "poisson": {"rate_multiple_of_plain_capacity": args.line_serve_rate, "runs": at_rate},
@@ -649,7 +696,7 @@ def run_batch(args):
         line["timing"] = f"median wall time of {repeats} runs, each from host meshes to level-0 results on the host"
         t_seq, seq = timed(solve_sequential, precision="fp64")
         results = {"sequential_fp64": nm / t_seq}
-        for prec in ("fp64", "mixed"):
+        for prec in ("fp64", "mixed", "dw"):
             t0 = time.perf_counter()
             best, timings = autotune.tune_batch(meshes, machs, aoas, precision=prec)
             t_tune = time.perf_counter() - t0
@@ -673,6 +720,7 @@ def run_batch(args):
     line["results_solves_per_s"] = {k: round(v, 3) for k, v in results.items()}
     line["speedup_batched_fp64_vs_sequential"] = round(results["batched_fp64"] / results["sequential_fp64"], 3)
     line["speedup_batched_mixed_vs_sequential_fp64"] = round(results["batched_mixed"] / results["sequential_fp64"], 3)
+    line["speedup_batched_dw_vs_sequential_fp64"] = round(results["batched_dw"] / results["sequential_fp64"], 3)
     print(json.dumps(line), flush=True)
 
 

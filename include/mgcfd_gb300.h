@@ -268,21 +268,23 @@ int mgcfd_op_count_differences(int32_t nnodes, const double* test, const double*
 /* ------------------------------------------------------------------------ */
 /* Device-resident multigrid solver.                                        */
 /* FP64: every operation in binary64.  MIXED: FP32 edge-flux arithmetic and
- * geometry, FP64 node sums, time step and norms.  DW: the state, node sums,
- * time step, norms and node primitives computed in binary64 as for FP64; the
- * edge flux evaluated on the FP32 pipes in double-word arithmetic (each input
- * held as an unevaluated pair of binary32 numbers, 48 significand bits,
- * error-free TwoSum / TwoProd steps), with its inputs -- the primitives and
- * the edge weights -- stored as such pairs.  Within the same 1e-10 relative
- * bar of the FP64 reference as FP64; the exponent range of the flux inputs is
- * binary32's.  DW takes the ATOMIC (AUTO) or GATHER increment. */
+ * geometry, FP64 node sums, time step and norms.  DW: the state, the time
+ * step, the norms and min_dt in binary64; the node primitives, the edge
+ * fluxes and their per-node sums in double-word arithmetic on the FP32 pipes
+ * (each value an unevaluated pair of binary32 numbers, 48 significand bits,
+ * built from error-free TwoSum / TwoProd steps), with the primitives and the
+ * edge weights stored as such pairs.  Within the same 1e-10 relative bar of
+ * the FP64 reference as FP64; the exponent range of the pairs is binary32's.
+ * DW takes the FUSED (AUTO), ATOMIC or GATHER increment. */
 enum { MGCFD_PRECISION_FP64 = 0, MGCFD_PRECISION_MIXED = 1, MGCFD_PRECISION_DW = 2 };
 /* How the edge fluxes reach the nodes.  ATOMIC: each edge adds +f / -f to its
  * end nodes with FP64 atomics.  GATHER: each edge stores f, then each node
  * sums its edges' f in a fixed order (deterministic).  FUSED (mixed precision
- * only): one node-centric kernel per RK stage computes the FP32 flux of every
- * edge at both of its end nodes from the same inputs in the same order, sums
- * them exactly as GATHER does and applies the time step -- GATHER's results
+ * and DW): one node-centric kernel per RK stage computes the flux of every
+ * edge at both of its end nodes, sums them in a fixed order and applies the
+ * time step (deterministic).  In mixed precision it computes each FP32 flux
+ * from the same inputs in the same order as GATHER and sums exactly as GATHER
+ * does -- GATHER's results
  * bit for bit, with no per-edge flux array and one launch per stage. */
 /* COLOURED (FP64, single-mesh solvers): each level's edges are split at set-up
  * into colour classes in which no two edges share a node (greedy, at most 64

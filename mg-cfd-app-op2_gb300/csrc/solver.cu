@@ -574,7 +574,9 @@ __device__ __forceinline__ void block_norms(double* srms, double* srho, int* sba
 // everything on min_dt < 0 or NaN/Inf (the reference aborts); batched
 // solvers mark the failing mesh and leave the others running.  The fused
 // stage with pair sums is latency-bound: capped at 48 registers (10 blocks
-// per SM, a few bytes spilled) it runs 2% faster.  Every other form keeps the
+// per SM, a few bytes spilled) it runs 2% faster; the DW stage capped at 64
+// (8 blocks, no spill) 1.5% faster than at its own 72, and slower at 56
+// (spills).  Every other form keeps the
 // compiler's own register choice: a minimum of 0 blocks is no constraint,
 // whereas a minimum of 1 lets it grow to 70-80 registers and lose occupancy.
 // Fused stage, STAGE (option stage_neighbour_ids): the block's neighbour ids
@@ -611,7 +613,7 @@ constexpr int kEpChunk = 768;
 // DW: the state goes to rec and the next stage's primitives to rec2 as pairs.
 template <bool GATHER, bool LAST, bool MIXED, bool SEG, bool PAIR = false, bool FUSED = false, int FV = 0,
           bool DW = false>
-__global__ void __launch_bounds__(kNodeThreads, (FUSED && PAIR) ? 10 : 0) k_update(UpdateArgs A) {
+__global__ void __launch_bounds__(kNodeThreads, (FUSED && PAIR) ? 10 : (FUSED && DW) ? 8 : 0) k_update(UpdateArgs A) {
   constexpr bool STAGE = FV == 1;  // neighbour ids staged by cp.async
   constexpr bool EP = FV == 2;     // edge-parallel ends through shared memory
   __shared__ int32_t s_aid[STAGE ? kStageIds : 1], s_bid[STAGE ? kStageIds : 1];
@@ -1484,8 +1486,9 @@ int build_dw_tables(mgcfd_solver* s, DevLevel& D) {
   return MGCFD_OK;
 }
 
-// Increment strategy: AUTO is FP64 atomics for FP64 and DW, and the fused
-// node-centric stage for mixed precision (the fastest of each, measured).
+// Increment strategy: AUTO is FP64 atomics for FP64, and the fused
+// node-centric stage for mixed precision and DW (the fastest of each,
+// measured; DW at 8M nodes: fused 248, gather 177, atomic 125 V-cycles/s).
 int resolve_increment(mgcfd_solver* s) {
   const int inc = s->opt.increment;
   const bool mixed = s->opt.precision == MGCFD_PRECISION_MIXED;
@@ -1499,7 +1502,7 @@ int resolve_increment(mgcfd_solver* s) {
   if (inc == MGCFD_INCREMENT_COLOURED && s->opt.precision != MGCFD_PRECISION_FP64)
     return set_error(MGCFD_ERR_INVALID, "the coloured increment is an FP64 strategy");
   s->coloured = inc == MGCFD_INCREMENT_COLOURED;
-  s->fused = inc == MGCFD_INCREMENT_FUSED || (inc == MGCFD_INCREMENT_AUTO && mixed);
+  s->fused = inc == MGCFD_INCREMENT_FUSED || (inc == MGCFD_INCREMENT_AUTO && (mixed || dw));
   s->gather = s->fused || inc == MGCFD_INCREMENT_GATHER;
   s->fused_variant = !s->fused ? 0 : s->opt.edge_parallel_stage ? 2 : s->opt.stage_neighbour_ids ? 1 : 0;
   return MGCFD_OK;

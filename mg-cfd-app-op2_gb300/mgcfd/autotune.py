@@ -27,8 +27,8 @@ def tune(make, total_nodes: int, precision: str = "fp64", cycles: int = 2, candi
         return _CACHE[key]
     timings = {}
     for inc, bs in candidates:
-        if inc == "fused" and precision != "mixed":
-            continue  # the fused node-centric stage exists for mixed precision only
+        if inc == "fused" and precision not in ("mixed", "dw"):
+            continue  # the fused node-centric stage exists for mixed precision and DW
         s = make(increment=inc, block_size=bs, precision=precision)
         s.run(1)  # warm-up, graph capture
         if s.synchronize() != 0:

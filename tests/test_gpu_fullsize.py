@@ -2,9 +2,9 @@
 23,880,000 edges, 4 levels) at Mach 0.8 and 3 degrees.
 
 The oracle's OpenMP form (coloured edges on every host core) runs this mesh
-at about half a V-cycle per second on 16 cores, so the FP64 path is checked
-against it directly over the 25 V-cycles the workload names (about a
-minute); the other checks are size-independent properties: the fused
+at about half a V-cycle per second on 16 cores, so the FP64 path and the
+double-word form are checked against it directly over the 25 V-cycles the
+workload names (about a minute); the other checks are size-independent properties: the fused
 mixed-precision stage equals the gather stage bit for bit, mixed precision
 stays within 1e-6 of FP64 after 25 V-cycles (the mixed-precision workload),
 and renumbering the nodes only relabels the solution."""
@@ -36,17 +36,23 @@ def _solve(mesh, cycles, **opts):
     return out
 
 
-def test_fp64_matches_oracle_at_8m_nodes(mesh):
-    cycles = 25
-    got = _solve(mesh, cycles)
+@pytest.fixture(scope="module")
+def oracle25(mesh):
     ref = O.OracleRun(mesh.levels())
-    assert ref.run(MACH, AOA, cycles, nthreads=os.cpu_count() or 1)[0] == 0
+    assert ref.run(MACH, AOA, 25, nthreads=os.cpu_count() or 1)[0] == 0
+    out = [ref.get(l, O.Q_VARIABLES) for l in range(LEVELS)]
+    ref.close()
+    return out
+
+
+@pytest.mark.parametrize("opts", [dict(), dict(precision="dw", increment="fused")], ids=["fp64", "dw_fused"])
+def test_matches_oracle_at_8m_nodes(mesh, oracle25, opts):
+    """FP64, and the double-word form at the same bar, over the workload's 25 V-cycles."""
+    got = _solve(mesh, 25, **opts)
     x0 = np.asarray(list(mgcfd.freestream(MACH, AOA).ff_variable))
     for l in range(LEVELS):
-        r = ref.get(l, O.Q_VARIABLES)
-        assert state_error(got[l], r) <= STATE_TOL
-        assert delta_error(got[l], r, x0) <= DELTA_TOL
-    ref.close()
+        assert state_error(got[l], oracle25[l]) <= STATE_TOL, (l, state_error(got[l], oracle25[l]))
+        assert delta_error(got[l], oracle25[l], x0) <= DELTA_TOL
 
 
 def test_fused_equals_gather_at_8m_nodes(mesh):

@@ -80,6 +80,30 @@ def test_served_mixed_alone_equals_mix_bitwise(meshes, accumulation):
         assert mx.max() <= MIXED_TOL and l2.max() <= MIXED_TOL, (i, mx, l2)
 
 
+def test_served_dw_alone_equals_mix_bitwise(meshes):
+    """The served double-word form (fused node-centric stage): the same bits
+    alone and in a mix of overlapping requests, at the FP64 bar of the oracle."""
+    cycles = 4
+    alone = {}
+    for i in range(len(CASES)):
+        srv = mgcfd.Server(max_active=1, precision="dw", max_cycles=cycles)
+        alone.update(run_requests(srv, meshes, [i]))
+        srv.close()
+    srv = mgcfd.Server(max_active=4, precision="dw", max_cycles=cycles)
+    mix = run_requests(srv, meshes, range(len(CASES)))
+    st = srv.stats()
+    srv.close()
+    assert st["completed"] == len(CASES) and st["failed"] == 0 and st["peak_active"] >= 2
+    for i in range(len(CASES)):
+        ra, va = alone[i]
+        rm, vm = mix[i]
+        assert ra["status"] == rm["status"] == 0 and ra["cycles"] == rm["cycles"] == cycles
+        np.testing.assert_array_equal(va, vm)
+        ref = O.OracleRun(meshes[i].levels())
+        assert ref.run(CASES[i][3], CASES[i][4], cycles)[0] == 0
+        assert state_error(vm, ref.get(0, O.Q_VARIABLES)) <= STATE_TOL
+
+
 def test_alone_equals_mix_within_tolerance_with_atomics(meshes):
     srv = mgcfd.Server(max_active=1, increment="atomic", max_cycles=3)
     alone = run_requests(srv, meshes, range(3))
@@ -227,7 +251,7 @@ def run_cohort_stream(meshes, cases, **opts):
 
 @pytest.mark.parametrize("opts", [dict(precision="mixed", increment="fused", accumulation="fp64"),
                                   dict(precision="mixed", increment="fused", accumulation="pair32"),
-                                  dict(precision="fp64", increment="gather")])
+                                  dict(precision="fp64", increment="gather"), dict(precision="dw")])
 def test_cohort_results_equal_requests_alone_bitwise(cohort_meshes, opts):
     cycles = 4
     mix, st = run_cohort_stream(cohort_meshes, COHORT, max_cycles=cycles, **opts)
@@ -250,6 +274,10 @@ def test_cohort_results_equal_requests_alone_bitwise(cohort_meshes, opts):
             assert ref.run(c[3], c[4], cycles)[0] == 0
             mx, l2 = per_variable_errors(vm, ref.get(0, O.Q_VARIABLES))
             assert mx.max() <= MIXED_TOL and l2.max() <= MIXED_TOL
+        elif opts["precision"] == "dw":
+            ref = O.OracleRun(m.levels())
+            assert ref.run(c[3], c[4], cycles)[0] == 0
+            assert state_error(vm, ref.get(0, O.Q_VARIABLES)) <= STATE_TOL
 
 
 def test_cohort_stop_rule_is_per_request(cohort_meshes):
