@@ -59,12 +59,12 @@ def algorithmic_flux_bytes(nnodes: int, nedges: int, precision: str = "fp64", in
     CSR offsets (20 B), state written (40 B) and next primitives written (32 B).
     DW (double-word flux): 32 B weights as pair words + 8 B map per edge; 64 B
     primitives as pair words read, 40 B flux read and 40 B written per node.
-    DW, fused stage: per edge both ends' table entries (neighbour id and
-    weight pair words, 2 x 36 B); per node the primitives read (64 B), old
-    state (40 B), 1/vol, boundary index and table offset (16 B), state written
-    (40 B) and next primitives written (64 B)."""
+    DW, fused stage: per edge both ends' table entries (neighbour and edge
+    index, 2 x 8 B) and the weights as pair words (32 B); per node the
+    primitives read (64 B), old state (40 B), 1/vol, boundary index and table
+    offset (16 B), state written (40 B) and next primitives written (64 B)."""
     if precision == "dw" and increment == "fused":
-        return 72 * nedges + 224 * nnodes
+        return 48 * nedges + 224 * nnodes
     if precision == "dw":
         return 40 * nedges + 144 * nnodes
     if precision == "mixed" and increment == "fused":

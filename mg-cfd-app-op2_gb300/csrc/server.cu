@@ -161,9 +161,9 @@ int64_t estimate_bytes(const std::vector<mgcfd_level_view>& lv, int precision, i
     int64_t node = 8 * 8 + 5 * 8 * 3 + 8 * 3 + 4 * 4 + 32;   // rec, old/res/flux, vol constants, maps, dvec
     int64_t edge = 8 + 32;                                    // e2n, w4
     if (mixed) { node += fused ? 64 : 32; edge += 16; }
-    if (dw) {  // rec2, w4dw; fused: rec2b, off2, nb2, w2
+    if (dw) {  // rec2, w4dw; fused: rec2b, off2, ent2
       node += 64 + (fused ? 68 : 0);
-      edge += 32 + (fused ? 72 : 0);
+      edge += 32 + (fused ? 16 : 0);
     }
     if (fused) edge += 4 + 4 + 16;                 // b_list, b_nbr, b_w4f
     else if (gather) edge += (mixed ? 20 : 40) + 4;  // per-edge fluxes, b_list

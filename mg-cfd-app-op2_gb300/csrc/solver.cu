@@ -340,35 +340,24 @@ __global__ void k_dw_offsets(int32_t n, const int32_t* __restrict__ a_off, const
   if (i <= n) off2[i] = a_off[i] + b_off[i];
 }
 
-__global__ void k_dw_table_a(int32_t ne, const int2* __restrict__ e2n, const double4_32a* __restrict__ w4dw,
-                             const int32_t* __restrict__ a_off, const int32_t* __restrict__ off2,
-                             int32_t* __restrict__ nb2, double4_32a* __restrict__ w2) {
+__global__ void k_dw_table_a(int32_t ne, const int2* __restrict__ e2n, const int32_t* __restrict__ a_off,
+                             const int32_t* __restrict__ off2, int2* __restrict__ ent2) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= ne) return;
   const int2 ab = e2n[e];
-  const int64_t k = off2[ab.x] + (e - a_off[ab.x]);
-  nb2[k] = ab.y;
-  w2[k] = w4dw[e];
+  ent2[off2[ab.x] + (e - a_off[ab.x])] = make_int2(ab.y, (int32_t)e);
 }
 
-// b side: the edge seen from its end b, with h = -w/2 negated (both words'
-// sign bits), so the stage evaluates it with its own node as end a.
-__global__ void k_dw_table_b(int32_t ne, const int2* __restrict__ e2n, const double4_32a* __restrict__ w4dw,
-                             const int32_t* __restrict__ b_list, const int32_t* __restrict__ a_off,
-                             const int32_t* __restrict__ b_off, const int32_t* __restrict__ off2,
-                             int32_t* __restrict__ nb2, double4_32a* __restrict__ w2) {
+// b side: the edge seen from its end b (bit 31 of the edge index set: the
+// stage evaluates it with its own node as end a and h negated).
+__global__ void k_dw_table_b(int32_t ne, const int2* __restrict__ e2n, const int32_t* __restrict__ b_list,
+                             const int32_t* __restrict__ a_off, const int32_t* __restrict__ b_off,
+                             const int32_t* __restrict__ off2, int2* __restrict__ ent2) {
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= ne) return;
   const int32_t e = b_list[j];
-  const int2 ab = e2n[e];
-  const int32_t b = ab.y;
-  const int64_t k = off2[b] + (a_off[b + 1] - a_off[b]) + (j - b_off[b]);
-  const double4_32a w = w4dw[e];
-  const long long flip = (long long)0x8000000080000000ull;
-  nb2[k] = ab.x;
-  w2[k] = make_double4_32a(__longlong_as_double(__double_as_longlong(w.x) ^ flip),
-                           __longlong_as_double(__double_as_longlong(w.y) ^ flip),
-                           __longlong_as_double(__double_as_longlong(w.z) ^ flip), w.w);
+  const int32_t a = e2n[e].x, b = e2n[e].y;
+  ent2[off2[b] + (a_off[b + 1] - a_off[b]) + (j - b_off[b])] = make_int2(a, (int32_t)((uint32_t)e | 0x80000000u));
 }
 
 // The edge weights as pair words (DW precision), once at set-up.
@@ -478,8 +467,8 @@ struct UpdateArgs {
   double* rec2;            // DW: the next stage's primitives as pairs
   const double* rec2_in;   // DW fused: the stage's input primitives
   const int32_t* off2;     // DW fused: per-node neighbour table
-  const int32_t* nb2;
-  const double4_32a* w2;
+  const int2* ent2;
+  const double4_32a* w4dw;
   float* rec32;
   const double* old;
   double* flux;
@@ -742,19 +731,26 @@ __global__ void __launch_bounds__(kNodeThreads, (FUSED && PAIR) ? 10 : (FUSED &&
       for (int k = 0; k < 5; k++) F[k] = PAIR ? f2d_bits(ep_hi[k]) + f2d_bits(ep_lo[k]) : ep_F[k];
     } else if (FUSED && DW) {
       // Node-centric stage in double-word arithmetic: every edge of this node
-      // evaluated with the node as end a (f(b, a; -h) = -f(a, b; h), so the
-      // b-side entries carry -h and need no negation), summed in pairs, and
-      // one FP64 addition per variable at the end.
+      // evaluated with the node as end a (f(b, a; -h) = -f(a, b; h): on the
+      // b side h changes sign), summed in pairs, and one FP64 addition per
+      // variable at the end.  Each edge's weights are read from the edge
+      // list from both ends; the second read mostly hits L2.
       const NodePrimDW me = load_prim_dw(A.rec2_in, i);
       dwacc S[5];
 #pragma unroll
       for (int k = 0; k < 5; k++) S[k] = dwacc{0.0f, 0.0f};
       const int32_t k0 = A.off2[i], k1 = A.off2[i + 1];
       for (int32_t j = k0; j < k1; j++) {
-        const NodePrimDW o = load_prim_dw(A.rec2_in, A.nb2[j]);
-        const double4_32a w = A.w2[j];
+        const int2 en = A.ent2[j];
+        const NodePrimDW o = load_prim_dw(A.rec2_in, en.x);
+        const double4_32a w = A.w4dw[en.y & 0x7fffffff];
+        const uint32_t sg = (uint32_t)en.y & 0x80000000u;  // b side: -h
+        dwf hx = dw_unpack(w.x), hy = dw_unpack(w.y), hz = dw_unpack(w.z);
+        hx = dwf{__uint_as_float(__float_as_uint(hx.h) ^ sg), __uint_as_float(__float_as_uint(hx.l) ^ sg)};
+        hy = dwf{__uint_as_float(__float_as_uint(hy.h) ^ sg), __uint_as_float(__float_as_uint(hy.l) ^ sg)};
+        hz = dwf{__uint_as_float(__float_as_uint(hz.h) ^ sg), __uint_as_float(__float_as_uint(hz.l) ^ sg)};
         dwacc f[5];
-        edge_flux_dw_acc(me, o, dw_unpack(w.x), dw_unpack(w.y), dw_unpack(w.z), dw_unpack(w.w), f);
+        edge_flux_dw_acc(me, o, hx, hy, hz, dw_unpack(w.w), f);
 #pragma unroll
         for (int k = 0; k < 5; k++) acc_add_acc(S[k], f[k], false);
       }
@@ -1226,7 +1222,7 @@ int enqueue_smooth(mgcfd_solver* s, int level) {
     A.seg_rho = s->seg_rho;
     A.seg_stop = seg ? s->seg_stop : nullptr;
     A.e2n = D.e2n; A.w4f = D.w4f; A.b_nbr = D.b_nbr; A.b_w4f = D.b_w4f;
-    A.rec2_in = nullptr; A.off2 = D.off2; A.nb2 = D.nb2; A.w2 = D.w2;
+    A.rec2_in = nullptr; A.off2 = D.off2; A.ent2 = D.ent2; A.w4dw = D.w4dw;
     if (s->fused && dw) {
       // Stage rk reads the primitives of stage rk and writes those of rk + 1
       // into the other buffer: k_step_begin fills rec2 for stage 0.
@@ -1473,13 +1469,12 @@ int build_dw_tables(mgcfd_solver* s, DevLevel& D) {
                                                                 reinterpret_cast<double*>(D.w4dw));
   if (s->fused) {
     if ((r = s->alloc(&D.rec2b, 8 * (size_t)D.n)) || (r = s->alloc(&D.off2, (size_t)D.n + 1)) ||
-        (r = s->alloc(&D.nb2, 2 * (size_t)D.ne)) || (r = s->alloc(&D.w2, 2 * (size_t)D.ne)))
+        (r = s->alloc(&D.ent2, 2 * (size_t)D.ne)))
       return r;
     k_dw_offsets<<<grid((int64_t)D.n + 1, 256), 256, 0, s->stream>>>(D.n, D.a_off, D.b_off, D.off2);
     if (D.ne) {
-      k_dw_table_a<<<grid(D.ne, 256), 256, 0, s->stream>>>(D.ne, D.e2n, D.w4dw, D.a_off, D.off2, D.nb2, D.w2);
-      k_dw_table_b<<<grid(D.ne, 256), 256, 0, s->stream>>>(D.ne, D.e2n, D.w4dw, D.b_list, D.a_off, D.b_off, D.off2,
-                                                           D.nb2, D.w2);
+      k_dw_table_a<<<grid(D.ne, 256), 256, 0, s->stream>>>(D.ne, D.e2n, D.a_off, D.off2, D.ent2);
+      k_dw_table_b<<<grid(D.ne, 256), 256, 0, s->stream>>>(D.ne, D.e2n, D.b_list, D.a_off, D.b_off, D.off2, D.ent2);
     }
   }
   CK(cudaGetLastError());

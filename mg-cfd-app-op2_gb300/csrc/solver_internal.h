@@ -70,9 +70,9 @@ struct DevLevel {
   double* rec2 = nullptr;         // DW: [N][8] node primitives as pair words (dw_math.cuh)
   double4_32a* w4dw = nullptr;    // DW: [E] w4 as pair words
   double* rec2b = nullptr;        // DW fused: second primitive buffer (stages ping-pong)
-  int32_t* off2 = nullptr;        // DW fused: [N+1] each node's entries in nb2/w2 (a_off + b_off)
-  int32_t* nb2 = nullptr;         // DW fused: [2E] a node's neighbours: its a-side edges, then its b-side ones
-  double4_32a* w2 = nullptr;      // DW fused: [2E] their weights as pair words, h negated on the b side
+  int32_t* off2 = nullptr;        // DW fused: [N+1] each node's entries in ent2 (a_off + b_off)
+  int2* ent2 = nullptr;           // DW fused: [2E] a node's a-side edges, then its b-side ones: (neighbour,
+                                  // edge index, bit 31 set on the b side)
   double* fe = nullptr;     // [E][5] per-edge fluxes, FP64 gather
   float* fe32 = nullptr;    // [E][5] per-edge fluxes, mixed-precision gather
   int32_t* a_off = nullptr;
