@@ -38,14 +38,17 @@ def test_config_file_keys(tmp_path):
 
 
 @pytest.mark.gpu
-def test_run_output_and_validate_against_reference_fixture(tmp_path):
+@pytest.mark.parametrize("precision", [[], ["--precision", "dw"]], ids=["fp64", "dw"])
+def test_run_output_and_validate_against_reference_fixture(tmp_path, precision):
     """The driver's --output-variables files match the reference's solution
-    (golden fixture), and -v accepts them as the reference's -v would."""
+    (golden fixture), and -v accepts them as the reference's -v would; the
+    double-word form (--precision dw) at the same bar."""
     z = np.load(GOLDEN / "lattice9_l3_c3.npz")
     meta = json.loads(str(z["meta"]))
     mesh = mgcfd.HostMesh.generate(meta["n"], meta["levels"], meta["seed"])
     mesh.write(str(tmp_path), "m_")
-    args = ["-i", "input.dat", "-d", tmp_path, "-g", meta["cycles"], "--mach", meta["mach"], "--aoa", meta["aoa"]]
+    args = ["-i", "input.dat", "-d", tmp_path, "-g", meta["cycles"], *precision, "--mach", meta["mach"],
+            "--aoa", meta["aoa"]]
     r = cli(*args, "--output-variables", "--output-step-factors", "-o", f"{tmp_path}/solution.")
     assert r.returncode == 0, r.stdout + r.stderr
     assert r.stdout.count("Performing MG cycle") == meta["cycles"] and "Max total runtime" in r.stdout
