@@ -235,7 +235,7 @@ def run_gb300(args):
     mesh = mgcfd.HostMesh.generate(args.n, NLEVELS, SEED)
     L0 = mesh.level(0)
     N, E = L0.nnodes, L0.nedges
-    inc = args.increment if args.increment != "auto" else ("fused" if args.precision == "mixed" else "atomic")
+    inc = args.increment if args.increment != "auto" else ("fused" if args.precision in ("mixed", "dw") else "atomic")
     variant = dict(precision=args.precision, increment=args.increment, renumber=args.renumber,
                    accumulation=args.accumulation, stage_neighbour_ids=args.stage_ids,
                    edge_parallel_stage=args.edge_parallel)
@@ -288,6 +288,17 @@ def run_gb300(args):
     te1 = time.perf_counter()
     barrier()
     e2e_value, e2e_elapsed = replicas.job_throughput(e2e_steps * E2E_CYCLES, te1 - te0, dist, device="cuda")
+    dw_e2e = None
+    if rank == 0 and not args.no_extra_forms:
+        # The same end-to-end step with the double-word form.
+        dopts = mgcfd.options(precision="dw", increment="fused", renumber=args.renumber)
+        _lib.check(lib.mgcfd_solve(len(hl), views, MACH, AOA, 1, C.byref(dopts), out_ptrs))  # warm-up
+        td0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            _lib.check(lib.mgcfd_solve(len(hl), views, MACH, AOA, E2E_CYCLES, C.byref(dopts), out_ptrs))
+        td1 = time.perf_counter()
+        dw_e2e = {"value": round(e2e_steps * E2E_CYCLES / (td1 - td0), 3), "unit": "cycles/s",
+                  "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": e2e_steps}
     del pinned, hl, outs
 
     mixed = dw = served = cpu = None
@@ -295,6 +306,7 @@ def run_gb300(args):
         want = fp64_reference(mesh, stream, MIXED_CYCLES)
         fp64_value = value if args.precision == "fp64" else None
         dw = dw_section(mesh, args, N, E, stream, fp64_value, want)
+        dw["e2e"] = dw_e2e
         mixed = mixed_section(mesh, args, N, E, stream, fp64_value, want)
         served = served_section(args)
     if rank == 0 and not args.no_cpu_baseline:
