@@ -276,6 +276,74 @@ __device__ __forceinline__ void edge_flux_dw(const NodePrimDW& a, const NodePrim
   for (int k = 0; k < 5; k++) f[k] = acc_to_double(F[k]);
 }
 
+// The node-centric sum of edge_flux_dw over one node's edges (the fused DW
+// stage), with the node ("me") as end a of every edge -- its b-side edges
+// taken as f(b, a; -h) = -f(a, b; h).  In
+//   f_rho = rho_a ga + rho_b gb,  f_m = m_a ga + m_b gb + (p_a + p_b) h,
+//   f_E = E_a ga + E_b gb + p_a (u_a.h) + p_b (u_b.h),
+// with ga = u_a.h + fac and gb = u_b.h - fac, the node's own terms factor out
+// of the sum over its edges: sum(ga) = u_me.H + FAC and sum(p_a h) = p_me H,
+// with H = sum(h) and FAC = sum(fac).  So each edge adds only the
+// neighbour's terms and its h and fac to pair accumulators
+// (node_flux_dw_edge), and the node's own terms are added once
+// (node_flux_dw_finish): about 207 FP32 operations per edge instead of the
+// 307 of edge_flux_dw_acc plus the pair sum, and 166 per node.  The same
+// algebra; the roundings differ, within the pairs' 2^-47.
+struct NodeFluxDW {
+  dwacc S[5];             // the node's increments
+  dwacc hx, hy, hz, fac;  // H and FAC
+};
+
+__device__ __forceinline__ void node_flux_dw_init(NodeFluxDW& A) {
+#pragma unroll
+  for (int k = 0; k < 5; k++) A.S[k] = dwacc{0.0f, 0.0f};
+  A.hx = A.hy = A.hz = A.fac = dwacc{0.0f, 0.0f};
+}
+
+__device__ __forceinline__ void node_flux_dw_edge(NodeFluxDW& A, dwf s_me, const NodePrimDW& o, dwf hx, dwf hy,
+                                                  dwf hz, dwf wfac) {
+  const dwf fac = dw_mul(wfac, dw_add(s_me, o.s));
+  dwacc t = acc_prod(o.mx, hx);
+  acc_add_prod(t, o.my, hy);
+  acc_add_prod(t, o.mz, hz);
+  const dwf uhb = dw_mul(acc_dw(t), o.rinv);  // -(u_b . w)/2
+  const dwf gb = dw_add(uhb, dw_neg(fac));
+  acc_add_prod(A.S[0], o.rho, gb);
+  acc_add_prod(A.S[1], o.mx, gb);
+  acc_add_prod(A.S[1], o.p, hx);
+  acc_add_prod(A.S[2], o.my, gb);
+  acc_add_prod(A.S[2], o.p, hy);
+  acc_add_prod(A.S[3], o.mz, gb);
+  acc_add_prod(A.S[3], o.p, hz);
+  acc_add_prod(A.S[4], o.rhoE, gb);
+  acc_add_prod(A.S[4], o.p, uhb);
+  acc_add(A.hx, hx);
+  acc_add(A.hy, hy);
+  acc_add(A.hz, hz);
+  acc_add(A.fac, fac);
+}
+
+// The node's own terms, then the five sums in binary64.
+__device__ __forceinline__ void node_flux_dw_finish(NodeFluxDW& A, const NodePrimDW& me, double F[5]) {
+  const dwf hx = acc_dw(A.hx), hy = acc_dw(A.hy), hz = acc_dw(A.hz);
+  dwacc t = acc_prod(me.mx, hx);
+  acc_add_prod(t, me.my, hy);
+  acc_add_prod(t, me.mz, hz);
+  const dwf uh = dw_mul(acc_dw(t), me.rinv);  // u_me . H
+  const dwf g = dw_add(uh, acc_dw(A.fac));    // sum of ga
+  acc_add_prod(A.S[0], me.rho, g);
+  acc_add_prod(A.S[1], me.mx, g);
+  acc_add_prod(A.S[1], me.p, hx);
+  acc_add_prod(A.S[2], me.my, g);
+  acc_add_prod(A.S[2], me.p, hy);
+  acc_add_prod(A.S[3], me.mz, g);
+  acc_add_prod(A.S[3], me.p, hz);
+  acc_add_prod(A.S[4], me.rhoE, g);
+  acc_add_prod(A.S[4], me.p, uh);
+#pragma unroll
+  for (int k = 0; k < 5; k++) F[k] = acc_to_double(A.S[k]);
+}
+
 // Sum += x, or sum -= x, for accumulators (a node's edge increments).
 __device__ __forceinline__ void acc_add_acc(dwacc& sum, dwacc x, bool neg) {
   const float xs = neg ? -x.s : x.s, xc = neg ? -x.c : x.c;

@@ -730,15 +730,16 @@ __global__ void __launch_bounds__(kNodeThreads, (FUSED && PAIR) ? 10 : (FUSED &&
 #pragma unroll
       for (int k = 0; k < 5; k++) F[k] = PAIR ? f2d_bits(ep_hi[k]) + f2d_bits(ep_lo[k]) : ep_F[k];
     } else if (FUSED && DW) {
-      // Node-centric stage in double-word arithmetic: every edge of this node
-      // evaluated with the node as end a (f(b, a; -h) = -f(a, b; h): on the
-      // b side h changes sign), summed in pairs, and one FP64 addition per
-      // variable at the end.  Each edge's weights are read from the edge
-      // list from both ends; the second read mostly hits L2.
-      const NodePrimDW me = load_prim_dw(A.rec2_in, i);
-      dwacc S[5];
-#pragma unroll
-      for (int k = 0; k < 5; k++) S[k] = dwacc{0.0f, 0.0f};
+      // Node-centric stage in double-word arithmetic: the sum of the fluxes
+      // of this node's edges with the node as end a (f(b, a; -h) = -f(a, b; h):
+      // on the b side h changes sign), in node_flux_dw's factored form, and
+      // one FP64 addition per variable at the end.  Each edge's weights are
+      // read from the edge list from both ends; the second read mostly hits L2.
+      // Only |u|+c of the node is needed in the loop; its other primitives
+      // are loaded for the finish (fewer registers live across the loop).
+      const dwf s_me = dw_unpack(A.rec2_in[8 * i + 6]);
+      NodeFluxDW acc;
+      node_flux_dw_init(acc);
       const int32_t k0 = A.off2[i], k1 = A.off2[i + 1];
       for (int32_t j = k0; j < k1; j++) {
         const int2 en = A.ent2[j];
@@ -749,13 +750,9 @@ __global__ void __launch_bounds__(kNodeThreads, (FUSED && PAIR) ? 10 : (FUSED &&
         hx = dwf{__uint_as_float(__float_as_uint(hx.h) ^ sg), __uint_as_float(__float_as_uint(hx.l) ^ sg)};
         hy = dwf{__uint_as_float(__float_as_uint(hy.h) ^ sg), __uint_as_float(__float_as_uint(hy.l) ^ sg)};
         hz = dwf{__uint_as_float(__float_as_uint(hz.h) ^ sg), __uint_as_float(__float_as_uint(hz.l) ^ sg)};
-        dwacc f[5];
-        edge_flux_dw_acc(me, o, hx, hy, hz, dw_unpack(w.w), f);
-#pragma unroll
-        for (int k = 0; k < 5; k++) acc_add_acc(S[k], f[k], false);
+        node_flux_dw_edge(acc, s_me, o, hx, hy, hz, dw_unpack(w.w));
       }
-#pragma unroll
-      for (int k = 0; k < 5; k++) F[k] = acc_to_double(S[k]);
+      node_flux_dw_finish(acc, load_prim_dw(A.rec2_in, i), F);
     } else if (FUSED) {
       // Node-centric stage: the flux of each edge of this node, computed from
       // the stage's input primitives exactly as k_flux_mixed computes it
