@@ -741,8 +741,10 @@ __global__ void __launch_bounds__(kNodeThreads, (FUSED && PAIR) ? 10 : (FUSED &&
       NodeFluxDW acc;
       node_flux_dw_init(acc);
       const int32_t k0 = A.off2[i], k1 = A.off2[i + 1];
+      int2 next = k0 < k1 ? A.ent2[k0] : make_int2(0, 0);
       for (int32_t j = k0; j < k1; j++) {
-        const int2 en = A.ent2[j];
+        const int2 en = next;  // the following entry loads during this edge's arithmetic
+        if (j + 1 < k1) next = A.ent2[j + 1];
         const NodePrimDW o = load_prim_dw(A.rec2_in, en.x);
         const double4_32a w = A.w4dw[en.y & 0x7fffffff];
         const uint32_t sg = (uint32_t)en.y & 0x80000000u;  // b side: -h
