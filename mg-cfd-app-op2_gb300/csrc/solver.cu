@@ -178,52 +178,47 @@ __global__ void k_init_state(int32_t n, double* __restrict__ rec, double v0, dou
 // first node's id by less than the block size; each mesh of the block gets
 // one shared slot and one global atomic.
 
-// copy_double_kernel + calculate_dt_kernel + get_min_dt_kernel (block part).
-// DW: the primitives go to rec2 as pairs (the edge flux's inputs); rec keeps
-// the state only.
-template <bool MIXED, bool SEG, bool DW = false>
-__global__ void __launch_bounds__(kNodeThreads) k_step_begin(int32_t n, double* __restrict__ rec,
-                                                             double* __restrict__ rec2,
-                                                             float* __restrict__ rec32, double* __restrict__ old,
-                                                             const double* __restrict__ cbrt_vol,
-                                                             unsigned long long* __restrict__ dt_key,
-                                                             const DevStatus* __restrict__ st,
-                                                             const int32_t* __restrict__ mesh_id,
-                                                             const SegStop* __restrict__ seg_stop) {
+// copy_double_kernel + calculate_dt_kernel + get_min_dt_kernel (block part)
+// for node i of a block of kNodeThreads threads whose state x is in hand:
+// old = x, the primitives for the first RK stage, and dt's candidate key into
+// the block's minimum and one atomic per block (per mesh of the block when
+// batched).  Every thread of the block calls it (it synchronises); `live`
+// is false for threads past the end and for stopped meshes.  DW: the
+// primitives go to rec2 as pairs (the edge flux's inputs); rec keeps the
+// state only.
+template <bool MIXED, bool SEG, bool DW>
+__device__ __forceinline__ void step_begin_core(int64_t i, bool live, const double x[5], double* __restrict__ rec,
+                                                double* __restrict__ rec2, float* __restrict__ rec32,
+                                                double* __restrict__ old, const double* __restrict__ cbrt_vol,
+                                                unsigned long long* __restrict__ dt_key,
+                                                const int32_t* __restrict__ mesh_id) {
   __shared__ unsigned long long smin[kNodeThreads / 32];
   __shared__ unsigned int sest[kNodeThreads / 32];
-  __shared__ int s_halt;
   __shared__ unsigned long long s_key[SEG ? kNodeThreads : 1];
-  if (threadIdx.x == 0) s_halt = st->halt;
-  if (SEG) s_key[threadIdx.x] = ~0ull;
-  __syncthreads();
-  if (s_halt) return;  // block-uniform: the reduction below synchronises
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (SEG) {
+    s_key[threadIdx.x] = ~0ull;
+    __syncthreads();
+  }
   // The minimum is taken over order-preserving integer keys of dt, so the
   // reduction issues no FP64 compare; ~0 = no candidate.
   unsigned long long key = ~0ull;
   double cv = 0.0, sp = 1.0;  // FP64: cbrt(vol) and |u| + c of this node
   float est = 0.0f;
-  // Batched solvers under a stop rule: a stopped mesh's nodes change no more.
-  const bool live = i < n && !(SEG && seg_stop && seg_stop[mesh_id[i]].halt);
   if (live) {
-    const double4_32a* r = reinterpret_cast<const double4_32a*>(rec + 8 * i);
-    const double4_32a x = r[0];
-    const double e = r[1].x;
     double* o = old + 5 * i;
-    o[0] = x.x; o[1] = x.y; o[2] = x.z; o[3] = x.w; o[4] = e;
+    o[0] = x[0]; o[1] = x[1]; o[2] = x[2]; o[3] = x[3]; o[4] = x[4];
     if (MIXED) {
       // The spectral radius is edge-flux arithmetic (FP32); min_dt itself
       // is exact in FP64 and the step factor and update stay FP64.
-      const NodePrimF q = store_rec32_from_var(rec32, i, x.x, x.y, x.z, x.w, e);
+      const NodePrimF q = store_rec32_from_var(rec32, i, x[0], x[1], x[2], x[3], x[4]);
       key = dt_candidate_key(f2d_bits(0.5f * (d2f_bits(cbrt_vol[i]) / q.s)));  // time_stepping_kernels.h:31
     } else {
       if (DW) {  // the primitives in double-word arithmetic, no FP64 instruction
-        const NodePrimDW q = node_prim_dw(x.x, x.y, x.z, x.w, e);
+        const NodePrimDW q = node_prim_dw(x[0], x[1], x[2], x[3], x[4]);
         store_prim_dw(rec2, i, q);
         sp = dw_to_double(q.s);
       } else {
-        const NodePrim p = node_prim(x.x, x.y, x.z, x.w, e);
+        const NodePrim p = node_prim(x[0], x[1], x[2], x[3], x[4]);
         store_rec(rec, i, p);
         sp = p.s;
       }
@@ -269,6 +264,32 @@ __global__ void __launch_bounds__(kNodeThreads) k_step_begin(int32_t n, double* 
     if (threadIdx.x == 0 && key != ~0ull && key < *reinterpret_cast<volatile unsigned long long*>(dt_key))
       atomicMin(dt_key, key);
   }
+}
+
+// The step begin on its own (a step that no prolongation precedes).
+template <bool MIXED, bool SEG, bool DW = false>
+__global__ void __launch_bounds__(kNodeThreads) k_step_begin(int32_t n, double* __restrict__ rec,
+                                                             double* __restrict__ rec2,
+                                                             float* __restrict__ rec32, double* __restrict__ old,
+                                                             const double* __restrict__ cbrt_vol,
+                                                             unsigned long long* __restrict__ dt_key,
+                                                             const DevStatus* __restrict__ st,
+                                                             const int32_t* __restrict__ mesh_id,
+                                                             const SegStop* __restrict__ seg_stop) {
+  __shared__ int s_halt;
+  if (threadIdx.x == 0) s_halt = st->halt;
+  __syncthreads();
+  if (s_halt) return;  // block-uniform: the reduction below synchronises
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  // Batched solvers under a stop rule: a stopped mesh's nodes change no more.
+  const bool live = i < n && !(SEG && seg_stop && seg_stop[mesh_id[i]].halt);
+  double x[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  if (live) {
+    const double4_32a* r = reinterpret_cast<const double4_32a*>(rec + 8 * i);
+    const double4_32a v = r[0];
+    x[0] = v.x; x[1] = v.y; x[2] = v.z; x[3] = v.w; x[4] = r[1].x;
+  }
+  step_begin_core<MIXED, SEG, DW>(i, live, x, rec, rec2, rec32, old, cbrt_vol, dt_key, mesh_id);
 }
 
 // compute_flux_edge_kernel (flux.h:41-208), FP64, both ends by FP64 atomics
@@ -959,30 +980,51 @@ __global__ void __launch_bounds__(kNodeThreads) k_restrict(int32_t nc, const int
   block_norms(srms, srho, sbad, ((q[0] + q[1]) + (q[2] + q[3])) + q[4], q[0], bad, st);
 }
 
-// down_kernel (mg.h:66-88) with the parent offsets precomputed.
-__global__ void k_prolong(int32_t nf, const int32_t* __restrict__ n2mg, const double4_32a* __restrict__ dvec,
-                          double* __restrict__ frec, const double* __restrict__ fres,
-                          const double* __restrict__ cres, const DevStatus* __restrict__ st,
-                          const int32_t* __restrict__ mesh_id, const SegStop* __restrict__ seg_stop) {
-  if (st->halt) return;
+// The fine level's step-begin arrays, for a prolongation that begins its
+// next smoothing step.
+struct BeginArgs {
+  double* rec2;
+  float* rec32;
+  double* old;
+  const double* cbrt_vol;
+  unsigned long long* dt_key;
+};
+
+// down_kernel (mg.h:66-88) with the parent offsets precomputed.  BEGIN: the
+// fine level's next smoothing step begins here (step_begin_core on the new
+// state while it is in registers) instead of in a separate pass that reads
+// the level's state again; every thread reaches the block reduction.
+template <bool BEGIN, bool MIXED, bool SEG, bool DW>
+__global__ void __launch_bounds__(kNodeThreads) k_prolong(int32_t nf, const int32_t* __restrict__ n2mg,
+                                                          const double4_32a* __restrict__ dvec,
+                                                          double* __restrict__ frec, const double* __restrict__ fres,
+                                                          const double* __restrict__ cres,
+                                                          const DevStatus* __restrict__ st,
+                                                          const int32_t* __restrict__ mesh_id,
+                                                          const SegStop* __restrict__ seg_stop, BeginArgs B) {
+  if (st->halt) return;  // the same for every thread of the launch
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nf) return;
-  if (seg_stop && seg_stop[mesh_id[i]].halt) return;  // a stopped mesh of a batch
-  const int64_t c = n2mg[i];
-  const double4_32a d = dvec[i];
-  // The record's first four values as one 32-byte access, the fifth alone.
-  double4_32a* r4 = reinterpret_cast<double4_32a*>(frec + 8 * i);
-  double4_32a x = r4[0];
-  double x4 = frec[8 * i + 4];
-  const double* cr = cres + 5 * c;
-  const double* fr = fres + 5 * i;
-  x.x -= d.w * (cr[0] - fr[0]);
-  x.y -= d.x * (cr[1] - fr[1]);
-  x.z -= d.y * (cr[2] - fr[2]);
-  x.w -= d.z * (cr[3] - fr[3]);
-  x4 -= d.w * (cr[4] - fr[4]);
-  r4[0] = x;
-  frec[8 * i + 4] = x4;
+  const bool live = i < nf && !(seg_stop && seg_stop[mesh_id[i]].halt);  // not a stopped mesh of a batch
+  double x[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  if (live) {
+    const int64_t c = n2mg[i];
+    const double4_32a d = dvec[i];
+    // The record's first four values as one 32-byte access, the fifth alone.
+    double4_32a* r4 = reinterpret_cast<double4_32a*>(frec + 8 * i);
+    double4_32a v = r4[0];
+    double v4 = frec[8 * i + 4];
+    const double* cr = cres + 5 * c;
+    const double* fr = fres + 5 * i;
+    v.x -= d.w * (cr[0] - fr[0]);
+    v.y -= d.x * (cr[1] - fr[1]);
+    v.z -= d.y * (cr[2] - fr[2]);
+    v.w -= d.z * (cr[3] - fr[3]);
+    v4 -= d.w * (cr[4] - fr[4]);
+    r4[0] = v;
+    frec[8 * i + 4] = v4;
+    x[0] = v.x; x[1] = v.y; x[2] = v.z; x[3] = v.w; x[4] = v4;
+  }
+  if (BEGIN) step_begin_core<MIXED, SEG, DW>(i, live, x, frec, B.rec2, B.rec32, B.old, B.cbrt_vol, B.dt_key, mesh_id);
 }
 
 // Far-field terms w.F_ff of every folded boundary row for a new freestream
@@ -1141,6 +1183,33 @@ using StepFn = void (*)(const DevLevel&, unsigned long long*, const DevStatus*, 
 const StepFn kStepBegin[6] = {launch_step_begin<0, 0>, launch_step_begin<0, 1>, launch_step_begin<1, 0>,
                               launch_step_begin<1, 1>, launch_step_begin<0, 0, 1>, launch_step_begin<0, 1, 1>};
 
+// The level's min_dt key and, after a step, the copy of the key it used
+// (for the step factors a fetch reports).
+unsigned long long* level_key(mgcfd_solver* s, int level) {
+  return s->nseg > 1 ? s->seg_keys + (size_t)level * s->nseg : &s->st->dt_key[level];
+}
+unsigned long long* level_key_used(mgcfd_solver* s, int level) {
+  return s->nseg > 1 ? s->seg_keys + ((size_t)kMaxLevels + level) * s->nseg : &s->st->dt_key_used[level];
+}
+
+template <bool B, bool M, bool S, bool W>
+void launch_prolong(const DevLevel& F, const DevLevel& Cl, const DevStatus* st, const SegStop* ss,
+                    unsigned long long* key, cudaStream_t stream) {
+  const BeginArgs b{F.rec2, F.rec32, F.old, F.cbrt_vol, key};
+  k_prolong<B, M, S, W><<<grid(F.n, kNodeThreads), kNodeThreads, 0, stream>>>(F.n, F.n2mg, F.dvec, F.rec, F.res,
+                                                                               Cl.res, st, F.mesh_id, ss, b);
+}
+using ProlongFn = void (*)(const DevLevel&, const DevLevel&, const DevStatus*, const SegStop*, unsigned long long*,
+                           cudaStream_t);
+// With the fine level's step begin, indexed by precision (FP64, MIXED, DW) * 2 + seg.
+const ProlongFn kProlongBegin[6] = {launch_prolong<1, 0, 0, 0>, launch_prolong<1, 0, 1, 0>,
+                                   launch_prolong<1, 1, 0, 0>, launch_prolong<1, 1, 1, 0>,
+                                   launch_prolong<1, 0, 0, 1>, launch_prolong<1, 0, 1, 1>};
+
+int precision_index(const mgcfd_solver* s) {
+  return s->opt.precision == MGCFD_PRECISION_DW ? 2 : s->opt.precision == MGCFD_PRECISION_MIXED ? 1 : 0;
+}
+
 // Where the level-0 norms (calc_rms_kernel, count_bad_vals) are taken: in
 // the last RK stage, or -- for plain multi-level solvers with the fused
 // stage, whose warps finish at uneven times and idle at the stage's block
@@ -1156,8 +1225,13 @@ int enqueue_smooth(mgcfd_solver* s, int level) {
   const bool dw = s->opt.precision == MGCFD_PRECISION_DW;
   const bool timing = s->opt.time_kernels && level == 0;
   const bool seg = s->nseg > 1;
-  unsigned long long* key = seg ? s->seg_keys + (size_t)level * s->nseg : &s->st->dt_key[level];
-  CK(cudaMemsetAsync(key, 0xff, sizeof(unsigned long long) * (size_t)s->nseg, s->stream));
+  unsigned long long* key = level_key(s, level);
+  if (!s->begun) {  // no prolongation began this step: its own begin pass
+    CK(cudaMemsetAsync(key, 0xff, sizeof(unsigned long long) * (size_t)s->nseg, s->stream));
+    kStepBegin[2 * precision_index(s) + (seg ? 1 : 0)](D, key, s->st, seg ? s->seg_stop : nullptr, s->stream);
+    s->launches++;
+  }
+  s->begun = false;
   if (level == 0) {
     CK(cudaMemsetAsync(&s->st->rms_acc, 0, 2 * sizeof(double), s->stream));  // rms_acc, rho_acc
     if (seg) {
@@ -1165,8 +1239,6 @@ int enqueue_smooth(mgcfd_solver* s, int level) {
       CK(cudaMemsetAsync(s->seg_rho, 0, sizeof(double) * (size_t)s->nseg, s->stream));
     }
   }
-  kStepBegin[(dw ? 4 : mixed ? 2 : 0) | (seg ? 1 : 0)](D, key, s->st, seg ? s->seg_stop : nullptr, s->stream);
-  s->launches++;
   const int et = edge_threads(s);
   const bool pair = mixed && s->opt.accumulation == MGCFD_ACCUM_PAIR32;
   for (int rk = 0; rk < kRK; rk++) {
@@ -1260,6 +1332,10 @@ int enqueue_smooth(mgcfd_solver* s, int level) {
       s->launches++;
     }
   }
+  // The key this step used, for the step factors a fetch reports (a
+  // prolongation may begin this level's next step before the fetch).
+  CK(cudaMemcpyAsync(level_key_used(s, level), key, sizeof(unsigned long long) * (size_t)s->nseg,
+                     cudaMemcpyDeviceToDevice, s->stream));
   CK(cudaGetLastError());
   s->steps++;
   return MGCFD_OK;
@@ -1290,8 +1366,12 @@ int enqueue_iteration(mgcfd_solver* s) {
     s->level--;
     DevLevel& F = s->L[(size_t)s->level];
     DevLevel& Cl = s->L[(size_t)s->level + 1];
-    k_prolong<<<grid(F.n, kNodeThreads), kNodeThreads, 0, s->stream>>>(F.n, F.n2mg, F.dvec, F.rec, F.res, Cl.res, s->st,
-                                                                       F.mesh_id, s->nseg > 1 ? s->seg_stop : nullptr);
+    // The fine level's next smoothing step begins in the prolongation.
+    unsigned long long* key = level_key(s, s->level);
+    CK(cudaMemsetAsync(key, 0xff, sizeof(unsigned long long) * (size_t)s->nseg, s->stream));
+    kProlongBegin[2 * precision_index(s) + (s->nseg > 1 ? 1 : 0)](F, Cl, s->st, s->nseg > 1 ? s->seg_stop : nullptr,
+                                                                   key, s->stream);
+    s->begun = true;
     s->launches++;
     if (s->level == 0) {
       s->up = true;
@@ -1376,9 +1456,10 @@ int init_state(mgcfd_solver* s) {
   }
   CK(cudaMemsetAsync(s->st, 0, sizeof(DevStatus), s->stream));
   CK(cudaMemsetAsync(s->st->dt_key, 0xff, sizeof(s->st->dt_key), s->stream));
+  CK(cudaMemsetAsync(s->st->dt_key_used, 0xff, sizeof(s->st->dt_key_used), s->stream));
   if (s->nseg > 1) {
     const size_t ns = (size_t)s->nseg;
-    CK(cudaMemsetAsync(s->seg_keys, 0xff, sizeof(unsigned long long) * kMaxLevels * ns, s->stream));
+    CK(cudaMemsetAsync(s->seg_keys, 0xff, sizeof(unsigned long long) * 2 * kMaxLevels * ns, s->stream));
     CK(cudaMemsetAsync(s->seg_neg, 0, sizeof(int) * ns, s->stream));
     CK(cudaMemsetAsync(s->seg_bad, 0, sizeof(int) * ns, s->stream));
     CK(cudaMemsetAsync(s->seg_rms, 0, sizeof(double) * ns, s->stream));
@@ -1386,6 +1467,13 @@ int init_state(mgcfd_solver* s) {
     if (s->seg_stop) CK(cudaMemsetAsync(s->seg_stop, 0, sizeof(SegStop) * ns, s->stream));
   }
   s->seg_status.assign((size_t)s->nseg, MGCFD_OK);
+  // The first V-cycle's first step begins here; every later V-cycle's
+  // begins in the prolongation that ends the one before, so every V-cycle
+  // (and the captured graph) has the same launches.  A one-level solver has
+  // no prolongation: each of its steps begins on its own.
+  s->begun = s->L.size() > 1;
+  if (s->begun)
+    kStepBegin[2 * precision_index(s) + (s->nseg > 1 ? 1 : 0)](s->L[0], level_key(s, 0), s->st, nullptr, s->stream);
   CK(cudaGetLastError());
   s->cycle = 0; s->level = 0; s->up = true; s->steps = 0; s->launches = 0;
   s->flux_ms = 0.0; s->flux_sweeps = 0; s->status = MGCFD_OK;
@@ -1667,7 +1755,7 @@ extern "C" int mgcfd_batch_create(int32_t nmeshes, int32_t nlevels, const mgcfd_
   for (auto& D : s->L) max_n = std::max(max_n, (size_t)D.n);
   const size_t ns = (size_t)nmeshes;
   if ((r = s->alloc(&s->st, 1)) || (r = s->alloc(&s->fetch_buf, 5 * max_n)) ||
-      (r = s->alloc(&s->seg_keys, kMaxLevels * ns)) || (r = s->alloc(&s->seg_neg, ns)) ||
+      (r = s->alloc(&s->seg_keys, 2 * kMaxLevels * ns)) || (r = s->alloc(&s->seg_neg, ns)) ||
       (r = s->alloc(&s->seg_bad, ns)) || (r = s->alloc(&s->seg_rms, ns)) || (r = s->alloc(&s->seg_rho, ns)) ||
       (r = s->upload(&s->seg_ffvar, ffvar.data(), 5 * ns)))
     return r;
@@ -1783,7 +1871,7 @@ int fetch_rows(mgcfd_solver* s, int32_t level, int32_t q, int32_t off, int32_t n
   DevLevel& D = s->L[(size_t)level];
   const int T = 256;
   int width = 5;
-  const unsigned long long* keys = s->nseg > 1 ? s->seg_keys + (size_t)level * s->nseg : &s->st->dt_key[level];
+  const unsigned long long* keys = level_key_used(s, level);
   switch (q) {
     case MGCFD_Q_VARIABLES:
       k_unpermute<<<grid((int64_t)n * 5, T), T, 0, s->stream>>>(n, off, 5, 8, D.rec, D.perm, s->fetch_buf);

@@ -23,7 +23,9 @@ constexpr int kMaxDevices = 64;
   } while (0)
 
 struct DevStatus {
-  unsigned long long dt_key[kMaxLevels];  // order-preserving key of each level's last min_dt
+  unsigned long long dt_key[kMaxLevels];  // order-preserving key of each level's min_dt (the step
+                                           // begun last: a prolongation begins its fine level's next step)
+  unsigned long long dt_key_used[kMaxLevels];  // the key each level's last finished step used
   int halt;                                // non-zero: stop all further work
   int neg_dt;                              // min_dt < 0 seen
   int bad_count;                           // NaN/Inf count at level 0
@@ -106,7 +108,7 @@ struct mgcfd_solver {
   int nseg = 1;
   std::vector<std::vector<int32_t>> seg_noff;    // [level][nseg + 1] node offsets
   std::vector<mgcfd_freestream> seg_ff;          // per mesh
-  unsigned long long* seg_keys = nullptr;        // [kMaxLevels][nseg] min_dt keys
+  unsigned long long* seg_keys = nullptr;        // [2][kMaxLevels][nseg] min_dt keys, then the keys used
   int* seg_neg = nullptr;                        // [nseg] min_dt < 0 seen
   int* seg_bad = nullptr;                        // [nseg] NaN/Inf count at level 0
   double* seg_rms = nullptr;                     // [nseg] sum of residual^2, last level-0 step
@@ -122,6 +124,7 @@ struct mgcfd_solver {
   int64_t steps = 0;
   int64_t launches = 0;
   int64_t launches_per_cycle = 0;
+  bool begun = false;   // the next smoothing step's begin is already enqueued (by a prolongation or set-up)
   bool gather = false;  // node-side CSR tables exist (GATHER or FUSED)
   bool fused = false;   // FUSED: flux and update in one node-centric kernel
   bool coloured = false;  // COLOURED: one flux launch per colour class, plain increments
