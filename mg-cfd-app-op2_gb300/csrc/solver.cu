@@ -22,6 +22,9 @@
 // Kernels per smoothing step (euler3d.cpp:467-550):
 //   memset(min_dt key)                      get_min_dt's DBL_MAX start
 //   k_step_begin   nodes  old = var, primitives, dt, block min -> atomicMin
+//                         (a step that a prolongation precedes -- every
+//                         level-0 step after the first -- begins inside
+//                         k_prolong instead, on the state it just wrote)
 //   3 x { k_flux   edges  edge flux, +f to a and -f to b (FP64 atomics) or
 //                         f stored per edge (gather strategy)
 //         k_update nodes  gathered flux + boundary flux, time step, flux = 0,
