@@ -274,8 +274,9 @@ int mgcfd_op_count_differences(int32_t nnodes, const double* test, const double*
  * (each value an unevaluated pair of binary32 numbers, 48 significand bits,
  * built from error-free TwoSum / TwoProd steps), with the primitives and the
  * edge weights stored as such pairs.  Within the same 1e-10 relative bar of
- * the FP64 reference as FP64; the exponent range of the pairs is binary32's.
- * DW takes the FUSED (AUTO), ATOMIC or GATHER increment. */
+ * the FP64 reference as FP64; the exponent range of the pairs is binary32's,
+ * and set-up refuses (MGCFD_ERR_INVALID) a mesh with edge weights outside
+ * [2^-70, 2^70).  DW takes the FUSED (AUTO), ATOMIC or GATHER increment. */
 enum { MGCFD_PRECISION_FP64 = 0, MGCFD_PRECISION_MIXED = 1, MGCFD_PRECISION_DW = 2 };
 /* How the edge fluxes reach the nodes.  ATOMIC: each edge adds +f / -f to its
  * end nodes with FP64 atomics.  GATHER: each edge stores f, then each node

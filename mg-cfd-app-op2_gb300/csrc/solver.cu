@@ -384,10 +384,18 @@ __global__ void k_dw_table_b(int32_t ne, const int2* __restrict__ e2n, const int
   ent2[off2[b] + (a_off[b + 1] - a_off[b]) + (j - b_off[b])] = make_int2(a, (int32_t)((uint32_t)e | 0x80000000u));
 }
 
-// The edge weights as pair words (DW precision), once at set-up.
-__global__ void k_split_weights(int64_t n, const double* __restrict__ w, double* __restrict__ w2) {
+// The edge weights as pair words (DW precision), once at set-up, counting
+// the finite non-zero weights outside [2^-70, 2^70): their products with the
+// flow state would leave the pairs' binary32 exponent range.
+__global__ void k_split_weights(int64_t n, const double* __restrict__ w, double* __restrict__ w2,
+                                unsigned int* __restrict__ out_of_range) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < n) w2[k] = dw_pack(dw_split(w[k]));
+  if (k >= n) return;
+  const double v = w[k];
+  w2[k] = dw_pack(dw_split(v));
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+  const int e = (int)(b >> 52) - 1023;
+  if (b != 0 && b < 0x7ff0000000000000ull && (e < -70 || e >= 70)) atomicAdd(out_of_range, 1u);
 }
 
 // compute_flux_edge_kernel over one colour class: no two of these edges share
@@ -1555,8 +1563,20 @@ int build_dw_tables(mgcfd_solver* s, DevLevel& D) {
   int r;
   if ((r = s->alloc(&D.rec2, 8 * (size_t)D.n)) || (r = s->alloc(&D.w4dw, (size_t)D.ne))) return r;
   const int64_t nw = 4 * (int64_t)D.ne;
-  if (nw) k_split_weights<<<grid(nw, 256), 256, 0, s->stream>>>(nw, reinterpret_cast<const double*>(D.w4),
-                                                                reinterpret_cast<double*>(D.w4dw));
+  if (nw) {
+    unsigned int* bad = nullptr;
+    unsigned int nbad = 0;
+    CK(cudaMallocAsync(&bad, sizeof(unsigned int), s->stream));
+    CK(cudaMemsetAsync(bad, 0, sizeof(unsigned int), s->stream));
+    k_split_weights<<<grid(nw, 256), 256, 0, s->stream>>>(nw, reinterpret_cast<const double*>(D.w4),
+                                                          reinterpret_cast<double*>(D.w4dw), bad);
+    CK(cudaMemcpyAsync(&nbad, bad, sizeof(unsigned int), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaFreeAsync(bad, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    if (nbad)
+      return set_error(MGCFD_ERR_INVALID, std::to_string(nbad) + " edge weight components outside the DW form's "
+                                          "range [2^-70, 2^70); use FP64 precision for this mesh");
+  }
   if (s->fused) {
     if ((r = s->alloc(&D.rec2b, 8 * (size_t)D.n)) || (r = s->alloc(&D.off2, (size_t)D.n + 1)) ||
         (r = s->alloc(&D.ent2, 2 * (size_t)D.ne)))

@@ -257,3 +257,17 @@ def test_dw_nan_weight_reports_bad_values(increment):
     assert s.synchronize() == mgcfd._lib.ERR_BAD_VALUES
     with pytest.raises(mgcfd._lib.MgcfdError):
         s.run(1)
+
+
+def test_dw_refuses_weights_outside_its_range():
+    """The pairs have binary32's exponent range: edge weights below 2^-70 (or
+    at and above 2^70) are refused at set-up; FP64 takes the same mesh."""
+    mesh = mgcfd.HostMesh.generate(8, 2, 3)
+    scaled = [mgcfd.Level(**{k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in L.__dict__.items()
+                             if k != "owner"}) for L in mesh.levels()]
+    scaled[1].edge_weights *= 2.0 ** -80
+    with pytest.raises(mgcfd._lib.MgcfdError, match="range"):
+        mgcfd.Solver(scaled, 0.5, 3.0, precision="dw")
+    s = mgcfd.Solver(scaled, 0.5, 3.0)
+    s.close()
+    mgcfd.Solver(mesh, 0.5, 3.0, precision="dw").close()  # the unscaled mesh is fine
