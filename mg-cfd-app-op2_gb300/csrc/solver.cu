@@ -870,13 +870,7 @@ __global__ void __launch_bounds__(kNodeThreads, (FUSED && PAIR) ? 10 : (FUSED &&
     }
     if (bi >= 0) {
       NodePrim p;
-      if (FUSED && DW) {
-        // The stage's input primitives (pair words) in binary64: the fused
-        // DW stages keep no FP64 state between stages (see below).
-        const NodePrimDW q = load_prim_dw(A.rec2_in, i);
-        p = NodePrim{dw_to_double(q.rho), dw_to_double(q.mx), dw_to_double(q.my), dw_to_double(q.mz),
-                     dw_to_double(q.rhoE), dw_to_double(q.p), dw_to_double(q.s), dw_to_double(q.rinv)};
-      } else if (MIXED || DW) {
+      if (MIXED || DW) {
         const double4_32a* r = reinterpret_cast<const double4_32a*>(A.rec + 8 * i);
         const double4_32a x = r[0];
         p = node_prim(x.x, x.y, x.z, x.w, r[1].x);
@@ -909,14 +903,19 @@ __global__ void __launch_bounds__(kNodeThreads, (FUSED && PAIR) ? 10 : (FUSED &&
         rr = d[0] * d[0];
       }
     } else if (MIXED) {
-      double4_32a* r = reinterpret_cast<double4_32a*>(A.rec + 8 * i);
-      r[0] = make_double4_32a(v[0], v[1], v[2], v[3]);
-      A.rec[8 * i + 4] = v[4];
+      // The fused stages read the next stage's state through its FP32
+      // primitives; only a boundary node's FP64 state is read (for its
+      // boundary flux) before the last stage writes every node's.
+      if (!FUSED || bi >= 0) {
+        double4_32a* r = reinterpret_cast<double4_32a*>(A.rec + 8 * i);
+        r[0] = make_double4_32a(v[0], v[1], v[2], v[3]);
+        A.rec[8 * i + 4] = v[4];
+      }
       store_rec32_from_var(A.rec32, i, v[0], v[1], v[2], v[3], v[4]);
     } else if (DW) {
-      // The fused stages read the next stage's state only through its
-      // primitives, so only the last stage writes the FP64 state.
-      if (!FUSED) {
+      // As for MIXED: the fused stages write the FP64 state of boundary
+      // nodes only; the last stage writes every node's.
+      if (!FUSED || bi >= 0) {
         double4_32a* r = reinterpret_cast<double4_32a*>(A.rec + 8 * i);
         r[0] = make_double4_32a(v[0], v[1], v[2], v[3]);
         A.rec[8 * i + 4] = v[4];
