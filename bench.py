@@ -53,22 +53,27 @@ def algorithmic_flux_bytes(nnodes: int, nedges: int, precision: str = "fp64", in
     plus the map and the read half of the increment).
     Mixed, edge kernel: 16 B FP32 weights + 8 B map read and 20 B FP32 edge
     flux written per edge; 32 B FP32 primitives read per node.
-    Mixed, fused stage (flux and time step in one node kernel): per edge the
-    a-side weights + map (24 B) and the b-side copies (20 B); per node the
-    FP32 primitives read (32 B), old state (40 B), 1/vol, boundary index and
-    CSR offsets (20 B), state written (40 B) and next primitives written (32 B).
+    Mixed, fused stage (flux and time step in one node kernel), the mean over
+    a step's three stages: per edge the a-side weights + map (24 B) and the
+    b-side copies (20 B); per node the FP32 primitives read (32 B), old state
+    (40 B), 1/vol, boundary index and CSR offsets (20 B), then in the first two
+    stages the next primitives written (32 B; the state is written for boundary
+    nodes only) and in the last the state and the residual written (80 B):
+    124 and 172 B, 140 B per node on average.
     DW (double-word flux): 32 B weights as pair words + 8 B map per edge; 64 B
     primitives as pair words read, 40 B flux read and 40 B written per node.
-    DW, fused stage: per edge both ends' table entries (neighbour and edge
-    index, 2 x 8 B) and the weights as pair words (32 B); per node the
-    primitives read (64 B), old state (40 B), 1/vol, boundary index and table
-    offset (16 B), state written (40 B) and next primitives written (64 B)."""
+    DW, fused stage, the mean over a step's three stages: per edge both ends'
+    table entries (neighbour and edge index, 2 x 8 B) and the weights as pair
+    words (32 B); per node the primitives read (64 B), old state (40 B), 1/vol,
+    boundary index and table offset (16 B), then the next primitives written
+    (64 B) in the first two stages and the state and residual (80 B) in the
+    last: 184 and 200 B, 568/3 B per node on average."""
     if precision == "dw" and increment == "fused":
-        return 48 * nedges + 224 * nnodes
+        return 48 * nedges + (568 * nnodes) // 3
     if precision == "dw":
         return 40 * nedges + 144 * nnodes
     if precision == "mixed" and increment == "fused":
-        return 44 * nedges + 164 * nnodes
+        return 44 * nedges + 140 * nnodes
     if precision == "mixed":
         return 44 * nedges + 32 * nnodes
     return 32 * nedges + 120 * nnodes
