@@ -810,6 +810,9 @@ def run_loops(args):
                   plan keeps the caller's order
       plan_free   file order with plans off (the naive per-loop kernels), a
                   few cycles, for contrast
+      *_dw        the same with the flux calls in the DW form
+                  (mgcfd_op_flux_precision: double-word primitives and fluxes
+                  through the plans, node-centric, no atomics)
     V-cycles/s from CUDA events on the driver's stream; the level-0 edge-flux
     call (primitives, flux, scatter) timed alone with events; the first cycle
     (upload, set-up loops, plan builds) reported separately; the final state
@@ -837,11 +840,14 @@ def run_loops(args):
     solver_value = args.steps / secs
     ref.close()
     peak, peak_kind = measured_peaks()
-    forms = {"file_order": ("auto", mesh), "renumbered": ("auto", mesh.renumber("spatial"))}
+    renumbered = mesh.renumber("spatial")
+    forms = {"file_order": ("auto", mesh, "fp64"), "renumbered": ("auto", renumbered, "fp64"),
+             "file_order_dw": ("auto", mesh, "dw"), "renumbered_dw": ("auto", renumbered, "dw")}
     out = {}
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as sampler:
-        for name, (mode, m) in forms.items():
+        for name, (mode, m, prec) in forms.items():
             ops.plans_mode(mode)
+            ops.flux_precision(prec)
             t0 = time.perf_counter()
             s = mgcfd.LoopSolver(m, MACH, AOA, stream=stream)
             s.run(1)
@@ -855,7 +861,7 @@ def run_loops(args):
             st, rms = s.synchronize()
             secs = e0.elapsed_time(e1) * 1e-3
             got = s.fetch(0)
-            if name == "renumbered":  # back to the file order of the reference solution
+            if name.startswith("renumbered"):  # back to the file order of the reference solution
                 perm = np.empty(N, np.int64)
                 perm[:] = mgcfd.renumber_nodes("spatial", L0.coords)
                 back = np.empty_like(got)
@@ -873,6 +879,8 @@ def run_loops(args):
             flux_ms = e0.elapsed_time(e1) / reps
             info = ops.plans_info()
             s.close()
+            ops.plans_release()  # each form builds its own plans
+            ops.flux_precision("fp64")
             byt = algorithmic_flux_bytes(N, E)
             out[name] = {"value": round(args.steps / secs, 3), "unit": "cycles/s", "status": st,
                          "first_cycle_s": round(first, 3), "plans": info,
@@ -895,7 +903,7 @@ def run_loops(args):
         s.close()
         ops.plans_mode("auto")
     solver_flux_ms = kernel_times(mesh, args.kernel_cycles)
-    for name in ("file_order", "renumbered"):
+    for name in ("file_order", "renumbered", "file_order_dw", "renumbered_dw"):
         out[name]["flux_call_vs_solver_flux"] = round(out[name]["flux_call_ms"] / solver_flux_ms, 3)
     line = {"metric": "MG V-cycles/s at 8M nodes through the per-loop entry points (OP2 dat layout)",
             "unit": "cycles/s", "higher_is_better": True, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,

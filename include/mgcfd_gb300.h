@@ -255,6 +255,16 @@ int mgcfd_op_plans_mode(int32_t mode);
 int mgcfd_op_plan_release(const void* map);
 int mgcfd_op_plans_release(void);
 int mgcfd_op_plans_info(int64_t* edge_plans, int64_t* child_plans, int64_t* reordered, int64_t* device_bytes);
+/* Arithmetic of mgcfd_op_compute_flux_edge calls that run through a plan:
+ * MGCFD_PRECISION_FP64 (the default) or MGCFD_PRECISION_DW, the solver's
+ * double-word form (see the solver section).  DW: the primitives and the edge
+ * fluxes in float-float pairs on the FP32 pipes; each node sums its edges'
+ * fluxes in pairs and adds the total to its row of fluxes once in FP64 -- no
+ * atomics, the same bits on every call -- within the FP64 bar of the
+ * reference (1e-10).  The pairs have binary32's exponent range: weights
+ * should lie in [2^-70, 2^70).  Plan-free calls stay FP64.  Process-wide,
+ * like mgcfd_op_plans_mode; other precisions are refused. */
+int mgcfd_op_flux_precision(int32_t precision);
 /* Number of elements the mapped entry points above skipped because a map
  * entry was outside [0, set size) since the last reset; reset != 0 zeroes the
  * counter.  Reads a device counter: call after the streams used are idle. */

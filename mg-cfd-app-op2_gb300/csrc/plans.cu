@@ -47,6 +47,7 @@
 #include <cub/cub.cuh>
 
 #include <algorithm>
+#include <atomic>
 #include <climits>
 #include <cmath>
 #include <map>
@@ -57,6 +58,7 @@
 
 #include "common.h"
 #include "device_math.cuh"
+#include "dw_math.cuh"
 #include "plans.h"
 #include "solver_internal.h"
 
@@ -75,6 +77,16 @@ struct EdgePlan {
   double memo_sc = NAN;     // smoothing coefficient of the memo (NaN: never used)
   double* rec = nullptr;    // [nn][8] state + primitives, internal order
   double* fl = nullptr;     // [nn][5] internal increments (permuted only)
+  // DW form (built on the first call with DW flux precision): each internal
+  // node's entries -- its a-side edges, then its b-side ones -- a memo of its
+  // own and the pair-word buffers.
+  bool dw_built = false;
+  int32_t* off2 = nullptr;          // [nn + 1] each node's entries in ent2
+  int2* ent2 = nullptr;             // [2 nvalid] (neighbour, edge; bit 31 set on the b side)
+  double4_32a* memo2 = nullptr;     // [nvalid] (h, wfac) of the last weight a DW call saw
+  double4_32a* memo_dw = nullptr;   // [nvalid] the same as pair words
+  double memo2_sc = NAN;
+  double* rec2 = nullptr;           // [nn][8] pair-word primitives, internal order
   int64_t bytes = 0;
 };
 
@@ -372,6 +384,122 @@ __global__ void k_plan_gather(int64_t n5, const int32_t* __restrict__ pos, const
   flux[j] += fl[5 * (int64_t)pos[c] + (j - 5 * c)];
 }
 
+// ---- edge plan, DW form ---------------------------------------------------------
+
+__global__ void k_count_ends(int32_t nv, const int2* __restrict__ e2n, int32_t* __restrict__ cnt_a,
+                             int32_t* __restrict__ cnt_b) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nv) return;
+  const int2 ab = e2n[e];
+  atomicAdd(cnt_a + ab.x, 1);
+  atomicAdd(cnt_b + ab.y, 1);
+}
+
+__global__ void k_b_keys(int32_t nv, const int2* __restrict__ e2n, uint32_t* __restrict__ key,
+                         int32_t* __restrict__ val) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nv) return;
+  key[e] = (uint32_t)e2n[e].y;
+  val[e] = (int32_t)e;
+}
+
+__global__ void k_off2(int32_t nn, const int32_t* __restrict__ a_off, const int32_t* __restrict__ b_off,
+                       int32_t* __restrict__ off2) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i <= nn) off2[i] = a_off[i] + b_off[i];
+}
+
+// Node a's entries start at a_off[a] + b_off[a]; the edges are sorted by a,
+// so edge e is its (e - a_off[a])-th a-side entry.
+__global__ void k_ent_a(int32_t nv, const int2* __restrict__ e2n, const int32_t* __restrict__ a_off,
+                        const int32_t* __restrict__ b_off, int2* __restrict__ ent2) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nv) return;
+  const int2 ab = e2n[e];
+  ent2[(int64_t)a_off[ab.x] + b_off[ab.x] + (e - a_off[ab.x])] = make_int2(ab.y, (int32_t)e);
+}
+
+// blist: the edges sorted by b (stable: ties in edge order).  Node b's b-side
+// entries follow its a-side ones: entry j of blist lands at a_off[b+1] + j.
+__global__ void k_ent_b(int32_t nv, const int2* __restrict__ e2n, const int32_t* __restrict__ blist,
+                        const int32_t* __restrict__ a_off, int2* __restrict__ ent2) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nv) return;
+  const int32_t e = blist[j];
+  const int2 ab = e2n[e];
+  ent2[(int64_t)a_off[ab.y + 1] + j] = make_int2(ab.x, (int32_t)((uint32_t)e | 0x80000000u));
+}
+
+// The memo of the DW form: (h, wfac) recomputed only when the caller's
+// weight changes bits (as k_plan_flux does), and kept as pair words.
+__global__ void k_plan_memo_dw(int32_t ne, const int32_t* __restrict__ eref, const double* __restrict__ ewt,
+                               double4_32a* __restrict__ memo, double4_32a* __restrict__ memo_dw, int memo_valid,
+                               double sc) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  const int32_t r = eref[e];
+  const bool flip = r < 0;
+  const int64_t ce = flip ? (int64_t)~r : (int64_t)r;
+  const double wx = ewt[3 * ce], wy = ewt[3 * ce + 1], wz = ewt[3 * ce + 2];
+  const double4_32a m = memo[e];
+  unsigned long long hx, hy, hz;
+  const bool exact = half_bits(wx, flip, &hx) & half_bits(wy, flip, &hy) & half_bits(wz, flip, &hz);
+  const bool hit = memo_valid && exact && hx == (unsigned long long)__double_as_longlong(m.x) &&
+                   hy == (unsigned long long)__double_as_longlong(m.y) &&
+                   hz == (unsigned long long)__double_as_longlong(m.z);
+  if (hit) return;
+  const double h = flip ? 0.5 : -0.5;
+  const double mag = sqrt(fma(wz, wz, fma(wy, wy, wx * wx)));
+  const double4_32a n = make_double4_32a(h * wx, h * wy, h * wz, -(mag * sc) * 0.5);
+  memo[e] = n;
+  memo_dw[e] = make_double4_32a(dw_pack(dw_split(n.x)), dw_pack(dw_split(n.y)), dw_pack(dw_split(n.z)),
+                                dw_pack(dw_split(n.w)));
+}
+
+// Pair-word primitives of every node in internal order (no FP64 instruction).
+template <bool PERM>
+__global__ void __launch_bounds__(kT) k_plan_prims_dw(int32_t nn, const int32_t* __restrict__ perm,
+                                                      const double* __restrict__ var, double* __restrict__ rec2) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nn) return;
+  const double* x = var + 5 * (PERM ? (int64_t)perm[i] : i);
+  store_prim_dw(rec2, i, node_prim_dw(x[0], x[1], x[2], x[3], x[4]));
+}
+
+// compute_flux_edge_kernel in the DW form, node-centric: each node sums the
+// fluxes of its edges with itself as end a (h negated on the b side) in
+// node_flux_dw's factored form and adds the total to its caller row once --
+// every caller row is one node's, so no atomics, and the same bits each call.
+template <bool PERM>
+__global__ void __launch_bounds__(128, 8) k_plan_flux_dw(int32_t nn, const int32_t* __restrict__ perm,
+                                                         const int32_t* __restrict__ off2,
+                                                         const int2* __restrict__ ent2,
+                                                         const double4_32a* __restrict__ memo_dw,
+                                                         const double* __restrict__ rec2, double* __restrict__ flux) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nn) return;
+  const dwf s_me = dw_unpack(rec2[8 * i + 6]);
+  NodeFluxDW acc;
+  node_flux_dw_init(acc);
+  const int32_t k0 = off2[i], k1 = off2[i + 1];
+  for (int32_t j = k0; j < k1; j++) {
+    const int2 en = ent2[j];
+    const NodePrimDW o = load_prim_dw(rec2, en.x);
+    const double4_32a w = memo_dw[en.y & 0x7fffffff];
+    const uint32_t sg = (uint32_t)en.y & 0x80000000u;
+    dwf hx = dw_unpack(w.x), hy = dw_unpack(w.y), hz = dw_unpack(w.z);
+    hx = dwf{__uint_as_float(__float_as_uint(hx.h) ^ sg), __uint_as_float(__float_as_uint(hx.l) ^ sg)};
+    hy = dwf{__uint_as_float(__float_as_uint(hy.h) ^ sg), __uint_as_float(__float_as_uint(hy.l) ^ sg)};
+    hz = dwf{__uint_as_float(__float_as_uint(hz.h) ^ sg), __uint_as_float(__float_as_uint(hz.l) ^ sg)};
+    node_flux_dw_edge(acc, s_me, o, hx, hy, hz, dw_unpack(w.w));
+  }
+  double F[5];
+  node_flux_dw_finish(acc, load_prim_dw(rec2, i), F);
+  double* row = flux + 5 * (PERM ? (int64_t)perm[i] : i);
+#pragma unroll
+  for (int k = 0; k < 5; k++) row[k] += F[k];
+}
+
 // ---- children plan -------------------------------------------------------------
 
 __global__ void k_child_pairs(int32_t nf, int32_t nc, const int32_t* __restrict__ map, uint32_t* __restrict__ key,
@@ -436,11 +564,12 @@ std::mutex g_mu;
 std::map<Key, EdgePlan*> g_edge;
 std::map<Key, ChildPlan*> g_child;
 int g_mode = MGCFD_PLANS_AUTO;
+std::atomic<int> g_flux_dw{0};  // mgcfd_op_flux_precision: DW form of the flux through plans
 
 void free_edge_plan(EdgePlan* P) {
   if (!P) return;
   for (void* p : {(void*)P->perm, (void*)P->pos, (void*)P->e2n, (void*)P->eref, (void*)P->memo, (void*)P->rec,
-                  (void*)P->fl})
+                  (void*)P->fl, (void*)P->off2, (void*)P->ent2, (void*)P->memo2, (void*)P->memo_dw, (void*)P->rec2})
     if (p) cudaFree(p);
   delete P;
 }
@@ -597,6 +726,50 @@ int build_edge_plan(const int32_t* e2n, int32_t ne, int32_t nn, int mode, cudaSt
   return MGCFD_OK;
 }
 
+// The DW form's tables of an edge plan: per internal node its a-side edges
+// (the sorted edge list's runs) then its b-side ones (a stable sort by b).
+int build_edge_plan_dw(EdgePlan* P, cudaStream_t s) {
+  Scratch S(s);
+  int r;
+  const int32_t nn = P->nn, nv = P->nvalid;
+  int32_t *cnt_a, *cnt_b, *a_off, *b_off, *val, *val_out;
+  uint32_t *key, *key_out;
+  if ((r = S.get(&cnt_a, (size_t)nn + 1)) || (r = S.get(&cnt_b, (size_t)nn + 1)) ||
+      (r = S.get(&a_off, (size_t)nn + 1)) || (r = S.get(&b_off, (size_t)nn + 1)) ||
+      (r = S.get(&key, (size_t)nv + 1)) || (r = S.get(&key_out, (size_t)nv + 1)) ||
+      (r = S.get(&val, (size_t)nv + 1)) || (r = S.get(&val_out, (size_t)nv + 1)))
+    return r;
+  CK(cudaMemsetAsync(cnt_a, 0, sizeof(int32_t) * ((size_t)nn + 1), s));
+  CK(cudaMemsetAsync(cnt_b, 0, sizeof(int32_t) * ((size_t)nn + 1), s));
+  if (nv > 0) k_count_ends<<<grid(nv), kT, 0, s>>>(nv, P->e2n, cnt_a, cnt_b);
+  if ((r = cub_call(S, [&](void* t, size_t& b) { return cub::DeviceScan::ExclusiveSum(t, b, cnt_a, a_off, nn + 1, s); })) ||
+      (r = cub_call(S, [&](void* t, size_t& b) { return cub::DeviceScan::ExclusiveSum(t, b, cnt_b, b_off, nn + 1, s); })))
+    return r;
+  if (nv > 0) {
+    k_b_keys<<<grid(nv), kT, 0, s>>>(nv, P->e2n, key, val);
+    if ((r = cub_call(S, [&](void* t, size_t& b) {
+           return cub::DeviceRadixSort::SortPairs(t, b, key, key_out, val, val_out, nv, 0, bits_for(nn), s);
+         })))
+      return r;
+  }
+  const size_t nv1 = (size_t)std::max(nv, 1);
+  if ((r = plan_alloc(&P->off2, (size_t)nn + 1, &P->bytes)) || (r = plan_alloc(&P->ent2, 2 * nv1, &P->bytes)) ||
+      (r = plan_alloc(&P->memo2, nv1, &P->bytes)) || (r = plan_alloc(&P->memo_dw, nv1, &P->bytes)) ||
+      (r = plan_alloc(&P->rec2, 8 * (size_t)std::max(nn, 1), &P->bytes)))
+    return r;
+  k_off2<<<grid((int64_t)nn + 1), kT, 0, s>>>(nn, a_off, b_off, P->off2);
+  if (nv > 0) {
+    k_ent_a<<<grid(nv), kT, 0, s>>>(nv, P->e2n, a_off, b_off, P->ent2);
+    k_ent_b<<<grid(nv), kT, 0, s>>>(nv, P->e2n, val_out, a_off, P->ent2);
+  }
+  // A memo of all-ones bits (a NaN) matches no weight until first written.
+  CK(cudaMemsetAsync(P->memo2, 0xff, sizeof(double4_32a) * nv1, s));
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(s));
+  P->dw_built = true;
+  return MGCFD_OK;
+}
+
 int build_child_plan(const int32_t* map, int32_t nf, int32_t nc, cudaStream_t s, ChildPlan* P) {
   Scratch S(s);
   int r;
@@ -675,6 +848,25 @@ int edge_plan_flux(EdgePlan* P, const double* var, const double* ewt, double sc,
                    int64_t* skipped) {
   *skipped = P->nbad;
   if (P->nn == 0) return MGCFD_OK;
+  if (g_flux_dw.load()) {
+    // The DW form: three kernels, no atomics, no work space of FP64 rows.
+    int r;
+    if (!P->dw_built && (r = build_edge_plan_dw(P, s))) return r;
+    const bool valid = P->memo2_sc == sc;  // false for NaN: never used yet
+    P->memo2_sc = sc;
+    if (P->nvalid > 0)
+      k_plan_memo_dw<<<grid(P->nvalid), kT, 0, s>>>(P->nvalid, P->eref, ewt, P->memo2, P->memo_dw, valid ? 1 : 0, sc);
+    if (P->permuted) {
+      k_plan_prims_dw<true><<<grid(P->nn), kT, 0, s>>>(P->nn, P->perm, var, P->rec2);
+      k_plan_flux_dw<true><<<grid(P->nn, 128), 128, 0, s>>>(P->nn, P->perm, P->off2, P->ent2, P->memo_dw, P->rec2, flux);
+    } else {
+      k_plan_prims_dw<false><<<grid(P->nn), kT, 0, s>>>(P->nn, nullptr, var, P->rec2);
+      k_plan_flux_dw<false><<<grid(P->nn, 128), 128, 0, s>>>(P->nn, nullptr, P->off2, P->ent2, P->memo_dw, P->rec2,
+                                                            flux);
+    }
+    CK(cudaGetLastError());
+    return MGCFD_OK;
+  }
   const bool memo_valid = P->memo_sc == sc;  // false for NaN: never used yet
   P->memo_sc = sc;
   if (P->permuted) {
@@ -724,6 +916,13 @@ extern "C" int mgcfd_op_plans_mode(int32_t mode) {
     return mgcfd::set_error(MGCFD_ERR_INVALID, "mgcfd_op_plans_mode: unknown mode");
   std::lock_guard<std::mutex> lock(mgcfd::g_mu);
   mgcfd::g_mode = mode;
+  return MGCFD_OK;
+}
+
+extern "C" int mgcfd_op_flux_precision(int32_t precision) {
+  if (precision != MGCFD_PRECISION_FP64 && precision != MGCFD_PRECISION_DW)
+    return mgcfd::set_error(MGCFD_ERR_INVALID, "mgcfd_op_flux_precision: FP64 or DW");
+  mgcfd::g_flux_dw.store(precision == MGCFD_PRECISION_DW ? 1 : 0);
   return MGCFD_OK;
 }
 

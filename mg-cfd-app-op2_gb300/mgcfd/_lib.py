@@ -110,6 +110,7 @@ SIGNATURES = {
     "mgcfd_op_up_post": (C.c_int, [_i32, _vp, _vp, _vp]),
     "mgcfd_op_down": (C.c_int, [_i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "mgcfd_op_plans_mode": (C.c_int, [_i32]),
+    "mgcfd_op_flux_precision": (C.c_int, [_i32]),
     "mgcfd_op_plan_release": (C.c_int, [_vp]),
     "mgcfd_op_plans_release": (C.c_int, []),
     "mgcfd_op_plans_info": (C.c_int, [_pp(C.c_int64), _pp(C.c_int64), _pp(C.c_int64), _pp(C.c_int64)]),

@@ -123,6 +123,12 @@ def plans_mode(mode="auto"):
     _call("mgcfd_op_plans_mode", PLANS[mode])
 
 
+def flux_precision(precision="fp64"):
+    """Arithmetic of compute_flux_edge calls through plans: "fp64" (default)
+    or "dw" (double-word primitives and fluxes, no atomics; the FP64 bar)."""
+    _call("mgcfd_op_flux_precision", {"fp64": 0, "dw": 2}[precision])
+
+
 def plan_release(map_ptr):
     """Free the plans built from the map at this device address (before the
     map's memory is freed or reused; synchronises the device)."""

@@ -46,3 +46,4 @@ def release_plans(request):
     if torch.cuda.is_available():
         _lib.check(_lib._LIB.mgcfd_op_plans_release())
         _lib.check(_lib._LIB.mgcfd_op_plans_mode(1))  # MGCFD_PLANS_AUTO
+        _lib.check(_lib._LIB.mgcfd_op_flux_precision(0))  # MGCFD_PRECISION_FP64

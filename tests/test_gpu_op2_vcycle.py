@@ -27,8 +27,9 @@ def _levels(kind):
     return irregular_levels(1500, 3, 5)
 
 
-def _run_loops(levels, cycles, mode):
+def _run_loops(levels, cycles, mode, precision="fp64"):
     ops.plans_mode(mode)
+    ops.flux_precision(precision)
     s = mgcfd.LoopSolver(levels, MACH, AOA)
     s.run(cycles)
     st, rms = s.synchronize()
@@ -37,15 +38,19 @@ def _run_loops(levels, cycles, mode):
     info = ops.plans_info()
     s.close()
     ops.plans_mode("auto")
+    ops.flux_precision("fp64")
     return st, rms, out, res0, info
 
 
 @pytest.mark.parametrize("kind", ["lattice", "renumbered", "irregular"])
-@pytest.mark.parametrize("mode", ["reorder", "caller_order", "off"])
-def test_vcycle_through_loops_matches_oracle(kind, mode):
+@pytest.mark.parametrize("mode,precision", [("reorder", "fp64"), ("caller_order", "fp64"), ("off", "fp64"),
+                                            ("reorder", "dw"), ("caller_order", "dw")])
+def test_vcycle_through_loops_matches_oracle(kind, mode, precision):
+    """Also with the flux calls in the DW form (double-word primitives and
+    fluxes through the plans, node-centric, no atomics), at the same bar."""
     levels = _levels(kind)
     cycles = 3
-    st, rms, got, res0, info = _run_loops(levels, cycles, mode)
+    st, rms, got, res0, info = _run_loops(levels, cycles, mode, precision)
     assert st == 0
     ref = O.OracleRun(levels)
     assert ref.run(MACH, AOA, cycles)[0] == 0
@@ -101,7 +106,8 @@ def _oracle_flux(e2n, var, w, sc, nn):
 
 
 @pytest.mark.parametrize("mode", ["reorder", "caller_order"])
-def test_plan_on_disconnected_graph_with_isolated_nodes_and_bad_entries(mode):
+@pytest.mark.parametrize("precision", ["fp64", "dw"])
+def test_plan_on_disconnected_graph_with_isolated_nodes_and_bad_entries(mode, precision):
     """Two separate lattices, isolated nodes (no edges), parallel and reversed
     edges and out-of-range map entries, all under a random relabelling: the
     Cuthill-McKee search covers every component and leaves isolated nodes at
@@ -121,6 +127,7 @@ def test_plan_on_disconnected_graph_with_isolated_nodes_and_bad_entries(mode):
     exp, nbad = _oracle_flux(e, var, w, 0.2, nn)
     assert nbad == 3
     ops.plans_mode(mode)
+    ops.flux_precision(precision)
     ops.map_errors(reset=True)
     d_e, d_v, d_w = (torch.from_numpy(x).cuda() for x in (e, var, w))
     for call in range(2):  # the second call reuses the plan and the weight memo
@@ -134,7 +141,8 @@ def test_plan_on_disconnected_graph_with_isolated_nodes_and_bad_entries(mode):
     ops.plan_release(d_e.data_ptr())
 
 
-def test_weight_memo_follows_changed_weights_and_smoothing():
+@pytest.mark.parametrize("precision", ["fp64", "dw"])
+def test_weight_memo_follows_changed_weights_and_smoothing(precision):
     """The plan keeps each edge's |w| term for the weight bits it last saw:
     new weights and a new smoothing coefficient give the oracle's fluxes for
     the new inputs, including weights whose halves are not normal numbers."""
@@ -145,6 +153,7 @@ def test_weight_memo_follows_changed_weights_and_smoothing():
     var, w = _flux_case(rng, nn, e)
     d_e, d_v = torch.from_numpy(e).cuda(), torch.from_numpy(var).cuda()
     ops.plans_mode("reorder")
+    ops.flux_precision(precision)
     w2 = w * 1.5
     w2[3] = [0.0, 1e-3, -1e-3]          # a zero component
     w2[8] = [5e-324, 1e-3, 2e-308]      # subnormal / smallest normal components
@@ -155,6 +164,37 @@ def test_weight_memo_follows_changed_weights_and_smoothing():
         exp, _ = _oracle_flux(e, var, weights, sc, nn)
         torch.cuda.synchronize()
         assert state_error(flux.cpu().numpy(), exp) <= STATE_TOL
+    ops.plan_release(d_e.data_ptr())
+
+
+def test_dw_and_fp64_flux_calls_share_a_plan():
+    """FP64 and DW calls alternate on one plan while the weights change: each
+    keeps its own memo, both stay within the FP64 bar of the oracle, and the
+    DW form gives the same bits on every call (no atomics)."""
+    rng = np.random.default_rng(17)
+    L = mgcfd.HostMesh.generate(11, 1, 3).level(0)
+    e = np.ascontiguousarray(L.edge_to_nodes)
+    nn = L.nnodes
+    var, w = _flux_case(rng, nn, e)
+    d_e, d_v = torch.from_numpy(e).cuda(), torch.from_numpy(var).cuda()
+    ops.plans_mode("reorder")
+    dw_bits = {}
+    for k, (weights, prec) in enumerate(((w, "fp64"), (w, "dw"), (w * 2, "fp64"), (w * 2, "dw"), (w, "dw"),
+                                         (w, "fp64"), (w * 2, "dw"))):
+        ops.flux_precision(prec)
+        d_w = torch.from_numpy(np.ascontiguousarray(weights)).cuda()
+        flux = torch.zeros((nn, 5), dtype=torch.float64, device="cuda")
+        ops.compute_flux_edge(len(e), nn, d_e.data_ptr(), d_v.data_ptr(), d_w.data_ptr(), 0.2, flux.data_ptr())
+        got = flux.cpu().numpy()
+        exp, _ = _oracle_flux(e, var, weights, 0.2, nn)
+        assert state_error(got, exp) <= STATE_TOL, (k, prec)
+        if prec == "dw":
+            key = float(weights[0, 0])
+            if key in dw_bits:
+                np.testing.assert_array_equal(got, dw_bits[key])
+            dw_bits[key] = got
+    assert ops.plans_info()["edge_plans"] == 1
+    ops.flux_precision("fp64")
     ops.plan_release(d_e.data_ptr())
 
 
