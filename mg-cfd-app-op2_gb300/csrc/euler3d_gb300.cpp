@@ -113,6 +113,7 @@ void usage() {
                "--mach=FLOAT (1.2)  --aoa=DEGREES (0.0)  --precision=fp64|mixed|dw\n"
                "--increment=auto|atomic|gather|fused|coloured  --accumulation=fp64|pair32\n"
                "--per-loop   run the reference's loop sequence through the per-loop entry points\n"
+               "             (with --precision dw, the edge-flux calls in the DW form)\n"
                "-m, -r, -p are accepted for compatibility and ignored (one GPU, no PAPI).\n");
 }
 
@@ -489,11 +490,14 @@ int main(int argc, char** argv) {
       else std::printf("Cannot find level %d solution file: %s\n", l, p.c_str());
     }
 
-  if (c.per_loop && c.precision != MGCFD_PRECISION_FP64) {
-    std::printf("ERROR: --per-loop runs the reference's FP64 loops; --precision mixed or dw needs the solver\n");
+  if (c.per_loop && c.precision == MGCFD_PRECISION_MIXED) {
+    std::printf("ERROR: --per-loop runs the reference's FP64 loops (the flux in the DW form with --precision dw); "
+                "--precision mixed needs the solver\n");
     mgcfd_host_mesh_destroy(mesh);
     return 1;
   }
+  // --per-loop --precision dw: the edge-flux calls in the DW form (through their plans).
+  if (c.per_loop) mgcfd_op_flux_precision(c.precision == MGCFD_PRECISION_DW ? MGCFD_PRECISION_DW : MGCFD_PRECISION_FP64);
   if (c.per_loop && c.renumber) std::printf("Note: -n has no effect with --per-loop (the loops' plans order the nodes)\n");
   Results res;
   st = c.per_loop ? run_per_loop(c, lv, &res) : run_solver(c, lv, &res);

@@ -115,16 +115,18 @@ def test_mixed_precision_flags(tmp_path, extra):
 
 
 @pytest.mark.gpu
-def test_per_loop_run_matches_reference_fixture(tmp_path):
+@pytest.mark.parametrize("precision", [[], ["--precision", "dw"]], ids=["fp64", "dw"])
+def test_per_loop_run_matches_reference_fixture(tmp_path, precision):
     """--per-loop runs the reference's loop sequence through the mgcfd_op_*
     entry points on OP2-layout dats: its solution files match the reference's
-    (golden fixture) and -v accepts them."""
+    (golden fixture) and -v accepts them; with --precision dw the flux calls
+    run in the DW form, at the same bar."""
     z = np.load(GOLDEN / "lattice9_l3_c3.npz")
     meta = json.loads(str(z["meta"]))
     mesh = mgcfd.HostMesh.generate(meta["n"], meta["levels"], meta["seed"])
     mesh.write(str(tmp_path), "m_")
     args = ["-i", "input.dat", "-d", tmp_path, "-g", meta["cycles"], "--mach", meta["mach"], "--aoa", meta["aoa"],
-            "--per-loop"]
+            "--per-loop", *precision]
     r = cli(*args, "--output-variables", "--output-step-factors", "--output-fluxes", "-o", f"{tmp_path}/solution.")
     assert r.returncode == 0, r.stdout + r.stderr
     assert r.stdout.count("Performing MG cycle") == meta["cycles"] and "Max total runtime" in r.stdout
