@@ -843,6 +843,8 @@ def run_loops(args):
     renumbered = mesh.renumber("spatial")
     forms = {"file_order": ("auto", mesh, "fp64"), "renumbered": ("auto", renumbered, "fp64"),
              "file_order_dw": ("auto", mesh, "dw"), "renumbered_dw": ("auto", renumbered, "dw")}
+    chosen = set(args.loops_forms.split(","))
+    forms = {k: v for k, v in forms.items() if k in chosen}
     out = {}
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as sampler:
         for name, (mode, m, prec) in forms.items():
@@ -890,26 +892,27 @@ def run_loops(args):
                          "roofline": {"bound": "hbm", "achieved": round(byt / (flux_ms * 1e-3) / 1e9, 1), "peak": peak,
                                       "unit": "GB/s", "frac": round(byt / (flux_ms * 1e-3) / 1e9 / peak, 4),
                                       "algorithmic_bytes_per_launch": byt, "peak_source": peak_kind}}
-        ops.plans_mode("off")
-        s = mgcfd.LoopSolver(mesh, MACH, AOA, stream=stream)
-        s.run(1)
-        s.synchronize()
-        e0.record(stream)
-        s.run(args.loops_plan_free_cycles)
-        e1.record(stream)
-        st, _ = s.synchronize()
-        out["plan_free"] = {"value": round(args.loops_plan_free_cycles / (e0.elapsed_time(e1) * 1e-3), 3),
-                            "unit": "cycles/s", "status": st, "cycles": args.loops_plan_free_cycles}
-        s.close()
-        ops.plans_mode("auto")
+        if "plan_free" in chosen:
+            ops.plans_mode("off")
+            s = mgcfd.LoopSolver(mesh, MACH, AOA, stream=stream)
+            s.run(1)
+            s.synchronize()
+            e0.record(stream)
+            s.run(args.loops_plan_free_cycles)
+            e1.record(stream)
+            st, _ = s.synchronize()
+            out["plan_free"] = {"value": round(args.loops_plan_free_cycles / (e0.elapsed_time(e1) * 1e-3), 3),
+                                "unit": "cycles/s", "status": st, "cycles": args.loops_plan_free_cycles}
+            s.close()
+            ops.plans_mode("auto")
     solver_flux_ms = kernel_times(mesh, args.kernel_cycles)
-    for name in ("file_order", "renumbered", "file_order_dw", "renumbered_dw"):
+    for name in forms:
         out[name]["flux_call_vs_solver_flux"] = round(out[name]["flux_call_ms"] / solver_flux_ms, 3)
     line = {"metric": "MG V-cycles/s at 8M nodes through the per-loop entry points (OP2 dat layout)",
             "unit": "cycles/s", "higher_is_better": True, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "data": "synthetic: seeded jittered 200^3 lattice, permuted ids",
             "config": line_config(args, N, E),
-            "value": out["file_order"]["value"], "forms": out,
+            "value": out.get("file_order", {}).get("value"), "forms": out,
             "device_solver": {"value": round(solver_value, 3), "unit": "cycles/s",
                               "flux_ms_per_launch": round(solver_flux_ms, 4)},
             "timing": "CUDA events on the driver's stream; globals stay on the device (no host wait per loop)",
@@ -964,6 +967,8 @@ def main():
     ap.add_argument("--serve-rate-multiples", type=float, nargs="*", default=[0.5, 0.9, 2.0],
                     help="Poisson rates as multiples of the plain path's capacity (none: capacity only)")
     ap.add_argument("--serve-slots", type=int, default=16)
+    ap.add_argument("--loops-forms", default="file_order,renumbered,file_order_dw,renumbered_dw,plan_free",
+                    help="--mode loops: which forms to run (comma-separated)")
     ap.add_argument("--kernel-cycles", type=int, default=5,
                     help="V-cycles of the separate per-kernel event pass behind the roofline")
     ap.add_argument("--no-extra-forms", action="store_true",

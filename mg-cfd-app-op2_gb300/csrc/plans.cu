@@ -83,9 +83,10 @@ struct EdgePlan {
   bool dw_built = false;
   int32_t* off2 = nullptr;          // [nn + 1] each node's entries in ent2
   int2* ent2 = nullptr;             // [2 nvalid] (neighbour, edge; bit 31 set on the b side)
-  double4_32a* memo2 = nullptr;     // [nvalid] (h, wfac) of the last weight a DW call saw
-  double4_32a* memo_dw = nullptr;   // [nvalid] the same as pair words
-  double memo2_sc = NAN;
+  int32_t* inv_e = nullptr;        // [ne] caller edge -> internal edge (bit 31: flipped; kNoEdge: left out)
+  double* wcopy = nullptr;          // [ne][3] the caller's weights of the last DW call, caller order
+  double4_32a* memo_dw = nullptr;   // [nvalid] (h, wfac) of those weights as pair words
+  double memo_dw_sc = NAN;          // smoothing coefficient of memo_dw (NaN: never used)
   double* rec2 = nullptr;           // [nn][8] pair-word primitives, internal order
   int64_t bytes = 0;
 };
@@ -294,6 +295,11 @@ __global__ void k_edge_final(int32_t nvalid, const unsigned long long* __restric
   eref[k] = (pa == lo) ? e : ~e;  // a became the high end: the edge is flipped
 }
 
+__global__ void k_fill_i32(int64_t n, int32_t v, int32_t* __restrict__ p) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = v;
+}
+
 __global__ void k_fill_u64(int64_t n, unsigned long long v, unsigned long long* __restrict__ p) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) p[i] = v;
@@ -430,30 +436,41 @@ __global__ void k_ent_b(int32_t nv, const int2* __restrict__ e2n, const int32_t*
   ent2[(int64_t)a_off[ab.y + 1] + j] = make_int2(ab.x, (int32_t)((uint32_t)e | 0x80000000u));
 }
 
-// The memo of the DW form: (h, wfac) recomputed only when the caller's
-// weight changes bits (as k_plan_flux does), and kept as pair words.
-__global__ void k_plan_memo_dw(int32_t ne, const int32_t* __restrict__ eref, const double* __restrict__ ewt,
-                               double4_32a* __restrict__ memo, double4_32a* __restrict__ memo_dw, int memo_valid,
-                               double sc) {
+constexpr int32_t kNoEdge = 0x7fffffff;  // inv_e of a caller edge left out of the plan
+
+__global__ void k_inv_e(int32_t nv, const int32_t* __restrict__ eref, int32_t* __restrict__ inv) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= ne) return;
+  if (e >= nv) return;
   const int32_t r = eref[e];
-  const bool flip = r < 0;
-  const int64_t ce = flip ? (int64_t)~r : (int64_t)r;
+  inv[r < 0 ? ~r : r] = (int32_t)((uint32_t)e | (r < 0 ? 0x80000000u : 0u));
+}
+
+// The weights of the DW form, in the caller's edge order (coalesced): each
+// caller edge whose weight bits differ from the copy of the last DW call (or
+// every edge, after a change of smoothing coefficient) gets its (h, wfac)
+// recomputed -- the FP64 plan's formula -- and stored as pair words at its
+// internal position.  Unchanged weights cost a compare.
+__global__ void k_plan_weights_dw(int32_t ne, const int32_t* __restrict__ inv, const double* __restrict__ ewt,
+                                  double* __restrict__ wcopy, double4_32a* __restrict__ memo_dw, int force,
+                                  double sc) {
+  const int64_t ce = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (ce >= ne) return;
+  const int32_t r = inv[ce];
+  if (r == kNoEdge) return;
   const double wx = ewt[3 * ce], wy = ewt[3 * ce + 1], wz = ewt[3 * ce + 2];
-  const double4_32a m = memo[e];
-  unsigned long long hx, hy, hz;
-  const bool exact = half_bits(wx, flip, &hx) & half_bits(wy, flip, &hy) & half_bits(wz, flip, &hz);
-  const bool hit = memo_valid && exact && hx == (unsigned long long)__double_as_longlong(m.x) &&
-                   hy == (unsigned long long)__double_as_longlong(m.y) &&
-                   hz == (unsigned long long)__double_as_longlong(m.z);
-  if (hit) return;
+  double* c = wcopy + 3 * ce;
+  const bool same = __double_as_longlong(wx) == __double_as_longlong(c[0]) &&
+                    __double_as_longlong(wy) == __double_as_longlong(c[1]) &&
+                    __double_as_longlong(wz) == __double_as_longlong(c[2]);
+  if (same && !force) return;
+  const bool flip = r < 0;
   const double h = flip ? 0.5 : -0.5;
   const double mag = sqrt(fma(wz, wz, fma(wy, wy, wx * wx)));
-  const double4_32a n = make_double4_32a(h * wx, h * wy, h * wz, -(mag * sc) * 0.5);
-  memo[e] = n;
-  memo_dw[e] = make_double4_32a(dw_pack(dw_split(n.x)), dw_pack(dw_split(n.y)), dw_pack(dw_split(n.z)),
-                                dw_pack(dw_split(n.w)));
+  memo_dw[r & 0x7fffffff] = make_double4_32a(dw_pack(dw_split(h * wx)), dw_pack(dw_split(h * wy)),
+                                             dw_pack(dw_split(h * wz)), dw_pack(dw_split(-(mag * sc) * 0.5)));
+  c[0] = wx;
+  c[1] = wy;
+  c[2] = wz;
 }
 
 // Pair-word primitives of every node in internal order (no FP64 instruction).
@@ -569,7 +586,8 @@ std::atomic<int> g_flux_dw{0};  // mgcfd_op_flux_precision: DW form of the flux 
 void free_edge_plan(EdgePlan* P) {
   if (!P) return;
   for (void* p : {(void*)P->perm, (void*)P->pos, (void*)P->e2n, (void*)P->eref, (void*)P->memo, (void*)P->rec,
-                  (void*)P->fl, (void*)P->off2, (void*)P->ent2, (void*)P->memo2, (void*)P->memo_dw, (void*)P->rec2})
+                  (void*)P->fl, (void*)P->off2, (void*)P->ent2, (void*)P->inv_e, (void*)P->wcopy, (void*)P->memo_dw,
+                  (void*)P->rec2})
     if (p) cudaFree(p);
   delete P;
 }
@@ -753,17 +771,19 @@ int build_edge_plan_dw(EdgePlan* P, cudaStream_t s) {
       return r;
   }
   const size_t nv1 = (size_t)std::max(nv, 1);
+  const size_t ne1 = (size_t)std::max(P->ne, 1);
   if ((r = plan_alloc(&P->off2, (size_t)nn + 1, &P->bytes)) || (r = plan_alloc(&P->ent2, 2 * nv1, &P->bytes)) ||
-      (r = plan_alloc(&P->memo2, nv1, &P->bytes)) || (r = plan_alloc(&P->memo_dw, nv1, &P->bytes)) ||
-      (r = plan_alloc(&P->rec2, 8 * (size_t)std::max(nn, 1), &P->bytes)))
+      (r = plan_alloc(&P->inv_e, ne1, &P->bytes)) || (r = plan_alloc(&P->wcopy, 3 * ne1, &P->bytes)) ||
+      (r = plan_alloc(&P->memo_dw, nv1, &P->bytes)) || (r = plan_alloc(&P->rec2, 8 * (size_t)std::max(nn, 1), &P->bytes)))
     return r;
   k_off2<<<grid((int64_t)nn + 1), kT, 0, s>>>(nn, a_off, b_off, P->off2);
   if (nv > 0) {
     k_ent_a<<<grid(nv), kT, 0, s>>>(nv, P->e2n, a_off, b_off, P->ent2);
     k_ent_b<<<grid(nv), kT, 0, s>>>(nv, P->e2n, val_out, a_off, P->ent2);
   }
-  // A memo of all-ones bits (a NaN) matches no weight until first written.
-  CK(cudaMemsetAsync(P->memo2, 0xff, sizeof(double4_32a) * nv1, s));
+  // Caller edges left out of the plan stay kNoEdge.
+  if (P->ne > 0) k_fill_i32<<<grid(P->ne), kT, 0, s>>>(P->ne, kNoEdge, P->inv_e);
+  if (nv > 0) k_inv_e<<<grid(nv), kT, 0, s>>>(nv, P->eref, P->inv_e);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(s));
   P->dw_built = true;
@@ -852,10 +872,10 @@ int edge_plan_flux(EdgePlan* P, const double* var, const double* ewt, double sc,
     // The DW form: three kernels, no atomics, no work space of FP64 rows.
     int r;
     if (!P->dw_built && (r = build_edge_plan_dw(P, s))) return r;
-    const bool valid = P->memo2_sc == sc;  // false for NaN: never used yet
-    P->memo2_sc = sc;
+    const bool force = !(P->memo_dw_sc == sc);  // the first DW call (NaN) or a new smoothing coefficient
+    P->memo_dw_sc = sc;
     if (P->nvalid > 0)
-      k_plan_memo_dw<<<grid(P->nvalid), kT, 0, s>>>(P->nvalid, P->eref, ewt, P->memo2, P->memo_dw, valid ? 1 : 0, sc);
+      k_plan_weights_dw<<<grid(P->ne), kT, 0, s>>>(P->ne, P->inv_e, ewt, P->wcopy, P->memo_dw, force ? 1 : 0, sc);
     if (P->permuted) {
       k_plan_prims_dw<true><<<grid(P->nn), kT, 0, s>>>(P->nn, P->perm, var, P->rec2);
       k_plan_flux_dw<true><<<grid(P->nn, 128), 128, 0, s>>>(P->nn, P->perm, P->off2, P->ent2, P->memo_dw, P->rec2, flux);
