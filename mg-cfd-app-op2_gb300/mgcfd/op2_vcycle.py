@@ -2,7 +2,8 @@
 entry points (mgcfd_op_* in include/mgcfd_gb300.h).
 
 This is what an OP2 application sees when its op_par_loop calls are bound to
-this library (the host stub in INTEGRATION.md): every dat is a device array
+this library (through a host stub that passes each dat's and map's device
+pointer to the matching entry point): every dat is a device array
 in OP2's layout ([set size][dim], row-major, in the mesh file's numbering),
 every map a 0-based int32 array, and each loop of euler3d.cpp is one call:
 
