@@ -58,6 +58,9 @@ def test_autotune_picks_the_fastest_candidate_and_closes_every_run():
     assert all(r.closed for r in FakeRun.made)
     best, _ = autotune.tune(maker(table), 1000, "mixed", cycles=1)
     assert best["increment"] == "fused"
+    # ... and for the double-word form.
+    best, timings = autotune.tune(maker(table), 1000, "dw", cycles=1)
+    assert best == {"increment": "fused", "block_size": 0, "precision": "dw"} and len(timings) == 5
 
 
 def test_autotune_skips_failed_candidates():
@@ -92,6 +95,10 @@ def test_server_estimate_grows_with_mesh_and_strategy():
     # auto means atomics in FP64 and the fused stage in mixed precision.
     assert server.estimate_bytes(small, "fp64", "auto") == atomic
     assert server.estimate_bytes(small, "mixed", "auto") == server.estimate_bytes(small, "mixed", "fused")
+    # DW: the pair-word primitives and weights on top of FP64's arrays; auto is the fused stage.
+    assert server.estimate_bytes(small, "dw", "atomic") > atomic
+    assert server.estimate_bytes(small, "dw", "auto") == server.estimate_bytes(small, "dw", "fused")
+    assert server.estimate_bytes(small, "dw", "fused") > server.estimate_bytes(small, "dw", "atomic")
 
 
 def test_server_estimate_rejects_bad_arguments():
