@@ -344,13 +344,4 @@ __device__ __forceinline__ void node_flux_dw_finish(NodeFluxDW& A, const NodePri
   for (int k = 0; k < 5; k++) F[k] = acc_to_double(A.S[k]);
 }
 
-// Sum += x, or sum -= x, for accumulators (a node's edge increments).
-__device__ __forceinline__ void acc_add_acc(dwacc& sum, dwacc x, bool neg) {
-  const float xs = neg ? -x.s : x.s, xc = neg ? -x.c : x.c;
-  float s, q;
-  two_sum(sum.s, xs, s, q);
-  sum.s = s;
-  sum.c = __fadd_rn(sum.c, __fadd_rn(q, xc));
-}
-
 }  // namespace mgcfd

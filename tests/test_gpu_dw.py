@@ -35,6 +35,7 @@ def dwlib():
     lib = C.CDLL(str(out))
     lib.dw_check_split.restype = C.c_int
     lib.dw_check_flux.restype = C.c_int
+    lib.dw_check_node.restype = C.c_int
     return lib
 
 
@@ -122,6 +123,58 @@ def test_edge_flux_error_bound(dwlib):
     assert e64.max() <= 2.0 ** -48, e64.max()
     assert edw.max() <= 2.0 ** -42, edw.max()
     assert np.all(fdw[:100] == 0.0)
+
+
+def _prims_ld(x):
+    """node_prim's formula in long double: rho, m, E, p, |u|+c, 1/rho."""
+    L = np.longdouble
+    rho, mx, my, mz, E = (x[:, k].astype(L) for k in range(5))
+    ri = 1 / rho
+    m2 = mx * mx + my * my + mz * mz
+    p = (L(1.4) - 1) * (E - m2 * ri / 2)
+    s = np.sqrt(m2) * ri + np.sqrt(L(1.4) * p * ri)
+    return np.stack([rho, mx, my, mz, E, p, s, ri], axis=1)
+
+
+def test_node_primitives_and_factored_node_sum(dwlib):
+    """node_prim_dw (the primitives in pairs, no FP64 instruction) against
+    node_prim and long double; node_flux_dw (each node's edge-flux sum in the
+    factored form the fused stage uses) against the long-double sum of the
+    same edges' fluxes, relative to the sum of the terms' magnitudes."""
+    rng = np.random.default_rng(21)
+    n, K = 50_000, 6
+
+    def states(shape):
+        rho = rng.uniform(0.3, 2.5, shape)
+        u = rng.uniform(-0.9, 0.9, shape + (3,))
+        p = rng.uniform(0.2, 2.0, shape)
+        E = p / 0.4 + 0.5 * rho * (u ** 2).sum(-1)
+        return np.concatenate([rho[..., None], rho[..., None] * u, E[..., None]], axis=-1)
+    me = np.ascontiguousarray(states((n,)))
+    nb = np.ascontiguousarray(states((n, K)))
+    nb[: n // 5] = me[: n // 5, None, :] * (1 + rng.uniform(-1e-7, 1e-7, (n // 5, K, 5)))  # near-uniform flow
+    w = np.concatenate([rng.uniform(-1, 1, (n, K, 3)), -rng.uniform(0, 1, (n, K, 1))], axis=-1)
+    w = np.ascontiguousarray(w * np.ldexp(1.0, rng.integers(-30, 0, (n, K, 1))))
+    out, pdw, p64 = np.empty((n, 5)), np.empty((n, 8)), np.empty((n, 8))
+    assert dwlib.dw_check_node(C.c_int64(n), C.c_int32(K), _p(me), _p(nb), _p(w), _p(out), _p(pdw), _p(p64)) == 0
+    ref = _prims_ld(me)
+    # p = 0.4 (E - rho|u|^2/2) cancels by up to 40x for these states: judged
+    # against the magnitude of its terms, 0.4|E|; c and so s inherit at most
+    # half of that amplification.
+    den = np.abs(ref)
+    den[:, 5] = 0.4 * np.abs(ref[:, 4])
+    err_dw = (np.abs(pdw - ref) / den).astype(np.float64)
+    err_64 = (np.abs(p64 - ref) / den).astype(np.float64)
+    assert err_dw.max() <= 2.0 ** -40, err_dw.max(axis=0)
+    assert err_64.max() <= 2.0 ** -46, err_64.max(axis=0)
+    # The node sum: every edge with the node as end a (weights already oriented).
+    a = np.repeat(_prims_ld(me).astype(np.float64), K, axis=0)
+    b = _prims_ld(nb.reshape(-1, 5)).astype(np.float64)
+    exact, mag = _flux_ref(a, b, w.reshape(-1, 4))
+    exact = exact.reshape(n, K, 5).sum(axis=1)
+    mag = mag.reshape(n, K, 5).sum(axis=1)
+    err = (np.abs(out - exact) / np.where(mag == 0, 1, mag)).astype(np.float64)
+    assert np.isfinite(out).all() and err.max() <= 2.0 ** -40, err.max()
 
 
 def _oracle(levels, mach, aoa, cycles):
