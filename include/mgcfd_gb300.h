@@ -262,8 +262,10 @@ int mgcfd_op_plans_info(int64_t* edge_plans, int64_t* child_plans, int64_t* reor
  * fluxes in pairs and adds the total to its row of fluxes once in FP64 -- no
  * atomics, the same bits on every call -- within the FP64 bar of the
  * reference (1e-10).  The pairs have binary32's exponent range: weights
- * should lie in [2^-70, 2^70).  Plan-free calls stay FP64.  Process-wide,
- * like mgcfd_op_plans_mode; other precisions are refused. */
+ * should lie in [2^-70, 2^70).  Plan-free calls stay FP64.  A plan builds
+ * its DW tables on its first DW call (synchronising the stream); a first DW
+ * call made while the stream captures a CUDA graph runs the FP64 form.
+ * Process-wide, like mgcfd_op_plans_mode; other precisions are refused. */
 int mgcfd_op_flux_precision(int32_t precision);
 /* Number of elements the mapped entry points above skipped because a map
  * entry was outside [0, set size) since the last reset; reset != 0 zeroes the

@@ -868,10 +868,22 @@ int edge_plan_flux(EdgePlan* P, const double* var, const double* ewt, double sc,
                    int64_t* skipped) {
   *skipped = P->nbad;
   if (P->nn == 0) return MGCFD_OK;
-  if (g_flux_dw.load()) {
+  bool dw = g_flux_dw.load();
+  if (dw && !P->dw_built) {
+    // The DW tables are built on the first DW call (synchronising the
+    // stream); a first DW call during graph capture runs the FP64 form.
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    CK(cudaStreamIsCapturing(s, &cap));
+    if (cap != cudaStreamCaptureStatusNone) {
+      dw = false;
+    } else {
+      std::lock_guard<std::mutex> lock(g_mu);
+      int r;
+      if (!P->dw_built && (r = build_edge_plan_dw(P, s))) return r;
+    }
+  }
+  if (dw) {
     // The DW form: three kernels, no atomics, no work space of FP64 rows.
-    int r;
-    if (!P->dw_built && (r = build_edge_plan_dw(P, s))) return r;
     const bool force = !(P->memo_dw_sc == sc);  // the first DW call (NaN) or a new smoothing coefficient
     P->memo_dw_sc = sc;
     if (P->nvalid > 0)
