@@ -234,15 +234,20 @@ int mgcfd_op_restrict_noalloc(int32_t nfine, int32_t ncoarse, const int32_t* nod
  *     L2, and adds the increments onto the caller's rows.  |w| is kept per
  *     edge and recomputed only when the weight's bits change;
  *   - restriction: the children of every coarse node, so up_kernel is a
- *     gather with no atomics (results independent of scheduling).
- * A plan holds integer structure derived from the map only: the map's
+ *     gather with no atomics (results independent of scheduling);
+ *   - mgcfd_op_calculate_dt: per vol dat (pointer and node count), each
+ *     node's cube root of its volume with the volume's bits beside it; a call
+ *     takes the root again only where the bits changed, so results are those
+ *     of cbrt on every call.
+ * A map plan holds integer structure derived from the map only: the map's
  * contents must not change while it is cached (OP2 maps are immutable too).
  * Building a plan synchronises the caller's stream; a first call made while
  * the stream captures a CUDA graph runs the plan-free kernel instead.  Calls
  * on the same map share the plan's work space: issue them in stream order.
  * Before freeing a map, or reusing its memory for another map, release its
  * plans with mgcfd_op_plan_release(map) (plans on the current device built
- * from that pointer); mgcfd_op_plans_release frees every plan.  Both
+ * from that pointer, a vol dat's included); mgcfd_op_plans_release frees
+ * every plan.  Both
  * synchronise the device.  mgcfd_op_plans_mode selects how plans built
  * from then on order the nodes (AUTO: the caller's order unless more than a
  * tenth of the edges join ids over max(65536, N/128) apart; REORDER: always

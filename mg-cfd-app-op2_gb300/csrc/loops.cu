@@ -406,6 +406,10 @@ extern "C" int mgcfd_op_calculate_dt(int32_t n, const double* v, const double* v
   CHECK_N(n, "mgcfd_op_calculate_dt");
   CHECK_PTR(v, n, "calculate_dt"); CHECK_PTR(vol, n, "calculate_dt"); CHECK_PTR(dt, n, "calculate_dt");
   if (n == 0) return MGCFD_OK;
+  VolPlan* plan = nullptr;
+  int r = vol_plan_get(vol, n, STREAM(s), &plan);
+  if (r) return r;
+  if (plan) return vol_plan_calculate_dt(plan, v, vol, dt, STREAM(s));
   k_calculate_dt<<<grid_for(n), kThreads, 0, STREAM(s)>>>(n, v, vol, dt);
   return launch_status("calculate_dt");
 }

@@ -99,6 +99,13 @@ struct ChildPlan {
   int64_t bytes = 0;
 };
 
+struct VolPlan {
+  int32_t n = 0;
+  double* vcopy = nullptr;  // [n] the volumes the roots were taken of (bits)
+  double* root = nullptr;   // [n] cbrt of those volumes
+  int64_t bytes = 0;
+};
+
 namespace {
 
 constexpr int kT = 256;
@@ -575,11 +582,12 @@ struct Key {
   }
 };
 
-enum { kEdgePlan = 0, kChildPlan = 1 };
+enum { kEdgePlan = 0, kChildPlan = 1, kVolPlan = 2 };
 
 std::mutex g_mu;
 std::map<Key, EdgePlan*> g_edge;
 std::map<Key, ChildPlan*> g_child;
+std::map<Key, VolPlan*> g_vol;
 int g_mode = MGCFD_PLANS_AUTO;
 std::atomic<int> g_flux_dw{0};  // mgcfd_op_flux_precision: DW form of the flux through plans
 
@@ -598,6 +606,17 @@ void free_child_plan(ChildPlan* P) {
   if (P->ch_list) cudaFree(P->ch_list);
   delete P;
 }
+
+void free_vol_plan(VolPlan* P) {
+  if (!P) return;
+  if (P->vcopy) cudaFree(P->vcopy);
+  if (P->root) cudaFree(P->root);
+  delete P;
+}
+
+void free_plan(EdgePlan* P) { free_edge_plan(P); }
+void free_plan(ChildPlan* P) { free_child_plan(P); }
+void free_plan(VolPlan* P) { free_vol_plan(P); }
 
 template <class F>
 int cub_call(Scratch& S, F&& f) {
@@ -824,6 +843,40 @@ int build_child_plan(const int32_t* map, int32_t nf, int32_t nc, cudaStream_t s,
   return MGCFD_OK;
 }
 
+// calculate_dt_kernel (time_stepping_kernels.h:13-32) with the volume's
+// cube root taken from the plan while the volume keeps the bits it had when
+// the root was taken (a bit compare per node), else computed and kept: the
+// same bits as cbrt on every call.  node_prim and the division stay per call.
+__global__ void k_plan_calculate_dt(int32_t n, const double* __restrict__ var, const double* __restrict__ vol,
+                                    double* __restrict__ vcopy, double* __restrict__ root, double* __restrict__ dt) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double v = vol[i];
+    double c;
+    if (__double_as_longlong(v) == __double_as_longlong(vcopy[i])) {
+      c = root[i];
+    } else {
+      c = cbrt(v);
+      root[i] = c;
+      vcopy[i] = v;
+    }
+    const double* x = var + 5 * i;
+    const NodePrim p = node_prim(x[0], x[1], x[2], x[3], x[4]);
+    dt[i] = 0.5 * (c / p.s);
+  }
+}
+
+// A volume plan starts with every copied volume and root set to the
+// all-ones bit pattern (a NaN): the first call takes every root, and a volume
+// with exactly those bits would read that NaN, as cbrt would give a NaN.
+int build_vol_plan(int32_t n, cudaStream_t s, VolPlan* P) {
+  int r;
+  P->n = n;
+  if ((r = plan_alloc(&P->vcopy, (size_t)n, &P->bytes)) || (r = plan_alloc(&P->root, (size_t)n, &P->bytes))) return r;
+  CK(cudaMemsetAsync(P->vcopy, 0xff, sizeof(double) * (size_t)n, s));
+  CK(cudaMemsetAsync(P->root, 0xff, sizeof(double) * (size_t)n, s));
+  return MGCFD_OK;
+}
+
 // Finds or builds a plan.  *out = nullptr (and MGCFD_OK) when plans are off,
 // or when none exists yet and the stream is capturing a graph.
 template <class P, class Build>
@@ -844,8 +897,7 @@ int get_plan(std::map<Key, P*>& cache, const Key& k, cudaStream_t s, Build build
   int r = build(p);
   if (r) {
     cudaStreamSynchronize(s);
-    if constexpr (std::is_same<P, EdgePlan>::value) free_edge_plan(p);
-    else free_child_plan(p);
+    free_plan(p);
     return r;
   }
   cache[k] = p;
@@ -941,6 +993,19 @@ int child_plan_up(ChildPlan* P, const double* fv, double* cv, int32_t* scratch, 
 
 bool edge_plan_permuted(const EdgePlan* P) { return P->permuted; }
 
+int vol_plan_get(const double* vol, int32_t n, cudaStream_t s, VolPlan** out) {
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  return get_plan(g_vol, Key{dev, vol, n, n, kVolPlan}, s, [&](VolPlan* p) { return build_vol_plan(n, s, p); },
+                  out);
+}
+
+int vol_plan_calculate_dt(VolPlan* P, const double* var, const double* vol, double* dt, cudaStream_t s) {
+  if (P->n > 0) k_plan_calculate_dt<<<grid(P->n), kT, 0, s>>>(P->n, var, vol, P->vcopy, P->root, dt);
+  CK(cudaGetLastError());
+  return MGCFD_OK;
+}
+
 }  // namespace mgcfd
 
 extern "C" int mgcfd_op_plans_mode(int32_t mode) {
@@ -963,8 +1028,10 @@ extern "C" int mgcfd_op_plans_release(void) {
   cudaError_t e = cudaDeviceSynchronize();
   for (auto& kv : mgcfd::g_edge) mgcfd::free_edge_plan(kv.second);
   for (auto& kv : mgcfd::g_child) mgcfd::free_child_plan(kv.second);
+  for (auto& kv : mgcfd::g_vol) mgcfd::free_vol_plan(kv.second);
   mgcfd::g_edge.clear();
   mgcfd::g_child.clear();
+  mgcfd::g_vol.clear();
   if (e != cudaSuccess) return mgcfd::set_error(MGCFD_ERR_CUDA, std::string("mgcfd_op_plans_release: ") + cudaGetErrorString(e));
   return MGCFD_OK;
 }
@@ -991,6 +1058,14 @@ extern "C" int mgcfd_op_plan_release(const void* map) {
       ++it;
     }
   }
+  for (auto it = mgcfd::g_vol.begin(); it != mgcfd::g_vol.end();) {
+    if (it->first.device == dev && it->first.map == map) {
+      mgcfd::free_vol_plan(it->second);
+      it = mgcfd::g_vol.erase(it);
+    } else {
+      ++it;
+    }
+  }
   return MGCFD_OK;
 }
 
@@ -1003,6 +1078,7 @@ extern "C" int mgcfd_op_plans_info(int64_t* edge_plans, int64_t* child_plans, in
     bytes += kv.second->bytes;
   }
   for (auto& kv : mgcfd::g_child) bytes += kv.second->bytes;
+  for (auto& kv : mgcfd::g_vol) bytes += kv.second->bytes;
   if (edge_plans) *edge_plans = (int64_t)mgcfd::g_edge.size();
   if (child_plans) *child_plans = (int64_t)mgcfd::g_child.size();
   if (reordered) *reordered = re;

@@ -1,5 +1,5 @@
-// Execution plans of the per-loop entry points (plans.cu): cached per map,
-// built on first use.  Internal to the library.
+// Execution plans of the per-loop entry points (plans.cu): cached per map
+// (or per vol dat), built on first use.  Internal to the library.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -23,5 +23,11 @@ int child_plan_get(const int32_t* map, int32_t nf, int32_t nc, cudaStream_t s, C
 // up_pre_kernel / up_kernel over the plan; *skipped = fine nodes out of range.
 int child_plan_up_pre(ChildPlan* P, double* cv, int32_t* scratch, cudaStream_t s, int64_t* skipped);
 int child_plan_up(ChildPlan* P, const double* fv, double* cv, int32_t* scratch, cudaStream_t s, int64_t* skipped);
+
+struct VolPlan;
+// calculate_dt_kernel's volume cube roots, cached per vol dat and checked
+// against the volumes' bits on every call.
+int vol_plan_get(const double* vol, int32_t n, cudaStream_t s, VolPlan** out);
+int vol_plan_calculate_dt(VolPlan* P, const double* var, const double* vol, double* dt, cudaStream_t s);
 
 }  // namespace mgcfd

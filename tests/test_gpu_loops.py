@@ -108,6 +108,43 @@ def test_dt_min_step_factor(case):
     assert host(md)[0] == np.finfo(np.float64).max
 
 
+def test_calculate_dt_volume_plan(case):
+    """calculate_dt through its volume plan (cube roots cached per vol dat,
+    checked against the volumes' bits) gives the plan-free kernel's bits on
+    the first call, on a repeat, and after volumes change in place."""
+    L0, ref = case["levels"][0], case["ref"]
+    n = L0.nnodes
+    vol = ref.get(0, O.Q_VOLUMES).copy()
+    v, vd = dev(case["var"]), dev(vol)
+
+    def run(mode):
+        ops.plans_mode(mode)
+        try:
+            dt = torch.empty(n, dtype=torch.float64, device="cuda")
+            ops.calculate_dt(n, v.data_ptr(), vd.data_ptr(), dt.data_ptr())
+            return host(dt)
+        finally:
+            ops.plans_mode("auto")
+
+    ops.plans_release()
+    free = run("off")
+    assert ops.plans_info()["device_bytes"] == 0
+    np.testing.assert_array_equal(run("auto"), free)
+    assert ops.plans_info()["device_bytes"] >= 16 * n
+    np.testing.assert_array_equal(run("auto"), free)
+    vd[::5] *= 1.5  # in place: the plan must notice the new bits
+    vd[3] = float("nan")
+    free2 = run("off")
+    got = run("auto")
+    np.testing.assert_array_equal(got, free2)
+    edt = np.empty(n)
+    O.lib().orc_loop_calculate_dt(n, dp(case["var"]), dp(host(vd)), dp(edt))
+    np.testing.assert_allclose(got, edt, rtol=1e-14)
+    assert not np.array_equal(got, free)
+    ops.plan_release(vd.data_ptr())
+    assert ops.plans_info()["device_bytes"] == 0
+
+
 @pytest.mark.parametrize("level", [0, 1])
 def test_flux_edge_and_boundary(case, level):
     L, ref, ff = case["levels"][level], case["ref"], case["ff"]
