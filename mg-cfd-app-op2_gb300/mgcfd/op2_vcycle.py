@@ -191,12 +191,13 @@ class LoopSolver:
         return self.L[level][what].cpu().numpy()
 
     def close(self):
-        """Release the plans built from this mesh's maps, then the dats."""
+        """Release the plans built from this mesh's maps and volume dats, then
+        the dats."""
         if not self.L:
             return
         self.stream.synchronize()
         for d in self.L:
-            for m in ("e2n", "n2mg"):
+            for m in ("e2n", "n2mg", "vol"):
                 if d.get(m) is not None:
                     ops.plan_release(d[m].data_ptr())
         self.L = []

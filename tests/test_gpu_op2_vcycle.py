@@ -37,6 +37,7 @@ def _run_loops(levels, cycles, mode, precision="fp64"):
     res0 = s.fetch(0, "res")
     info = ops.plans_info()
     s.close()
+    assert ops.plans_info()["device_bytes"] == 0  # close() releases every plan it built
     ops.plans_mode("auto")
     ops.flux_precision("fp64")
     return st, rms, out, res0, info
