@@ -322,7 +322,7 @@ def run_gb300(args):
             dist.destroy_process_group()
         return
     line = {
-        "metric": "MG V-cycles/s at 8M nodes (200^3, 4 levels)",
+        "metric": metric_name(args, N),
         "value": round(value, 3),
         "unit": "cycles/s",
         "n_gpus": world,
@@ -333,7 +333,7 @@ def run_gb300(args):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": {"fp64": "f64", "mixed": "f32-flux/f64-accumulate", "dw": "f32x2-flux/f64"}[args.precision],
-        "data": "synthetic: seeded jittered 200^3 lattice, permuted ids",
+        "data": data_words(args),
         "config": line_config(args, N, E),
         "variant": {"increment": inc, "renumber": args.renumber,
                     "accumulation": args.accumulation if args.precision == "mixed" else "fp64",
@@ -375,6 +375,21 @@ def line_config(args, N, E):
     return {"workload": f"{args.n}^3 jittered lattice, {NLEVELS} levels, Mach {MACH}, AoA {AOA} deg, "
                         f"{N} nodes / {E} edges on level 0",
             "precision": args.precision, "l2": l2}
+
+
+def node_count_words(N):
+    """8000000 -> "8M"; other counts with thousands separators."""
+    return f"{N // 10**6}M" if N >= 10**6 and N % 10**6 == 0 else f"{N:,}"
+
+
+def metric_name(args, N, where=None):
+    """The line's metric: "MG V-cycles/s at 8M nodes (200^3, 4 levels)" for the default workload."""
+    base = f"MG V-cycles/s at {node_count_words(N)} nodes"
+    return f"{base} ({args.n}^3, {NLEVELS} levels)" if where is None else f"{base} {where}"
+
+
+def data_words(args):
+    return f"synthetic: seeded jittered {args.n}^3 lattice, permuted ids"
 
 
 def fp64_reference(mesh, stream, cycles):
@@ -648,11 +663,11 @@ def run_reference(args):
     L0 = levels[0]
     line = {
         "impl": "reference",
-        "metric": "MG V-cycles/s at 8M nodes (200^3, 4 levels)",
+        "metric": metric_name(args, L0.nnodes),
         "value": round(value, 4), "unit": "cycles/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(1e3 * secs / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic: seeded jittered 200^3 lattice, permuted ids",
+        "data": data_words(args),
         "config": line_config(args, L0.nnodes, L0.nedges),
         "implementation": "CPU restatement of the reference path (oracle/mgcfd_oracle.c), OpenMP over coloured edges",
         "cpu_baseline": {"value": round(value, 4), "unit": "cycles/s", "cores": threads, "kind": "port",
@@ -918,9 +933,9 @@ def run_loops(args):
     solver_flux_ms = kernel_times(mesh, args.kernel_cycles)
     for name in forms:
         out[name]["flux_call_vs_solver_flux"] = round(out[name]["flux_call_ms"] / solver_flux_ms, 3)
-    line = {"metric": "MG V-cycles/s at 8M nodes through the per-loop entry points (OP2 dat layout)",
+    line = {"metric": metric_name(args, N, "through the per-loop entry points (OP2 dat layout)"),
             "unit": "cycles/s", "higher_is_better": True, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-            "data": "synthetic: seeded jittered 200^3 lattice, permuted ids",
+            "data": data_words(args),
             "config": line_config(args, N, E),
             "value": out.get("file_order", {}).get("value"), "forms": out,
             "device_solver": {"value": round(solver_value, 3), "unit": "cycles/s",
