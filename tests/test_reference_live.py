@@ -70,3 +70,39 @@ def test_legacy_mode_files(tmp_path):
         b = mgcfd.h5_read(tmp_path / f"b.variables.L{l}.cycles=2.h5", f"p_variables_result_L{l}")
         np.testing.assert_array_equal(a, b)
         np.testing.assert_array_equal(run.get(l, O.Q_VARIABLES), b)
+
+
+def test_reference_solution_unchanged_by_flipped_edges(tmp_path):
+    """The reference itself, on a mesh whose edges are partly stored end for
+    end: calculate_cell_volumes (misc.h:40-76) uses each input weight's
+    magnitude only and re-derives its direction from b - a, and flux.h:41-208
+    mirrors end a's expressions for end b, so the solution is the same bit
+    for bit.  This is the identity behind the device tables' a < b
+    orientation and the node-centric stages (each edge evaluated from either
+    end)."""
+    mesh = mgcfd.HostMesh.generate(9, 2, 8)
+    levels = mesh.levels()
+    rng = np.random.default_rng(2)
+    flipped = []
+    for L in levels:
+        flip = rng.random(L.nedges) < 0.5
+        e2n = np.array(L.edge_to_nodes, dtype=np.int32, copy=True)
+        e2n[flip] = e2n[flip][:, ::-1]
+        w = np.array(L.edge_weights, copy=True)
+        w[flip] = -w[flip]  # any sign: only |w| is read
+        flipped.append(mgcfd.Level(coords=np.array(L.coords), edge_to_nodes=np.ascontiguousarray(e2n),
+                                   bnd_to_node=np.array(L.bnd_to_node), bnd_group=np.array(L.bnd_group),
+                                   edge_weights=np.ascontiguousarray(w), bnd_weights=np.array(L.bnd_weights),
+                                   node_to_mg=None if L.node_to_mg is None else np.array(L.node_to_mg),
+                                   n_axis=L.n_axis))
+    (tmp_path / "a").mkdir()
+    (tmp_path / "b").mkdir()
+    mesh.write(str(tmp_path / "a"), "m_")
+    mgcfd.HostMesh.from_levels(flipped).write(str(tmp_path / "b"), "m_")
+    for d in ("a", "b"):
+        r = O.run_reference_binary(tmp_path / d, 3, 0.7, 2.0)
+        assert r.returncode == 0, r.stderr
+    for l in range(len(levels)):
+        a = mgcfd.h5_read(tmp_path / "a" / f"solution.variables.L{l}.cycles=3.h5", f"p_variables_result_L{l}")
+        b = mgcfd.h5_read(tmp_path / "b" / f"solution.variables.L{l}.cycles=3.h5", f"p_variables_result_L{l}")
+        np.testing.assert_array_equal(a, b)
